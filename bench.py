@@ -1,0 +1,338 @@
+"""Benchmark of the Livre rendering hot path on GB300.
+
+Workload (the plain path at scale): a 2048^3 uint8 blob volume (256 blobs,
+noise +-8) in 64^3 bricks with a 1-voxel overlap (6 LOD levels), rendered at
+1920x1080 along a 64-frame orbit at 2.5x the volume diagonal, 256-entry RGBA
+float32 transfer function with 4 Gaussian peaks, LOD threshold 2 px, step
+0.5 voxel of the finest rendered level, trilinear sampling, early ray
+termination at alpha 0.99.
+
+One step = one frame of one view: LOD selection, residency (brick streaming
+on a miss), leaf grid, ray cast. `value` is frames/s with every brick the
+orbit needs already resident in HBM, timed per frame with CUDA events on the
+rendering stream after an L2 flush (a 256 MiB write). `e2e` is the same
+metric through the public C ABI with host buffers: the brick pool starts
+empty, bricks stream host->device from a page-locked host store on a miss,
+and each frame is converted to RGBA8 and copied back to host memory.
+
+`--impl reference` times the CPU restatement of the reference path (the
+reference itself needs an OpenGL context and cannot run here): the FP32 LOD
+selection single-threaded as on the reference render thread, plus the FP64
+ray cast on every host thread over a bounded sample of rows of the same
+frame, extrapolated to the full frame.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "plain2048": dict(workload="plain_2048c_u8_64b_1080p_orbit64", voxels=2048, block=64,
+                      overlap=1, n_blobs=256, noise=8, seed=2, width=1920, height=1080,
+                      frames=64, sse=2.0, early=0.99, tf_entries=256, tf_seed=4,
+                      pool_gib=24),
+    "plain256": dict(workload="plain_256c_u8_32b_512sq_orbit64", voxels=256, block=32,
+                     overlap=1, n_blobs=16, noise=0, seed=1, width=512, height=512,
+                     frames=64, sse=1.0, early=0.999, tf_entries=256, tf_seed=None,
+                     pool_gib=1),
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=64)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--config", default="plain2048", choices=sorted(CONFIGS))
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-rows", type=int, default=12)
+    return p.parse_args()
+
+
+def transfer_function(cfg):
+    import livre_gb300 as lv
+    if cfg["tf_seed"] is None:
+        return lv.linear_ramp_tf(cfg["tf_entries"])
+    return lv.gaussian_peaks_tf(cfg["tf_entries"], seed=cfg["tf_seed"])
+
+
+def cameras(cfg, world_size):
+    import livre_gb300 as lv
+    return [lv.orbit_camera(k, cfg["frames"], world_size, cfg["width"], cfg["height"])
+            for k in range(cfg["frames"])]
+
+
+# ------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        import statistics
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# ------------------------------------------------------ CPU baseline
+def cpu_frame_estimate(cfg, k=0, rows=12):
+    """Seconds per frame of the CPU restatement: LOD selection (1 thread) +
+    FP64 ray cast (all threads) of `rows` evenly spaced rows, extrapolated."""
+    import concurrent.futures as cf
+    import numpy as np
+    import livre_gb300 as lv
+    from oracle import pyoracle as O
+
+    W, H = cfg["width"], cfg["height"]
+    ovol = O.volume(cfg["voxels"], cfg["block"], cfg["overlap"])
+    mv, proj = lv.orbit_camera(k, cfg["frames"], tuple(ovol.world_size), W, H)
+    t0 = time.perf_counter()
+    ids, _ = O.select_visible(ovol, mv, proj, H, cfg["sse"])
+    t_lod = time.perf_counter() - t0
+    bp = O.blob_params(cfg["n_blobs"], cfg["seed"], cfg["noise"], 1)
+    with cf.ThreadPoolExecutor(os.cpu_count()) as ex:
+        bricks = np.stack(list(ex.map(lambda i: O.blob_brick(ovol, bp, int(i)), ids)))
+    max_level = max(int(i) & 0xF for i in ids)
+    n_samples = (2 * cfg["voxels"]) >> (ovol.depth - 1 - max_level)
+    view = O.make_view(mv, proj, W, H, n_samples, early_exit=cfg["early"])
+    tf = transfer_function(cfg)
+    picks = [int((j + 0.5) * H / rows) for j in range(rows)]
+    t0 = time.perf_counter()
+    for y in picks:
+        O.raycast(ovol, 1, ids, bricks, tf, view, rows=(y, y + 1))
+    t_rows = time.perf_counter() - t0
+    return t_lod + t_rows * H / rows, t_lod, t_rows
+
+
+def reference_arm(args, cfg):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import build as ob
+    ob.build()
+    times = []
+    for s in range(args.warmup + args.steps):
+        sec, t_lod, t_rows = cpu_frame_estimate(cfg, k=s % cfg["frames"], rows=args.cpu_rows)
+        if s >= args.warmup:
+            times.append(sec)
+    ms = 1000.0 * sum(times) / len(times)
+    fps = 1000.0 / ms
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": cfg["workload"], "note": "CPU restatement of the reference "
+                       "path (the reference renders through OpenGL, unavailable on this box)"},
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
+                             "sample": "per step: full-frame FP32 LOD selection (1 thread) + "
+                                       "FP64 ray cast of %d evenly spaced rows (all threads), "
+                                       "extrapolated to %d rows" % (args.cpu_rows, cfg["height"])},
+            "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ GPU arm
+def gb300_arm(args, cfg):
+    import numpy as np
+    import torch
+    import livre_gb300 as lv
+    from livre_gb300 import build as nb
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    nb.build()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    W, H = cfg["width"], cfg["height"]
+
+    ctx = lv.Context(local, pool_bytes=cfg["pool_gib"] << 30)
+    vi = lv.VolumeInformation(cfg["voxels"], cfg["block"], cfg["overlap"])
+    t0 = time.time()
+    vol = ctx.blob_volume(vi, cfg["n_blobs"], cfg["seed"], cfg["noise"], placement=lv.BLOB_HOST)
+    gen_s = time.time() - t0
+    tf = ctx.transfer_function(transfer_function(cfg))
+    cams = cameras(cfg, vi.world_size)
+    descs = [ctx.render_desc(mv, pr, W, H, sse=cfg["sse"], early_exit=cfg["early"],
+                             step_policy=lv.STEP_HALF_VOXEL, filt=lv.FILTER_TRILINEAR,
+                             synchronous=True) for mv, pr in cams]
+    my_frames = [k for k in range(cfg["frames"]) if k % world == rank] or [0]
+    out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    out8 = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
+    host8 = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def frame_of(i):
+        return my_frames[i % len(my_frames)]
+
+    # ---- e2e: cold pool, bricks streamed from the host store, RGBA8 back
+    for i in range(args.warmup):
+        ctx.render(vol, tf, descs[frame_of(i)], out)
+        ctx.last_stats()
+    ctx.purge()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    e2e_t, h2d, launches_e2e = [], 0, 0
+    for i in range(args.steps):
+        t1 = time.perf_counter()
+        ctx.render(vol, tf, descs[frame_of(i)], out)
+        ctx.to_rgba8(out, out8)
+        host8.copy_(out8, non_blocking=True)
+        stream.synchronize()
+        e2e_t.append(time.perf_counter() - t1)
+        st = ctx.last_stats()
+        h2d += st["bytes_uploaded"]
+        launches_e2e += st["n_launches"] + 1
+    e2e_total = sum(e2e_t)
+
+    # ---- value: every brick of the orbit resident, L2 flushed between frames
+    for k in my_frames:
+        ctx.render(vol, tf, descs[k], out)
+    ctx.last_stats()
+    for i in range(args.warmup):
+        ctx.render(vol, tf, descs[frame_of(i)], out)
+        ctx.last_stats()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    stats = []
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clocks:
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            ev0[i].record(stream)
+            ctx.render(vol, tf, descs[frame_of(i)], out)
+            ev1[i].record(stream)
+            stats.append(ctx.last_stats())
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    if dist:
+        dist.barrier()
+    frame_ms = np.array([a.elapsed_time(b) for a, b in zip(ev0, ev1)])
+    total_ms = float(frame_ms.sum())
+    if dist:
+        t = torch.tensor([total_ms, e2e_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_total = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+    frames_all = args.steps * world
+    value = frames_all / (total_ms / 1000.0)
+    ray_ms = np.array([s["raycast_ms"] for s in stats])
+    n_samples = np.array([s["n_samples"] for s in stats], dtype=np.float64)
+    bpv = vi.bytes_per_voxel
+    alg_bytes = n_samples * 8 * bpv + W * H * 16
+    achieved = float(alg_bytes.sum() / (ray_ms.sum() / 1000.0) / 1e9)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    line = {
+        "metric": "frames/s", "value": value, "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": cfg["workload"], "volume": "%d^3 u8" % cfg["voxels"],
+                   "brick": "%d^3 + overlap %d" % (cfg["block"], cfg["overlap"]),
+                   "viewport": "%dx%d" % (W, H), "frames": cfg["frames"], "lod_px": cfg["sse"],
+                   "step": "0.5 voxel of finest rendered level", "filter": "trilinear",
+                   "early_exit": cfg["early"], "tf": "%d-entry RGBA f32" % cfg["tf_entries"],
+                   "mode": "plain per-view launch (synchronous residency)",
+                   "l2": "flushed between frames (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "p50_ms": float(np.percentile(frame_ms, 50)), "p99_ms": float(np.percentile(frame_ms, 99)),
+        "samples_per_s": float(n_samples.sum() / (total_ms / 1000.0)),
+        "wall_s": wall, "volume_generation_s": gen_s,
+        "gpu_launches": int(sum(s["n_launches"] for s in stats)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "raycast_kernel<u8,trilinear>",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800"},
+        "e2e": {"value": args.steps * world / e2e_total, "unit": "frames/s",
+                "h2d_bytes_per_step": int(h2d / args.steps),
+                "d2h_bytes_per_step": W * H * 4,
+                "note": "pool purged before the timed steps; bricks streamed from pinned host "
+                        "memory; RGBA8 frame copied to host every step"},
+        "e2e_gpu_launches": launches_e2e,
+        "clocks": clocks.summary(),
+        "visible_bricks_mean": float(np.mean([s["n_visible"] for s in stats])),
+        "samples_per_ray": int(stats[-1]["samples_per_ray"]),
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        sec, t_lod, t_rows = cpu_frame_estimate(cfg, k=0, rows=args.cpu_rows)
+        line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "frames/s", "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": "frame 0: FP32 LOD selection (1 thread, %.3f s) + FP64 "
+                                          "ray cast of %d evenly spaced rows on all threads "
+                                          "(%.2f s), extrapolated to %d rows"
+                                          % (t_lod, args.cpu_rows, t_rows, H)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        reference_arm(args, cfg)
+    else:
+        gb300_arm(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,276 @@
+/*
+ * livre_gb300: GB300-native (sm_103a) implementation of Livre's rendering hot
+ * path behind a C ABI: octree LOD + frustum brick selection, a device-resident
+ * HBM brick pool with an LRU page table fed from host memory, and
+ * front-to-back ray-cast compositing with a 1D RGBA transfer function.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and returns
+ * an lv_status. Device buffers passed in (d_*) are CUDA device pointers owned
+ * by the caller; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * The library owns the brick pool, page tables and transfer-function copies.
+ * A context is used by one host thread at a time (or externally serialised).
+ *
+ * Reference interfaces (paths inside BlueBrain/Livre) are cited per entry.
+ */
+#ifndef LIVRE_GB300_H
+#define LIVRE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LV_ABI_VERSION 1
+
+typedef enum lv_status
+{
+    LV_OK = 0,
+    LV_EINVAL = 1,    /* invalid argument */
+    LV_ENOMEM = 2,    /* device/host allocation failed or capacity exceeded */
+    LV_ETIMEDOUT = 3, /* a bounded device wait gave up */
+    LV_EDEVICE = 4,   /* CUDA error */
+    LV_ENOTFOUND = 5, /* data source returned no data for a node */
+    LV_EAGAIN = 6     /* resource busy (pool full of bricks in use) */
+} lv_status;
+
+/* Voxel types, same order as livre::DataType (livre/data/VolumeInformation.h:31-41). */
+typedef enum lv_dtype
+{
+    LV_DT_FLOAT = 0,
+    LV_DT_UINT8 = 1,
+    LV_DT_UINT16 = 2,
+    LV_DT_UINT32 = 3,
+    LV_DT_INT8 = 4,
+    LV_DT_INT16 = 5,
+    LV_DT_INT32 = 6
+} lv_dtype;
+
+/* livre::VolumeInformation (livre/data/VolumeInformation.h:42-111). The caller
+ * fills voxels, max_block (maximumBlockSize = block + 2 * overlap), overlap,
+ * dtype and comp_count; lv_fill_regular_volume_info derives the rest. */
+typedef struct lv_volume_info
+{
+    uint32_t voxels[3];
+    uint32_t max_block[3];
+    uint32_t overlap[3];
+    uint32_t dtype;
+    uint32_t comp_count;
+    float world_space_per_voxel;
+    float world_size[3];
+    uint32_t depth;          /* RootNode::getDepth() */
+    uint32_t root_blocks[3]; /* RootNode::getBlockSize(0) */
+} lv_volume_info;
+
+/* Replaces livre::fillRegularVolumeInfo (livre/data/DataSourcePlugin.cpp:73-95). */
+lv_status lv_fill_regular_volume_info(lv_volume_info* info);
+
+/* livre::Frustum(modelView, projection) (livre/data/Frustum.h:46-47):
+ * 4x4 matrices stored column-major like vmml::Matrix4f::array. */
+typedef struct lv_camera
+{
+    float modelview[16];
+    float projection[16];
+} lv_camera;
+
+/* Inputs of SelectVisibles (livre/data/SelectVisibles.h:44-47) as wired by
+ * VisibleSetGeneratorFilter::execute (livre/lib/pipeline/
+ * VisibleSetGeneratorFilter.cpp:40-66). */
+typedef struct lv_lod_params
+{
+    uint32_t window_height;   /* pixel viewport height (vp[3]) */
+    float screen_space_error; /* VolumeRendererParameters screen_space_error */
+    uint32_t min_lod;
+    uint32_t max_lod;
+    float range[2];           /* sort-last data range, {0, 1} on one GPU */
+    uint32_t time_step;
+    uint32_t n_clip_planes;   /* <= 6; plane (n, d) keeps n.p + d >= 0 */
+    float clip_planes[6][4];
+} lv_lod_params;
+
+/* Result words written by lv_select_visible into d_result[LV_SELECT_RESULT_WORDS]. */
+enum
+{
+    LV_SEL_WRITTEN = 0,   /* ids written to d_out_ids (<= capacity) */
+    LV_SEL_FOUND = 1,     /* visible ids found (after the range slice) */
+    LV_SEL_VISITED = 2,   /* octree nodes visited */
+    LV_SEL_MAX_LEVEL = 3, /* finest level among the visible ids */
+    LV_SEL_OVERFLOW = 4,  /* nonzero: a traversal frontier overflowed */
+    LV_SELECT_RESULT_WORDS = 8
+};
+
+typedef struct lv_ctx lv_ctx;
+typedef struct lv_volume lv_volume;
+typedef struct lv_tf lv_tf;
+
+/* Context on one CUDA device. Not in the reference (GL context + caches of
+ * livre/eq/Window.cpp:54-72 play this role). */
+lv_status lv_ctx_create(int device, lv_ctx** out);
+void lv_ctx_destroy(lv_ctx* ctx);
+/* Last error message of this context ("" when none). */
+const char* lv_last_error(const lv_ctx* ctx);
+/* Library ABI version and the CUDA architecture it was built for. */
+uint32_t lv_abi_version(void);
+
+/* LOD selection on the device. Replaces DFSTraversal::traverse(rootNode,
+ * SelectVisibles, timeStep) (livre/data/DFSTraversal.cpp:63-76 with
+ * livre/data/SelectVisibles.cpp:45-131). The visible NodeIds are bit-exact to
+ * the reference's FP32 selection; they are written level by level (the
+ * reference's DFS order is restored only when the range slice needs it).
+ * d_out_ids: capacity uint64 device slots; d_result: LV_SELECT_RESULT_WORDS
+ * uint32 device words. Asynchronous on `stream`. Scratch (frontier queues) is
+ * allocated by the context on first use and reused. */
+lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
+                            const lv_camera* camera,
+                            const lv_lod_params* params, uint64_t* d_out_ids,
+                            uint32_t capacity, uint32_t* d_result,
+                            void* stream);
+
+/* ---------------------------------------------------------- brick pool */
+
+/* Device brick pool budget in bytes (VolumeRendererParameters
+ * max_gpu_cache_memory, livre/lib/zeroeq/volumeRendererParameters.fbs:9;
+ * Cache byte budget, livre/core/cache/Cache.cpp:41-96). Must be called before
+ * the first volume is created. Default: 3072 MiB. */
+lv_status lv_pool_configure(lv_ctx* ctx, size_t bytes);
+/* Drops every resident brick (Cache::purge, livre/core/cache/Cache.cpp:186-192). */
+lv_status lv_pool_purge(lv_ctx* ctx);
+
+/* livre::DataSourcePlugin::getData (livre/data/DataSourcePlugin.h:81) as a C
+ * callback: fill `dst` (page-locked host memory, `bytes` long: the node's
+ * (block + 2 * overlap)^3 voxels, x fastest) for `node_id` and return 0, or
+ * return nonzero for a null MemoryUnitPtr. Called from library worker
+ * threads; must be thread-safe like the reference plugin contract. */
+typedef int (*lv_get_data_fn)(void* user, uint64_t node_id, void* dst,
+                              size_t bytes);
+
+/* A volume whose bricks come from a data-source callback (plugin). */
+lv_status lv_volume_create(lv_ctx* ctx, const lv_volume_info* info,
+                           lv_get_data_fn get_data, void* user,
+                           lv_volume** out);
+
+/* Synthetic blob volume: sum of n_blobs isotropic Gaussians (centres uniform
+ * in the volume, sigma U[8,32] voxels, amplitude U[0.3,1], cut off at
+ * 6 sigma) plus integer noise U[-noise, noise], from `seed`. */
+typedef struct lv_blob_desc
+{
+    uint32_t n_blobs;
+    uint32_t noise;
+    uint64_t seed;
+} lv_blob_desc;
+
+/* Where the bricks of a blob volume live before they are needed. */
+enum
+{
+    LV_BLOB_DEVICE = 0, /* generated on the device, straight into the pool */
+    LV_BLOB_HOST = 1    /* generated once into page-locked host memory and
+                           streamed host->device on a miss */
+};
+lv_status lv_volume_create_blob(lv_ctx* ctx, const lv_volume_info* info,
+                                const lv_blob_desc* blob, uint32_t placement,
+                                lv_volume** out);
+void lv_volume_destroy(lv_volume* vol);
+/* The derived VolumeInformation of a volume. */
+lv_status lv_volume_get_info(const lv_volume* vol, lv_volume_info* out);
+
+/* Loads the bricks `ids` (host array) of `vol` into the pool now, evicting
+ * the oldest resident bricks when it is full, like Cache::load<TextureObject>
+ * (livre/core/cache/Cache.cpp:111-123) driven by DataUploadFilter::load
+ * (livre/lib/pipeline/DataUploadFilter.cpp:45-77). Already resident ids are
+ * hits and keep their place in the eviction order. Synchronous. */
+lv_status lv_volume_load(lv_volume* vol, const uint64_t* ids, uint32_t n,
+                         uint32_t* n_loaded);
+/* Resident node ids of `vol` in eviction order (oldest load first), like
+ * the LRU queue of livre/core/cache/Cache.cpp:41-96. */
+lv_status lv_volume_resident(const lv_volume* vol, uint64_t* ids,
+                             uint32_t capacity, uint32_t* n);
+
+/* Generates blob bricks for `n` node ids (host array `ids`) into d_out (n
+ * bricks of max_block^3 voxels, x fastest) on the device. */
+lv_status lv_blob_generate(lv_ctx* ctx, const lv_volume_info* info,
+                           const lv_blob_desc* blob, const uint64_t* ids,
+                           uint32_t n, void* d_out, void* stream);
+
+/* ------------------------------------------------------ transfer function */
+
+/* A resident 1D RGBA transfer function of n float entries (host rgba, 4*n
+ * floats). Replaces the GL_RGBA8 1D texture of
+ * livre/eq/render/RayCastRenderer.cpp:175-193; sampled with linear filtering
+ * and clamp-to-edge. */
+lv_status lv_tf_create(lv_ctx* ctx, const float* rgba, uint32_t n,
+                       lv_tf** out);
+void lv_tf_destroy(lv_tf* tf);
+
+/* ----------------------------------------------------------- rendering */
+
+enum
+{
+    LV_FILTER_NEAREST = 0,
+    LV_FILTER_TRILINEAR = 1
+};
+enum
+{
+    LV_STEP_REFERENCE = 0, /* max(maxVoxels >> (depth-1-L), 512) per unit
+                              (livre/eq/render/RayCastRenderer.cpp:216-233) */
+    LV_STEP_HALF_VOXEL = 1 /* 0.5 voxel of the finest rendered level */
+};
+
+typedef struct lv_render_desc
+{
+    lv_camera camera;
+    uint32_t width, height;    /* pixel viewport */
+    lv_lod_params lod;         /* window_height is taken from `height` if 0 */
+    uint32_t samples_per_ray;  /* 0 = from step_policy */
+    uint32_t step_policy;
+    float early_exit;          /* 0.999 in fragRayCast.glsl:12 */
+    uint32_t filter;
+    float data_range[2];       /* dataSourceRange; hi <= lo: dtype range */
+    uint32_t synchronous;      /* 1: stream every missing brick first
+                                  (RenderPipeline::renderSync); 0: render the
+                                  nearest resident ancestors and stream up to
+                                  max_uploads misses (renderAsync) */
+    uint32_t max_uploads;      /* async mode only; reference: 1 per frame */
+} lv_render_desc;
+
+typedef struct lv_frame_stats
+{
+    uint32_t n_visible;       /* visible set size */
+    uint32_t n_rendered;      /* rendering set size (after ancestor fallback) */
+    uint32_t n_available;     /* NodeAvailability::nAvailable */
+    uint32_t n_not_available; /* NodeAvailability::nNotAvailable */
+    uint32_t n_visited;       /* octree nodes visited by the selection */
+    uint32_t max_level;       /* finest level rendered */
+    uint32_t samples_per_ray; /* nSamplesPerRay used */
+    uint32_t n_uploaded;      /* bricks streamed into the pool */
+    uint64_t n_samples;       /* composited samples */
+    uint64_t bytes_uploaded;  /* host->device brick bytes */
+    uint32_t n_launches;      /* kernels this library launched for the frame */
+    float select_ms;          /* device time of the LOD selection */
+    float raycast_ms;         /* device time of the ray-cast kernel */
+} lv_frame_stats;
+
+/* One frame of one view: LOD selection, brick residency (streaming misses
+ * from the volume's source into the pool), and the ray cast into d_rgba
+ * (width*height float RGBA, row 0 at the bottom, premultiplied colour as the
+ * reference's RGBA32F render texture holds it). Replaces
+ * RenderPipeline::render (livre/lib/pipeline/RenderPipeline.cpp:268-278) with
+ * Renderer::render (livre/core/render/Renderer.cpp:33-47) and the
+ * RayCastRenderer shaders. Returns once the frame is enqueued on `stream`. */
+lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
+                    const lv_render_desc* desc, float* d_rgba, void* stream);
+
+/* Statistics of the last lv_render / lv_render_batch call (synchronises with
+ * its stream). */
+lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out);
+
+/* RGBA32F -> RGBA8 (alpha forced to 255 like the framebuffer copy of
+ * livre/eq/render/shaders/fragTexCopy.glsl:11-15 onto the RGB window of
+ * livre/eq/Window.cpp:122-124), truncating x * 255 after clamping to [0,1]. */
+lv_status lv_frame_to_rgba8(lv_ctx* ctx, const float* d_rgba, uint32_t width,
+                            uint32_t height, uint8_t* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,599 @@
+/*
+ * Octree LOD + frustum brick selection on the device.
+ *
+ * Replaces the recursive CPU traversal of livre/data/DFSTraversal.cpp:29-76
+ * driving livre/data/SelectVisibles.cpp:45-131 with a level-synchronous,
+ * warp-cooperative traversal: each level is one launch over a device
+ * frontier; a node is culled (frustum / clip planes), emitted (LOD visible)
+ * or replaced by its 8 children in the next frontier. Emission and child
+ * pushes are warp-aggregated (ballot / match + one atomic per group) and
+ * compact the output without a separate prefix-sum pass.
+ *
+ * Bit-exactness: every float operation of a node visit is an explicit IEEE
+ * round-to-nearest intrinsic (__fadd_rn, __fmul_rn, __fdiv_rn), in the same
+ * order as the reference's FP32 code, so no FMA contraction can change a
+ * decision. Per-frame constants (planes, limits, eye) are computed once on
+ * the host with the same single-precision formulas.
+ */
+#include <algorithm>
+#include <cmath>
+
+#include "lv_runtime.h"
+
+namespace lv
+{
+namespace
+{
+/* ------------------------------------------------------------- host math */
+inline float Mh(const float* m, int r, int c) { return m[c * 4 + r]; }
+
+/* 4x4 inverse by Laplace expansion along the first two rows (2x2 minors). */
+bool inverse4(const float* m, float* inv)
+{
+    const float m00 = Mh(m, 0, 0), m01 = Mh(m, 0, 1), m02 = Mh(m, 0, 2),
+                m03 = Mh(m, 0, 3);
+    const float m10 = Mh(m, 1, 0), m11 = Mh(m, 1, 1), m12 = Mh(m, 1, 2),
+                m13 = Mh(m, 1, 3);
+    const float m20 = Mh(m, 2, 0), m21 = Mh(m, 2, 1), m22 = Mh(m, 2, 2),
+                m23 = Mh(m, 2, 3);
+    const float m30 = Mh(m, 3, 0), m31 = Mh(m, 3, 1), m32 = Mh(m, 3, 2),
+                m33 = Mh(m, 3, 3);
+    const float s0 = m00 * m11 - m10 * m01;
+    const float s1 = m00 * m12 - m10 * m02;
+    const float s2 = m00 * m13 - m10 * m03;
+    const float s3 = m01 * m12 - m11 * m02;
+    const float s4 = m01 * m13 - m11 * m03;
+    const float s5 = m02 * m13 - m12 * m03;
+    const float c5 = m22 * m33 - m32 * m23;
+    const float c4 = m21 * m33 - m31 * m23;
+    const float c3 = m21 * m32 - m31 * m22;
+    const float c2 = m20 * m33 - m30 * m23;
+    const float c1 = m20 * m32 - m30 * m22;
+    const float c0 = m20 * m31 - m30 * m21;
+    const float det =
+        s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    if (det == 0.0f || !std::isfinite(det))
+        return false;
+    const float id = 1.0f / det;
+    const float r[4][4] = {
+        {(m11 * c5 - m12 * c4 + m13 * c3) * id,
+         (-m01 * c5 + m02 * c4 - m03 * c3) * id,
+         (m31 * s5 - m32 * s4 + m33 * s3) * id,
+         (-m21 * s5 + m22 * s4 - m23 * s3) * id},
+        {(-m10 * c5 + m12 * c2 - m13 * c1) * id,
+         (m00 * c5 - m02 * c2 + m03 * c1) * id,
+         (-m30 * s5 + m32 * s2 - m33 * s1) * id,
+         (m20 * s5 - m22 * s2 + m23 * s1) * id},
+        {(m10 * c4 - m11 * c2 + m13 * c0) * id,
+         (-m00 * c4 + m01 * c2 - m03 * c0) * id,
+         (m30 * s4 - m31 * s2 + m33 * s0) * id,
+         (-m20 * s4 + m21 * s2 - m23 * s0) * id},
+        {(-m10 * c3 + m11 * c1 - m12 * c0) * id,
+         (m00 * c3 - m01 * c1 + m02 * c0) * id,
+         (-m30 * s3 + m31 * s1 - m32 * s0) * id,
+         (m20 * s3 - m21 * s1 + m22 * s0) * id}};
+    for (int rr = 0; rr < 4; ++rr)
+        for (int cc = 0; cc < 4; ++cc)
+            inv[cc * 4 + rr] = r[rr][cc];
+    return true;
+}
+
+/* ---------------------------------------------------------- device math */
+__device__ __forceinline__ float pdot(const float* pl, const float* p)
+{
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(pl[0], p[0]),
+                                         __fmul_rn(pl[1], p[1])),
+                               __fmul_rn(pl[2], p[2])),
+                     pl[3]);
+}
+
+__device__ __forceinline__ bool outside(const float* pl, const float* bmin,
+                                        const float* bmax)
+{
+    float pv[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        pv[i] = pl[i] >= 0.0f ? bmax[i] : bmin[i];
+    return pdot(pl, pv) < 0.0f;
+}
+
+/* 0 = culled, 1 = emit (LOD visible), 2 = descend. SelectVisibles.cpp:66-107 */
+__device__ int visit(const LodView& V, uint64_t id)
+{
+    const uint32_t L = nid_level(id);
+    uint32_t bm = V.root_blocks[0] << L;
+    bm = max(bm, V.root_blocks[1] << L);
+    bm = max(bm, V.root_blocks[2] << L);
+    const float denom = __uint2float_rn(bm);
+    const uint32_t pos[3] = {nid_x(id), nid_y(id), nid_z(id)};
+    float bmin[3], bmax[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        const float cmin = __fdiv_rn(__int2float_rn(int(pos[a])), denom);
+        const float cmax = __fdiv_rn(__int2float_rn(int(pos[a] + 1u)), denom);
+        bmin[a] = __fsub_rn(__fmul_rn(cmin, V.world_size[a]), V.half[a]);
+        bmax[a] = __fsub_rn(__fmul_rn(cmax, V.world_size[a]), V.half[a]);
+    }
+#pragma unroll
+    for (int p = 0; p < 6; ++p)
+        if (outside(V.planes[p], bmin, bmax))
+            return 0;
+    for (uint32_t c = 0; c < V.n_clip; ++c)
+        if (outside(V.clip[c], bmin, bmax))
+            return 0;
+
+    const float* np = V.planes[4];
+    float vmin[3], vmax[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        const bool pos_n = np[i] >= 0.0f;
+        vmin[i] = pos_n ? bmin[i] : bmax[i];
+        vmax[i] = pos_n ? bmax[i] : bmin[i];
+    }
+    if (pdot(np, vmin) < 0.0f || pdot(np, vmax) < 0.0f)
+    {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            vmin[i] = V.eye_near[i];
+    }
+    float wspv = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        const float w = __fdiv_rn(__fsub_rn(bmax[a], bmin[a]),
+                                  __uint2float_rn(V.block[a]));
+        wspv = (a == 0 || w < wspv) ? w : wspv;
+    }
+    const float ppv = __fdiv_rn(wspv, V.wspp);
+    const float dist = fabsf(pdot(np, vmin));
+    const float ppvd =
+        __fdiv_rn(__fmul_rn(ppv, V.nearp), __fadd_rn(V.nearp, dist));
+    bool vis = ppvd <= V.sse;
+    vis = (vis && L >= V.min_lod) || L == V.max_lod || L == V.depth - 1u;
+    return vis ? 1 : 2;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt()
+{
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+/* Zeroes the per-level counters and every view's result words, and writes
+ * the level-0 frontier (root blocks in any order). One block per view. */
+__global__ void lod_roots_kernel(const LodView* __restrict__ views,
+                                 uint32_t n_views, uint64_t* __restrict__ ids,
+                                 uint32_t* __restrict__ view_of,
+                                 uint32_t* __restrict__ counts,
+                                 uint32_t n_counts, uint32_t total_roots,
+                                 uint32_t capacity)
+{
+    const uint32_t v = blockIdx.x;
+    if (v == 0)
+    {
+        for (uint32_t i = threadIdx.x; i < n_counts; i += blockDim.x)
+            counts[i] = i == 0 ? min(total_roots, capacity) : 0u;
+    }
+    if (v >= n_views)
+        return;
+    const LodView& V = views[v];
+    if (threadIdx.x < LV_SELECT_RESULT_WORDS)
+        V.result[threadIdx.x] = 0u;
+    const uint32_t rx = V.root_blocks[0], ry = V.root_blocks[1],
+                   rz = V.root_blocks[2];
+    const uint32_t n = rx * ry * rz;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    {
+        const uint32_t x = i / (ry * rz), y = (i / rz) % ry, z = i % rz;
+        const uint32_t slot = V.root_offset + i;
+        if (slot < capacity)
+        {
+            ids[slot] = nid_make(0, x, y, z, V.time_step);
+            view_of[slot] = v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256)
+    lod_level_kernel(const LodView* __restrict__ views,
+                     const uint64_t* __restrict__ in_ids,
+                     const uint32_t* __restrict__ in_view,
+                     const uint32_t* __restrict__ in_count,
+                     uint64_t* __restrict__ out_ids,
+                     uint32_t* __restrict__ out_view,
+                     uint32_t* __restrict__ out_count, uint32_t capacity,
+                     uint32_t* __restrict__ overflow)
+{
+    const uint32_t n = min(*in_count, capacity);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lt = lanemask_lt();
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n;
+         base += gridDim.x * blockDim.x)
+    {
+        const uint32_t i = base + threadIdx.x;
+        const bool active = i < n;
+        uint64_t id = 0;
+        uint32_t v = 0;
+        int decision = 0;
+        if (active)
+        {
+            id = in_ids[i];
+            v = in_view[i];
+            decision = visit(views[v], id);
+        }
+        /* per-view groups of active lanes: visited + emitted counts */
+        const uint32_t key = active ? v : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        const uint32_t leader = __ffs(peers) - 1u;
+        const uint32_t emit_mask = __ballot_sync(0xFFFFFFFFu, decision == 1);
+        const uint32_t my_emits = emit_mask & peers;
+        uint32_t ebase = 0;
+        if (active && lane == leader)
+        {
+            uint32_t* res = views[v].result;
+            atomicAdd(&res[LV_SEL_VISITED], __popc(peers));
+            if (my_emits)
+            {
+                ebase = atomicAdd(&res[LV_SEL_FOUND], __popc(my_emits));
+                atomicMax(&res[LV_SEL_MAX_LEVEL], nid_level(id));
+            }
+        }
+        ebase = __shfl_sync(0xFFFFFFFFu, ebase, leader);
+        if (decision == 1)
+        {
+            const uint32_t slot = ebase + __popc(my_emits & lt);
+            if (slot < views[v].capacity)
+                views[v].out_ids[slot] = id;
+        }
+        /* children of descending lanes, 8 per lane */
+        const uint32_t desc = __ballot_sync(0xFFFFFFFFu, decision == 2);
+        uint32_t cbase = 0;
+        if (lane == 0 && desc)
+            cbase = atomicAdd(out_count, 8u * __popc(desc));
+        cbase = __shfl_sync(0xFFFFFFFFu, cbase, 0);
+        if (decision == 2)
+        {
+            const uint32_t slot = cbase + 8u * __popc(desc & lt);
+            if (slot + 8u <= capacity)
+            {
+                const uint32_t L = nid_level(id) + 1u, t = nid_t(id);
+                const uint32_t x = nid_x(id) * 2u, y = nid_y(id) * 2u,
+                               z = nid_z(id) * 2u;
+#pragma unroll
+                for (uint32_t c = 0; c < 8; ++c)
+                {
+                    out_ids[slot + c] =
+                        nid_make(L, x + (c >> 2), y + ((c >> 1) & 1u),
+                                 z + (c & 1u), t);
+                    out_view[slot + c] = v;
+                }
+            }
+            else
+                atomicExch(overflow, 1u);
+        }
+    }
+}
+
+/* WRITTEN = min(FOUND, capacity); OVERFLOW from the frontier flag. */
+__global__ void lod_finish_kernel(const LodView* __restrict__ views,
+                                  uint32_t n_views,
+                                  const uint32_t* __restrict__ overflow)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_views)
+        return;
+    uint32_t* res = views[v].result;
+    res[LV_SEL_WRITTEN] = min(res[LV_SEL_FOUND], views[v].capacity);
+    res[LV_SEL_OVERFLOW] = *overflow;
+}
+
+/* DFS preorder key: root index then the child index (x*4 + y*2 + z) of
+ * every level, padded to the tree depth (DFSTraversal.cpp:63-76 visits the
+ * roots x, y, z outer to inner and children in NodeId::getChildren order). */
+__global__ void dfs_key_kernel(const uint64_t* __restrict__ ids,
+                               const uint32_t* __restrict__ result,
+                               uint32_t depth, uint32_t rx, uint32_t ry,
+                               uint32_t rz, uint64_t* __restrict__ keys,
+                               uint64_t* __restrict__ vals, uint32_t n_pad)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad)
+        return;
+    const uint32_t n = result[LV_SEL_WRITTEN];
+    if (i >= n)
+    {
+        keys[i] = ~0ull;
+        vals[i] = ~0ull;
+        return;
+    }
+    const uint64_t id = ids[i];
+    const uint32_t L = nid_level(id);
+    const uint32_t x = nid_x(id), y = nid_y(id), z = nid_z(id);
+    uint64_t key = (uint64_t(x >> L) * ry + (y >> L)) * rz + (z >> L);
+    for (uint32_t l = 1; l < depth; ++l)
+    {
+        uint64_t c = 0;
+        if (l <= L)
+        {
+            const uint32_t s = L - l;
+            c = (((x >> s) & 1u) << 2) | (((y >> s) & 1u) << 1) | ((z >> s) & 1u);
+        }
+        key = key * 8u + c;
+    }
+    keys[i] = key;
+    vals[i] = id;
+}
+
+/* One bitonic compare-exchange pass over n_pad (power of two) pairs. */
+__global__ void bitonic_pass_kernel(uint64_t* __restrict__ keys,
+                                    uint64_t* __restrict__ vals, uint32_t n_pad,
+                                    uint32_t j, uint32_t k)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_pad)
+        return;
+    const uint32_t p = i ^ j;
+    if (p <= i)
+        return;
+    const bool up = (i & k) == 0;
+    const uint64_t a = keys[i], b = keys[p];
+    if ((a > b) == up)
+    {
+        keys[i] = b;
+        keys[p] = a;
+        const uint64_t t = vals[i];
+        vals[i] = vals[p];
+        vals[p] = t;
+    }
+}
+
+/* visitPost (SelectVisibles.cpp:110-131): keep DFS indices [start, end). */
+__global__ void slice_kernel(const uint64_t* __restrict__ sorted_ids,
+                             uint64_t* __restrict__ out,
+                             uint32_t* __restrict__ result, float r0, float r1)
+{
+    const uint32_t n = result[LV_SEL_WRITTEN];
+    const uint32_t start = uint32_t(__fmul_rn(r0, __uint2float_rn(n)));
+    const uint32_t end = min(uint32_t(__fmul_rn(r1, __uint2float_rn(n))), n);
+    for (uint32_t i = start + threadIdx.x; i < end; i += blockDim.x)
+        out[i - start] = sorted_ids[i];
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        const uint32_t k = end > start ? end - start : 0u;
+        result[LV_SEL_WRITTEN] = k;
+        result[LV_SEL_FOUND] = k;
+    }
+}
+
+} // namespace
+
+void frustum_setup(const float* mv, const float* p, float inv_mv[16],
+                   float inv_p[16], float limits[6], float planes[6][4],
+                   float eye[3], float dir[3], bool* ok)
+{
+    *ok = inverse4(mv, inv_mv) && inverse4(p, inv_p);
+    if (!*ok)
+        return;
+    /* vmml::Frustumf(projection): left right bottom top near far */
+    const float p22 = Mh(p, 2, 2), p23 = Mh(p, 2, 3);
+    const float nearp = p23 / (p22 - 1.0f);
+    limits[4] = nearp;
+    limits[5] = p23 / (p22 + 1.0f);
+    limits[2] = nearp * (Mh(p, 1, 2) - 1.0f) / Mh(p, 1, 1);
+    limits[3] = nearp * (Mh(p, 1, 2) + 1.0f) / Mh(p, 1, 1);
+    limits[0] = nearp * (Mh(p, 0, 2) - 1.0f) / Mh(p, 0, 0);
+    limits[1] = nearp * (Mh(p, 0, 2) + 1.0f) / Mh(p, 0, 0);
+    /* FrustumCuller(P * MV): planes from the rows of the clip matrix */
+    float row[4][4];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c)
+        {
+            float acc = 0.0f;
+            for (int k = 0; k < 4; ++k)
+                acc = acc + Mh(p, r, k) * Mh(mv, k, c);
+            row[r][c] = acc;
+        }
+    for (int c = 0; c < 4; ++c)
+    {
+        planes[0][c] = row[3][c] + row[0][c];
+        planes[1][c] = row[3][c] - row[0][c];
+        planes[2][c] = row[3][c] + row[1][c];
+        planes[3][c] = row[3][c] - row[1][c];
+        planes[4][c] = row[3][c] + row[2][c];
+        planes[5][c] = row[3][c] - row[2][c];
+    }
+    for (int pl = 0; pl < 6; ++pl)
+    {
+        float* q = planes[pl];
+        const float len = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+        const float inv = float(1.0 / double(len));
+        for (int c = 0; c < 4; ++c)
+            q[c] = q[c] * inv;
+    }
+    for (int i = 0; i < 3; ++i)
+    {
+        eye[i] = Mh(inv_mv, i, 3);
+        dir[i] = Mh(inv_mv, i, 2);
+    }
+}
+
+lv_status make_lod_view(lv_ctx* ctx, const lv_volume_info& vol,
+                        const lv_camera& cam, const lv_lod_params& p,
+                        LodView& V)
+{
+    if (vol.depth == 0 || vol.depth > kMaxLevels)
+        return fail(ctx, LV_EINVAL, "volume depth out of range");
+    if (p.window_height == 0)
+        return fail(ctx, LV_EINVAL, "window height is 0");
+    if (p.n_clip_planes > 6)
+        return fail(ctx, LV_EINVAL, "more than 6 clip planes");
+    float inv_mv[16], inv_p[16], lim[6], planes[6][4], eye[3], dir[3];
+    bool ok = false;
+    frustum_setup(cam.modelview, cam.projection, inv_mv, inv_p, lim, planes,
+                  eye, dir, &ok);
+    if (!ok)
+        return fail(ctx, LV_EINVAL, "singular modelview or projection");
+    std::memset(&V, 0, sizeof(V));
+    std::memcpy(V.planes, planes, sizeof(planes));
+    V.nearp = lim[4];
+    for (int i = 0; i < 3; ++i)
+        V.eye_near[i] = eye[i] - dir[i] * V.nearp;
+    V.wspp = (lim[3] - lim[2]) / float(p.window_height);
+    V.sse = p.screen_space_error;
+    for (int i = 0; i < 3; ++i)
+    {
+        V.world_size[i] = vol.world_size[i];
+        V.half[i] = vol.world_size[i] * 0.5f;
+        V.root_blocks[i] = vol.root_blocks[i];
+        if (vol.max_block[i] <= 2u * vol.overlap[i])
+            return fail(ctx, LV_EINVAL, "max_block <= 2 * overlap");
+        V.block[i] = vol.max_block[i] - 2u * vol.overlap[i];
+    }
+    V.n_clip = p.n_clip_planes;
+    std::memcpy(V.clip, p.clip_planes, sizeof(V.clip));
+    V.min_lod = p.min_lod;
+    V.max_lod = p.max_lod;
+    V.depth = vol.depth;
+    V.time_step = p.time_step;
+    return LV_OK;
+}
+
+uint64_t max_frontier(const lv_volume_info& vol)
+{
+    const uint64_t roots = uint64_t(vol.root_blocks[0]) * vol.root_blocks[1] *
+                           vol.root_blocks[2];
+    uint64_t m = roots;
+    for (uint32_t l = 1; l < vol.depth; ++l)
+        m = std::max(m, roots << (3 * l));
+    return m;
+}
+
+lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
+                        uint32_t n_views, uint32_t max_depth,
+                        cudaStream_t stream)
+{
+    SelectScratch& S = ctx->sel;
+    if (S.frontier_capacity == 0)
+        return fail(ctx, LV_EINVAL, "selection scratch not reserved");
+    const uint32_t cap = S.frontier_capacity;
+    LV_CUDA(ctx, S.staging.reserve(sizeof(LodView) * n_views));
+    LV_CUDA(ctx, S.views.reserve(sizeof(LodView) * n_views));
+    /* The pinned staging copy may still be read by a previous in-flight
+     * transfer: wait for the stream before overwriting it. */
+    LV_CUDA(ctx, cudaStreamSynchronize(stream));
+    std::memcpy(S.staging.ptr, host_views, sizeof(LodView) * n_views);
+    uint32_t total_roots = 0;
+    for (uint32_t v = 0; v < n_views; ++v)
+    {
+        S.staging.as<LodView>()[v].root_offset = total_roots;
+        total_roots += host_views[v].root_blocks[0] *
+                       host_views[v].root_blocks[1] *
+                       host_views[v].root_blocks[2];
+    }
+    if (total_roots > cap)
+        return fail(ctx, LV_ENOMEM, "root frontier exceeds scratch capacity");
+    LV_CUDA(ctx, cudaMemcpyAsync(S.views.ptr, S.staging.ptr,
+                                 sizeof(LodView) * n_views,
+                                 cudaMemcpyHostToDevice, stream));
+    const LodView* dviews = S.views.as<LodView>();
+    uint32_t* counts = S.counts.as<uint32_t>();
+    const uint32_t n_counts = kMaxLevels + 2;
+    uint32_t* overflow = counts + kMaxLevels + 1;
+    lod_roots_kernel<<<n_views, 128, 0, stream>>>(
+        dviews, n_views, S.ids[0].as<uint64_t>(), S.view[0].as<uint32_t>(),
+        counts, n_counts, total_roots, cap);
+    LV_CUDA(ctx, cudaGetLastError());
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    for (uint32_t l = 0; l < max_depth; ++l)
+    {
+        const int in = l & 1, out = in ^ 1;
+        lod_level_kernel<<<2 * sms, 256, 0, stream>>>(
+            dviews, S.ids[in].as<uint64_t>(), S.view[in].as<uint32_t>(),
+            counts + l, S.ids[out].as<uint64_t>(), S.view[out].as<uint32_t>(),
+            counts + l + 1, cap, overflow);
+        LV_CUDA(ctx, cudaGetLastError());
+    }
+    lod_finish_kernel<<<(n_views + 127) / 128, 128, 0, stream>>>(dviews, n_views,
+                                                                 overflow);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+lv_status range_slice(lv_ctx* ctx, const lv_volume_info& vol,
+                      const float range[2], uint64_t* d_ids, uint32_t* d_result,
+                      cudaStream_t stream)
+{
+    uint32_t written = 0;
+    LV_CUDA(ctx, cudaMemcpyAsync(&written, d_result + LV_SEL_WRITTEN,
+                                 sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                 stream));
+    LV_CUDA(ctx, cudaStreamSynchronize(stream));
+    uint32_t n_pad = 1;
+    while (n_pad < written)
+        n_pad <<= 1;
+    SelectScratch& S = ctx->sel;
+    LV_CUDA(ctx, S.sort.reserve(sizeof(uint64_t) * 2 * n_pad));
+    uint64_t* keys = S.sort.as<uint64_t>();
+    uint64_t* vals = keys + n_pad;
+    const uint32_t tb = 256, nb = (n_pad + tb - 1) / tb;
+    dfs_key_kernel<<<nb, tb, 0, stream>>>(d_ids, d_result, vol.depth,
+                                          vol.root_blocks[0], vol.root_blocks[1],
+                                          vol.root_blocks[2], keys, vals, n_pad);
+    for (uint32_t k = 2; k <= n_pad; k <<= 1)
+        for (uint32_t j = k >> 1; j > 0; j >>= 1)
+            bitonic_pass_kernel<<<nb, tb, 0, stream>>>(keys, vals, n_pad, j, k);
+    slice_kernel<<<1, 256, 0, stream>>>(vals, d_ids, d_result, range[0],
+                                        range[1]);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+} // namespace lv
+
+extern "C" lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
+                                       const lv_camera* camera,
+                                       const lv_lod_params* params,
+                                       uint64_t* d_out_ids, uint32_t capacity,
+                                       uint32_t* d_result, void* stream)
+{
+    using namespace lv;
+    if (!ctx || !vol || !camera || !params || !d_result ||
+        (!d_out_ids && capacity))
+        return fail(ctx, LV_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    LodView V;
+    lv_status st = make_lod_view(ctx, *vol, *camera, *params, V);
+    if (st != LV_OK)
+        return st;
+    V.out_ids = d_out_ids;
+    V.capacity = capacity;
+    V.result = d_result;
+    const uint64_t need = max_frontier(*vol);
+    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(need, 64), 1u << 24);
+    SelectScratch& S = ctx->sel;
+    if (S.frontier_capacity < cap)
+    {
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        for (int i = 0; i < 2; ++i)
+        {
+            LV_CUDA(ctx, S.ids[i].reserve(sizeof(uint64_t) * cap));
+            LV_CUDA(ctx, S.view[i].reserve(sizeof(uint32_t) * cap));
+        }
+        LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 2)));
+        S.frontier_capacity = uint32_t(cap);
+    }
+    st = run_selection(ctx, &V, 1, vol->depth, s);
+    if (st != LV_OK)
+        return st;
+    const bool full = params->range[0] == 0.0f && params->range[1] == 1.0f;
+    if (!full)
+        return range_slice(ctx, *vol, params->range, d_out_ids, d_result, s);
+    return LV_OK;
+}

@@ -1,0 +1,149 @@
+/*
+ * Internal device/host structures of the livre_gb300 runtime.
+ *
+ * NodeId packing follows livre::NodeId (livre/data/NodeId.h:34-49,
+ * livre/data/types.h:80-93): bits [0,4) level, [4,18) x, [18,32) y,
+ * [32,46) z, [46,64) time step; all ones = invalid.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "livre_gb300.h"
+
+#define LV_HD __host__ __device__ __forceinline__
+
+namespace lv
+{
+constexpr uint32_t kMaxLevels = 15;
+constexpr uint32_t kLeafEmpty = 0xFFFFFFFFu;
+constexpr uint32_t kLeafSlotBits = 27;
+constexpr uint32_t kLeafSlotMask = (1u << kLeafSlotBits) - 1u;
+constexpr uint64_t kInvalidNode = ~0ull;
+/* Pool addresses are stored as 1 KiB units (27 bits: 128 GiB). */
+constexpr uint64_t kSlotUnit = 1024;
+
+LV_HD uint32_t nid_level(uint64_t id) { return uint32_t(id & 0xFu); }
+LV_HD uint32_t nid_x(uint64_t id) { return uint32_t((id >> 4) & 0x3FFFu); }
+LV_HD uint32_t nid_y(uint64_t id) { return uint32_t((id >> 18) & 0x3FFFu); }
+LV_HD uint32_t nid_z(uint64_t id) { return uint32_t((id >> 32) & 0x3FFFu); }
+LV_HD uint32_t nid_t(uint64_t id) { return uint32_t(id >> 46); }
+LV_HD uint64_t nid_make(uint32_t level, uint32_t x, uint32_t y, uint32_t z,
+                        uint32_t t)
+{
+    return uint64_t(level & 0xFu) | (uint64_t(x & 0x3FFFu) << 4) |
+           (uint64_t(y & 0x3FFFu) << 18) | (uint64_t(z & 0x3FFFu) << 32) |
+           (uint64_t(t & 0x3FFFFu) << 46);
+}
+
+/* Per-view constants of the LOD selection (derived on the host from
+ * Frustum(MV, P) and the SelectVisibles arguments). */
+struct LodView
+{
+    float planes[6][4];  /* culler planes: left right bottom top near far */
+    float eye_near[3];   /* eye - dir * near (SelectVisibles.cpp:88-89) */
+    float nearp;         /* frustum near limit */
+    float wspp;          /* (top - bottom) / windowHeight */
+    float sse;
+    float world_size[3];
+    float half[3];       /* world_size * 0.5f */
+    float clip[6][4];
+    uint32_t n_clip;
+    uint32_t min_lod, max_lod, depth;
+    uint32_t root_blocks[3];
+    uint32_t block[3];   /* maximumBlockSize - 2 * overlap */
+    uint32_t time_step;
+    uint32_t root_offset; /* first root of this view in the level-0 frontier */
+    uint32_t capacity;    /* of out_ids */
+    uint64_t* out_ids;
+    uint32_t* result;     /* LV_SELECT_RESULT_WORDS */
+};
+
+/* Per-view constants of the ray cast. */
+struct RayView
+{
+    float inv_p[16];
+    float inv_mv[16];
+    float eye[3];
+    float nearp;
+    float gmin[3], gmax[3], gscale[3];
+    float clip[6][4];
+    uint32_t n_clip;
+    uint32_t dims[3]; /* leaf grid (finest level) */
+    uint32_t Lf;      /* finest level = depth - 1 */
+    uint32_t N[3], B[3], O[3];
+    uint32_t dtype;   /* lv_dtype */
+    uint32_t filter;
+    float dmul, dadd; /* density = value * dmul + dadd */
+    float early;
+    uint32_t W, H;
+    uint32_t samples_fixed; /* 0 = policy */
+    uint32_t step_policy;
+    uint32_t max_voxel_dim;
+    uint32_t depth;
+    const uint32_t* leaf;
+    const uint8_t* pool; /* brick = pool + slot * kSlotUnit */
+    const float4* tf;
+    uint32_t tfn;
+    float4* out;
+    uint32_t* counters; /* FrameCounters */
+};
+
+/* Device counters of one frame of one view. */
+enum FrameCounter
+{
+    FC_RENDERED = 0,      /* rendering-set entries */
+    FC_AVAILABLE = 1,
+    FC_NOT_AVAILABLE = 2,
+    FC_MISSING = 3,       /* entries appended to the missing list */
+    FC_MAX_LEVEL = 4,     /* finest level rendered, +1 (0 = none) */
+    FC_SAMPLES_PER_RAY = 5,
+    FC_SAMPLES_LO = 6,    /* 64-bit composited-sample counter */
+    FC_SAMPLES_HI = 7,
+    FC_ERROR = 8,         /* nonzero: an index check failed in a kernel */
+    FC_WORDS = 16
+};
+
+/* Per-view inputs of the residency pass. */
+struct ResolveView
+{
+    const uint64_t* visible;  /* visible ids of the view */
+    const uint32_t* n_visible_ptr; /* LV_SEL_WRITTEN word of the selection */
+    const int32_t* node_table;     /* slot unit per node (-1 = not resident) */
+    uint32_t* node_stamp;          /* last frame a node was rendered (in use) */
+    uint32_t frame;
+    uint32_t depth;
+    uint32_t root_blocks[3];
+    uint64_t level_offset[kMaxLevels + 1];
+    uint32_t synchronous;     /* no ancestor fallback */
+    uint64_t* render_ids;     /* rendering set: ids */
+    uint32_t* render_slots;   /* rendering set: slot */
+    uint32_t render_capacity;
+    uint64_t* missing;        /* missing ids */
+    uint32_t missing_capacity;
+    uint32_t* counters;       /* FrameCounters */
+    uint32_t* leaf;           /* leaf grid */
+    uint32_t dims[3];
+    uint32_t Lf;
+};
+
+LV_HD uint64_t node_index(const uint64_t* level_offset,
+                          const uint32_t* root_blocks, uint64_t id)
+{
+    const uint32_t L = nid_level(id);
+    const uint64_t by = uint64_t(root_blocks[1]) << L;
+    const uint64_t bz = uint64_t(root_blocks[2]) << L;
+    return level_offset[L] +
+           (uint64_t(nid_x(id)) * by + nid_y(id)) * bz + nid_z(id);
+}
+
+} // namespace lv
+
+/* Host-side helpers implemented in the .cu files. */
+namespace lv
+{
+void frustum_setup(const float* mv, const float* p, float inv_mv[16],
+                   float inv_p[16], float limits[6], float planes[6][4],
+                   float eye[3], float dir[3], bool* ok);
+}

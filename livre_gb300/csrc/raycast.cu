@@ -1,0 +1,471 @@
+/*
+ * Residency resolve, leaf-grid build and the ray-cast kernel.
+ *
+ * Replaces the per-brick GL draw loop of livre/eq/render/RayCastRenderer.cpp
+ * (onFrameRender :467-481, renderBrick :503-571) and the fragment shader
+ * livre/eq/render/shaders/fragRayCast.glsl:113-207. Instead of one draw call
+ * per brick with a read-modify-write of an RGBA32F image, one thread walks one
+ * ray through every brick in ray order:
+ *
+ *  - the rendering set (visible bricks, or their nearest resident ancestors,
+ *    RenderingSetGeneratorFilter.cpp:32-111) is splatted into a dense leaf
+ *    grid at the finest octree level: one 32-bit entry per finest cell,
+ *    (level << 27 | pool slot), coarser level winning;
+ *  - samples lie on the global grid t = tnearGlobal + k * step, exactly the
+ *    positions the shader's residue snapping produces (fragRayCast.glsl:
+ *    142-147); a sample belongs to the brick whose cell contains it;
+ *  - voxels are read straight from the HBM brick pool (nearest or trilinear,
+ *    clamp to edge), mapped through the 1D transfer function (linear,
+ *    clamp to edge) and composited front to back with the shader's opacity
+ *    correction 1 - (1 - min(a, 255/256))^(32 / nSamples) and early exit.
+ *
+ * Ray geometry (direction, box and near-plane distances, sample positions,
+ * cell and voxel coordinates) uses explicit IEEE round-to-nearest float
+ * intrinsics in a fixed order, so every sample reads the same voxels as the
+ * CPU oracle; shading runs in FP32 with fused multiply-adds.
+ */
+#include "lv_runtime.h"
+
+namespace lv
+{
+namespace
+{
+/* std::min / std::max semantics (first argument on ties), as the oracle. */
+__device__ __forceinline__ float smin(float a, float b) { return b < a ? b : a; }
+__device__ __forceinline__ float smax(float a, float b) { return a < b ? b : a; }
+
+/* Emits (id, slot) into the rendering set of the view. */
+__device__ __forceinline__ void emit_render(const ResolveView& R, uint64_t id,
+                                            uint32_t slot)
+{
+    const uint32_t k = atomicAdd(&R.counters[FC_RENDERED], 1u);
+    if (k < R.render_capacity)
+    {
+        R.render_ids[k] = id;
+        R.render_slots[k] = slot;
+    }
+    else
+        atomicExch(&R.counters[FC_ERROR], 1u);
+    atomicMax(&R.counters[FC_MAX_LEVEL], nid_level(id) + 1u);
+}
+
+/* For each visible id: resident -> rendering set; missing -> missing list
+ * and (async mode) the nearest resident ancestor, once per frame. */
+__global__ void resolve_kernel(ResolveView R)
+{
+    const uint32_t n = *R.n_visible_ptr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += gridDim.x * blockDim.x)
+    {
+        const uint64_t id = R.visible[i];
+        const uint64_t idx = node_index(R.level_offset, R.root_blocks, id);
+        const int32_t slot = R.node_table[idx];
+        if (slot >= 0)
+        {
+            R.node_stamp[idx] = R.frame;
+            atomicAdd(&R.counters[FC_AVAILABLE], 1u);
+            emit_render(R, id, uint32_t(slot));
+            continue;
+        }
+        atomicAdd(&R.counters[FC_NOT_AVAILABLE], 1u);
+        const uint32_t m = atomicAdd(&R.counters[FC_MISSING], 1u);
+        if (m < R.missing_capacity)
+            R.missing[m] = id;
+        if (R.synchronous)
+            continue;
+        uint64_t cur = id;
+        while (nid_level(cur) > 0)
+        {
+            const uint32_t L = nid_level(cur) - 1u;
+            cur = nid_make(L, nid_x(cur) >> 1, nid_y(cur) >> 1, nid_z(cur) >> 1,
+                           nid_t(cur));
+            const uint64_t pidx = node_index(R.level_offset, R.root_blocks, cur);
+            const int32_t ps = R.node_table[pidx];
+            if (ps >= 0)
+            {
+                if (atomicExch(&R.node_stamp[pidx], R.frame) != R.frame)
+                    emit_render(R, cur, uint32_t(ps));
+                break;
+            }
+        }
+    }
+}
+
+/* Splats the rendering set into the leaf grid; one warp per entry. */
+__global__ void leaf_fill_kernel(ResolveView R)
+{
+    const uint32_t n = min(R.counters[FC_RENDERED], R.render_capacity);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t e = warp; e < n; e += nwarps)
+    {
+        const uint64_t id = R.render_ids[e];
+        const uint32_t slot = R.render_slots[e];
+        const uint32_t L = nid_level(id);
+        const uint32_t sh = R.Lf - L;
+        const uint32_t side = 1u << sh;
+        const uint32_t x0 = nid_x(id) << sh, y0 = nid_y(id) << sh,
+                       z0 = nid_z(id) << sh;
+        const uint32_t key = (L << kLeafSlotBits) | (slot & kLeafSlotMask);
+        const uint64_t cells = uint64_t(side) * side * side;
+        for (uint64_t c = lane; c < cells; c += 32)
+        {
+            const uint32_t cx = x0 + uint32_t(c % side);
+            const uint32_t cy = y0 + uint32_t((c / side) % side);
+            const uint32_t cz = z0 + uint32_t(c / (uint64_t(side) * side));
+            if (cx < R.dims[0] && cy < R.dims[1] && cz < R.dims[2])
+                atomicMin(&R.leaf[(uint64_t(cz) * R.dims[1] + cy) * R.dims[0] + cx],
+                          key);
+        }
+    }
+}
+
+/* nSamplesPerRay from the finest rendered level (RayCastRenderer.cpp:
+ * 216-233 for LV_STEP_REFERENCE; half a voxel for LV_STEP_HALF_VOXEL). */
+__global__ void step_kernel(uint32_t* counters, uint32_t fixed, uint32_t policy,
+                            uint32_t max_voxel_dim, uint32_t depth)
+{
+    uint32_t n = fixed;
+    if (n == 0)
+    {
+        const uint32_t ml = counters[FC_MAX_LEVEL];
+        const uint32_t L = ml ? ml - 1u : 0u;
+        const uint32_t shift = depth - L - 1u;
+        if (policy == LV_STEP_HALF_VOXEL)
+            n = (2u * max_voxel_dim) >> shift;
+        else
+        {
+            const float at_lod = float(max_voxel_dim) / float(1u << shift);
+            n = uint32_t(fmaxf(at_lod, 512.0f));
+        }
+        if (n == 0)
+            n = 1;
+    }
+    counters[FC_SAMPLES_PER_RAY] = n;
+}
+
+template <int DT>
+__device__ __forceinline__ float voxel(const uint8_t* brick, uint32_t i)
+{
+    if (DT == LV_DT_UINT16)
+        return float(__ldg(reinterpret_cast<const uint16_t*>(brick) + i));
+    return float(__ldg(brick + i));
+}
+
+template <int DT, int FILTER>
+__device__ __forceinline__ float sample_brick(const RayView& V,
+                                              const uint8_t* brick,
+                                              const float local[3])
+{
+    const int n0 = int(V.N[0]), n1 = int(V.N[1]), n2 = int(V.N[2]);
+    if (FILTER == LV_FILTER_NEAREST)
+    {
+        const int x = min(max(int(floorf(local[0])), 0), n0 - 1);
+        const int y = min(max(int(floorf(local[1])), 0), n1 - 1);
+        const int z = min(max(int(floorf(local[2])), 0), n2 - 1);
+        return voxel<DT>(brick, uint32_t((z * n1 + y) * n0 + x));
+    }
+    const float sx = local[0] - 0.5f, sy = local[1] - 0.5f, sz = local[2] - 0.5f;
+    const float fx0 = floorf(sx), fy0 = floorf(sy), fz0 = floorf(sz);
+    const float fx = sx - fx0, fy = sy - fy0, fz = sz - fz0;
+    const int ix = int(fx0), iy = int(fy0), iz = int(fz0);
+    const int x0 = min(max(ix, 0), n0 - 1), x1 = min(max(ix + 1, 0), n0 - 1);
+    const int y0 = min(max(iy, 0), n1 - 1), y1 = min(max(iy + 1, 0), n1 - 1);
+    const int z0 = min(max(iz, 0), n2 - 1), z1 = min(max(iz + 1, 0), n2 - 1);
+    const int r00 = (z0 * n1 + y0) * n0, r01 = (z0 * n1 + y1) * n0;
+    const int r10 = (z1 * n1 + y0) * n0, r11 = (z1 * n1 + y1) * n0;
+    const float c000 = voxel<DT>(brick, r00 + x0), c001 = voxel<DT>(brick, r00 + x1);
+    const float c010 = voxel<DT>(brick, r01 + x0), c011 = voxel<DT>(brick, r01 + x1);
+    const float c100 = voxel<DT>(brick, r10 + x0), c101 = voxel<DT>(brick, r10 + x1);
+    const float c110 = voxel<DT>(brick, r11 + x0), c111 = voxel<DT>(brick, r11 + x1);
+    const float a0 = fmaf(c001 - c000, fx, c000);
+    const float a1 = fmaf(c011 - c010, fx, c010);
+    const float a2 = fmaf(c101 - c100, fx, c100);
+    const float a3 = fmaf(c111 - c110, fx, c110);
+    const float b0 = fmaf(a1 - a0, fy, a0);
+    const float b1 = fmaf(a3 - a2, fy, a2);
+    return fmaf(b1 - b0, fz, b0);
+}
+
+__device__ __forceinline__ float4 tf_lookup(const RayView& V, float d)
+{
+    const float s = fmaf(d, float(V.tfn), -0.5f);
+    const float fl = floorf(s);
+    const float f = s - fl;
+    const int last = int(V.tfn) - 1;
+    const int i0 = min(max(int(fl), 0), last);
+    const int i1 = min(max(int(fl) + 1, 0), last);
+    const float4 a = __ldg(V.tf + i0), b = __ldg(V.tf + i1);
+    return make_float4(fmaf(b.x - a.x, f, a.x), fmaf(b.y - a.y, f, a.y),
+                       fmaf(b.z - a.z, f, a.z), fmaf(b.w - a.w, f, a.w));
+}
+
+__device__ __forceinline__ float Md(const float* m, int r, int c)
+{
+    return m[c * 4 + r];
+}
+
+struct RayGeom
+{
+    float dir[3];
+    float tg, tlo, thi;
+    bool hit;
+};
+
+/* Ray through the centre of pixel (px, py); FP32 IEEE ops in fixed order. */
+__device__ __forceinline__ RayGeom ray_setup(const RayView& V, uint32_t px,
+                                             uint32_t py)
+{
+    RayGeom g;
+    const float nx = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(__uint2float_rn(px), 0.5f), 2.0f),
+                                         __uint2float_rn(V.W)),
+                               1.0f);
+    const float ny = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(__uint2float_rn(py), 0.5f), 2.0f),
+                                         __uint2float_rn(V.H)),
+                               1.0f);
+    float e[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        e[i] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(Md(V.inv_p, i, 0), nx),
+                                             __fmul_rn(Md(V.inv_p, i, 1), ny)),
+                                   __fmul_rn(Md(V.inv_p, i, 2), -1.0f)),
+                         __fmul_rn(Md(V.inv_p, i, 3), 1.0f));
+    const float ep[3] = {__fdiv_rn(e[0], e[3]), __fdiv_rn(e[1], e[3]),
+                         __fdiv_rn(e[2], e[3])};
+    float d[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        const float pw =
+            __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(Md(V.inv_mv, i, 0), ep[0]),
+                                          __fmul_rn(Md(V.inv_mv, i, 1), ep[1])),
+                                __fmul_rn(Md(V.inv_mv, i, 2), ep[2])),
+                      Md(V.inv_mv, i, 3));
+        d[i] = __fsub_rn(pw, V.eye[i]);
+    }
+    const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]),
+                                                     __fmul_rn(d[1], d[1])),
+                                           __fmul_rn(d[2], d[2])));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        g.dir[i] = __fdiv_rn(d[i], len);
+    const float lenE = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ep[0], ep[0]),
+                                                      __fmul_rn(ep[1], ep[1])),
+                                            __fmul_rn(ep[2], ep[2])));
+    const float nz = __fdiv_rn(ep[2], lenE);
+    const float tnp = __fdiv_rn(-V.nearp, nz);
+    float tmin[3], tmax[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+    {
+        const float di = g.dir[i] == 0.0f ? 1e-10f : g.dir[i];
+        const float inv = __fdiv_rn(1.0f, di);
+        const float tb = __fmul_rn(inv, __fsub_rn(V.gmin[i], V.eye[i]));
+        const float tt = __fmul_rn(inv, __fsub_rn(V.gmax[i], V.eye[i]));
+        tmin[i] = smin(tt, tb);
+        tmax[i] = smax(tt, tb);
+    }
+    const float t0 = smax(smax(tmin[0], tmin[1]), smax(tmin[0], tmin[2]));
+    const float t1 = smin(smin(tmax[0], tmax[1]), smin(tmax[0], tmax[2]));
+    g.hit = t0 <= t1;
+    g.tg = t0;
+    float tlo = smax(t0, tnp);
+    float thi = t1;
+    for (uint32_t c = 0; c < V.n_clip; ++c)
+    {
+        const float* cp = V.clip[c];
+        float rn = __fadd_rn(__fadd_rn(__fmul_rn(g.dir[0], cp[0]), __fmul_rn(g.dir[1], cp[1])),
+                             __fmul_rn(g.dir[2], cp[2]));
+        if (rn == 0.0f)
+            rn = 1e-10f;
+        const float ne = __fadd_rn(__fadd_rn(__fmul_rn(cp[0], V.eye[0]), __fmul_rn(cp[1], V.eye[1])),
+                                   __fmul_rn(cp[2], V.eye[2]));
+        const float t = __fdiv_rn(-__fadd_rn(ne, cp[3]), rn);
+        if (rn > 0.0f)
+            tlo = smax(tlo, t);
+        else
+            thi = smin(thi, t);
+    }
+    g.tlo = tlo;
+    g.thi = thi;
+    return g;
+}
+
+template <int DT, int FILTER>
+__device__ float4 march(const RayView& V, const RayGeom& g, float step,
+                        float ac, uint32_t& nsamp)
+{
+    float4 dst = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!g.hit || !(g.tlo <= g.thi))
+        return dst;
+    int k = 0;
+    if (g.tlo > g.tg)
+        k = int(ceilf(__fdiv_rn(__fsub_rn(g.tlo, g.tg), step)));
+    const float dimf[3] = {__uint2float_rn(V.dims[0]), __uint2float_rn(V.dims[1]),
+                           __uint2float_rn(V.dims[2])};
+    uint32_t cur = 0xFFFFFFFFu, entry = kLeafEmpty;
+    const uint8_t* brick = nullptr;
+    float vs[3] = {0.f, 0.f, 0.f}, base[3] = {0.f, 0.f, 0.f};
+    const float early = V.early;
+    for (;; ++k)
+    {
+        const float t = __fadd_rn(g.tg, __fmul_rn(__int2float_rn(k), step));
+        if (!(t < g.thi))
+            break;
+        float f[3];
+        int c[3];
+        bool inside = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            const float p = __fadd_rn(V.eye[a], __fmul_rn(g.dir[a], t));
+            f[a] = __fmul_rn(__fsub_rn(p, V.gmin[a]), V.gscale[a]);
+            const float fl = floorf(f[a]);
+            inside = inside && (fl >= 0.0f) && (fl < dimf[a]);
+            c[a] = int(fl);
+        }
+        if (!inside)
+            continue;
+        const uint32_t lin =
+            (uint32_t(c[2]) * V.dims[1] + uint32_t(c[1])) * V.dims[0] + uint32_t(c[0]);
+        if (lin != cur)
+        {
+            cur = lin;
+            entry = __ldg(V.leaf + lin);
+            if (entry != kLeafEmpty)
+            {
+                const uint32_t L = entry >> kLeafSlotBits;
+                const uint32_t slot = entry & kLeafSlotMask;
+                const uint32_t sh = V.Lf - L;
+                brick = V.pool + uint64_t(slot) * kSlotUnit;
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+                {
+                    vs[a] = __fdiv_rn(__uint2float_rn(V.B[a]), __uint2float_rn(1u << sh));
+                    base[a] = __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a]);
+                }
+            }
+        }
+        if (entry == kLeafEmpty)
+            continue;
+        float local[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            local[a] = __fadd_rn(__fsub_rn(__fmul_rn(f[a], vs[a]), base[a]),
+                                 __uint2float_rn(V.O[a]));
+        const float value = sample_brick<DT, FILTER>(V, brick, local);
+        const float dens = fmaf(value, V.dmul, V.dadd);
+        const float4 src = tf_lookup(V, dens);
+        const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
+        const float alpha = 1.0f - exp2f(ac * __log2f(1.0f - am));
+        const float w = alpha * (1.0f - dst.w);
+        dst.x = fmaf(src.x, w, dst.x);
+        dst.y = fmaf(src.y, w, dst.y);
+        dst.z = fmaf(src.z, w, dst.z);
+        dst.w = fmaf(alpha, 1.0f - dst.w, dst.w);
+        ++nsamp;
+        if (dst.w > early)
+            break;
+    }
+    return dst;
+}
+
+template <int DT, int FILTER>
+__global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
+{
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t py = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
+    const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
+    const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
+    uint32_t nsamp = 0;
+    if (px < V.W && py < V.H)
+    {
+        const RayGeom g = ray_setup(V, px, py);
+        const float4 r = march<DT, FILTER>(V, g, step, ac, nsamp);
+        V.out[uint64_t(py) * V.W + px] = r;
+    }
+    /* warp-aggregated 64-bit sample count */
+    unsigned long long s = nsamp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_down_sync(0xFFFFFFFFu, s, o);
+    if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0 && s)
+        atomicAdd(reinterpret_cast<unsigned long long*>(V.counters + FC_SAMPLES_LO), s);
+}
+
+__global__ void to_rgba8_kernel(const float4* __restrict__ in,
+                                uchar4* __restrict__ out, uint64_t n)
+{
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+         i += uint64_t(gridDim.x) * blockDim.x)
+    {
+        const float4 c = in[i];
+        const auto q = [](float v) {
+            return (unsigned char)(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f);
+        };
+        out[i] = make_uchar4(q(c.x), q(c.y), q(c.z), 255);
+    }
+}
+
+} // namespace
+
+lv_status launch_resolve(lv_ctx* ctx, const ResolveView& R, cudaStream_t s)
+{
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    resolve_kernel<<<sms, 256, 0, s>>>(R);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+lv_status launch_leaf_fill(lv_ctx* ctx, const ResolveView& R, cudaStream_t s)
+{
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    leaf_fill_kernel<<<2 * sms, 256, 0, s>>>(R);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
+{
+    step_kernel<<<1, 1, 0, s>>>(V.counters, V.samples_fixed, V.step_policy,
+                                V.max_voxel_dim, V.depth);
+    LV_CUDA(ctx, cudaGetLastError());
+    const dim3 block(16, 8);
+    const dim3 grid((V.W + block.x - 1) / block.x, (V.H + block.y - 1) / block.y);
+    if (V.dtype == LV_DT_UINT8 && V.filter == LV_FILTER_TRILINEAR)
+        raycast_kernel<LV_DT_UINT8, LV_FILTER_TRILINEAR><<<grid, block, 0, s>>>(V);
+    else if (V.dtype == LV_DT_UINT8)
+        raycast_kernel<LV_DT_UINT8, LV_FILTER_NEAREST><<<grid, block, 0, s>>>(V);
+    else if (V.dtype == LV_DT_UINT16 && V.filter == LV_FILTER_TRILINEAR)
+        raycast_kernel<LV_DT_UINT16, LV_FILTER_TRILINEAR><<<grid, block, 0, s>>>(V);
+    else if (V.dtype == LV_DT_UINT16)
+        raycast_kernel<LV_DT_UINT16, LV_FILTER_NEAREST><<<grid, block, 0, s>>>(V);
+    else
+        return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+} // namespace lv
+
+extern "C" lv_status lv_frame_to_rgba8(lv_ctx* ctx, const float* d_rgba,
+                                       uint32_t width, uint32_t height,
+                                       uint8_t* d_out, void* stream)
+{
+    using namespace lv;
+    if (!ctx || (!d_rgba && width * height) || (!d_out && width * height))
+        return fail(ctx, LV_EINVAL, "null argument");
+    const uint64_t n = uint64_t(width) * height;
+    if (n == 0)
+        return LV_OK;
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    const uint32_t blocks = uint32_t(std::min<uint64_t>((n + 255) / 256, 4096));
+    to_rgba8_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<const float4*>(d_rgba), reinterpret_cast<uchar4*>(d_out), n);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}

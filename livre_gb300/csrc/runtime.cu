@@ -1,0 +1,1163 @@
+/*
+ * Host runtime of livre_gb300: context, HBM brick pool with LRU residency,
+ * volumes and their data sources, transfer functions and the per-view frame
+ * (select -> resolve -> stream misses -> leaf grid -> ray cast).
+ *
+ * Reference counterparts (paths inside BlueBrain/Livre):
+ *  - brick pool + residency: TexturePool (livre/core/render/TexturePool.cpp:
+ *    33-126), CacheT<TextureObject> with LRUCachePolicy (livre/core/cache/
+ *    Cache.cpp:41-209), TextureObject upload (livre/lib/cache/
+ *    TextureObject.cpp:76-120), DataUploadFilter (livre/lib/pipeline/
+ *    DataUploadFilter.cpp:45-123);
+ *  - frame: RenderPipeline::renderSync / renderAsync (livre/lib/pipeline/
+ *    RenderPipeline.cpp:92-225) and Renderer::render (livre/core/render/
+ *    Renderer.cpp:33-47).
+ *
+ * LRU semantics kept from the reference cache: residency order is load
+ * order (a hit does not refresh it, Cache.cpp:111-123); when the pool is
+ * full the oldest brick not in use by the frame being built is evicted
+ * (objects still referenced are skipped, Cache.cpp:141-156).
+ */
+#include <algorithm>
+#include <cmath>
+#include <list>
+#include <map>
+#include <unordered_map>
+#include <vector>
+
+#include "lv_runtime.h"
+
+namespace lv
+{
+struct Blob
+{
+    float cx, cy, cz, inv2s2, cut2, amp;
+};
+std::vector<Blob> make_blobs(const lv_volume_info& v, const lv_blob_desc& d);
+lv_status launch_blob_bricks(lv_ctx* ctx, const lv_volume_info& v,
+                             const lv_blob_desc& d, const Blob* d_blobs,
+                             const uint64_t* d_ids, uint32_t n, uint8_t* out,
+                             const uint64_t* d_offsets, cudaStream_t stream);
+lv_status launch_resolve(lv_ctx* ctx, const ResolveView& R, cudaStream_t s);
+lv_status launch_leaf_fill(lv_ctx* ctx, const ResolveView& R, cudaStream_t s);
+lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s);
+
+enum SourceKind
+{
+    SRC_CALLBACK = 0,
+    SRC_BLOB_DEVICE = 1,
+    SRC_BLOB_HOST = 2
+};
+
+namespace
+{
+__global__ void scatter_kernel(int32_t* __restrict__ table,
+                               const int64_t* __restrict__ pairs, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        table[pairs[2 * i]] = int32_t(pairs[2 * i + 1]);
+}
+
+__global__ void fill_i32_kernel(int32_t* p, uint64_t n, int32_t v)
+{
+    for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+         i += uint64_t(gridDim.x) * blockDim.x)
+        p[i] = v;
+}
+
+uint64_t round_units(uint64_t bytes)
+{
+    return (bytes + kSlotUnit - 1) / kSlotUnit;
+}
+} // namespace
+
+/* One resident brick. */
+struct Resident
+{
+    lv_volume* vol;
+    uint64_t node_idx;
+    uint32_t unit;
+    uint32_t units;
+};
+
+struct Pool
+{
+    DeviceBuffer arena;
+    uint64_t capacity_units = 0;
+    uint64_t bump = 0;
+    std::map<uint32_t, std::vector<uint32_t>> free_by_units;
+    std::list<Resident> lru; /* front = oldest load */
+    uint64_t resident_bytes = 0;
+};
+
+struct Renderer
+{
+    DeviceBuffer visible, sel_result, render_ids, render_slots, missing,
+        counters, leaf, pairs;
+    PinnedBuffer h_counters, h_missing, h_pairs;
+    uint64_t visible_capacity = 0;
+    uint32_t frame = 0;
+    lv_frame_stats stats{};
+    cudaStream_t last_stream = nullptr;
+    bool have_last = false;
+    /* async mode: misses of the previous frame, copied back */
+    cudaEvent_t pending_event = nullptr;
+    lv_volume* pending_vol = nullptr;
+    uint32_t pending_max = 0;
+    uint32_t pending_frame = 0;
+    cudaEvent_t render_event = nullptr;
+    cudaEvent_t upload_event = nullptr;
+    /* timing of the last frame: selection and ray cast */
+    cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
+    uint32_t launches = 0;
+};
+
+} // namespace lv
+
+struct lv_tf
+{
+    lv_ctx* ctx;
+    lv::DeviceBuffer rgba;
+    uint32_t n;
+};
+
+struct lv_volume
+{
+    lv_ctx* ctx = nullptr;
+    lv_volume_info info{};
+    int kind = lv::SRC_CALLBACK;
+    lv_get_data_fn fn = nullptr;
+    void* user = nullptr;
+    lv_blob_desc blob{};
+    lv::DeviceBuffer d_blobs;
+    lv::PinnedBuffer host_store;
+    uint64_t brick_bytes = 0;
+    uint32_t slot_units = 0;
+    uint64_t level_offset[lv::kMaxLevels + 1] = {};
+    uint64_t n_nodes = 0;
+    lv::DeviceBuffer node_table, node_stamp;
+    std::vector<int32_t> host_table;
+    uint32_t time_step = 0;
+    /* pinned staging ring for callback sources */
+    std::vector<lv::PinnedBuffer*> staging;
+    std::vector<cudaEvent_t> staging_ev;
+    ~lv_volume()
+    {
+        for (auto* p : staging)
+            delete p;
+        for (auto e : staging_ev)
+            cudaEventDestroy(e);
+    }
+};
+
+namespace lv
+{
+namespace
+{
+uint32_t bytes_per_voxel(uint32_t dt)
+{
+    switch (dt)
+    {
+    case LV_DT_UINT8:
+    case LV_DT_INT8:
+        return 1;
+    case LV_DT_UINT16:
+    case LV_DT_INT16:
+        return 2;
+    case LV_DT_FLOAT:
+    case LV_DT_UINT32:
+    case LV_DT_INT32:
+        return 4;
+    default:
+        return 0;
+    }
+}
+
+/* dataSourceRange of RayCastRenderer::onFrameStart (RayCastRenderer.cpp:
+ * 236-285): the integer type's range. */
+void type_range(uint32_t dt, float& lo, float& hi)
+{
+    switch (dt)
+    {
+    case LV_DT_UINT16:
+        lo = 0.0f;
+        hi = 65535.0f;
+        break;
+    default:
+        lo = 0.0f;
+        hi = 255.0f;
+        break;
+    }
+}
+
+lv_status ensure_pool(lv_ctx* ctx)
+{
+    if (ctx->pool)
+        return LV_OK;
+    Pool* p = new Pool();
+    const uint64_t units = ctx->pool_bytes / kSlotUnit;
+    if (units == 0 || units > (uint64_t(1) << kLeafSlotBits))
+    {
+        delete p;
+        return fail(ctx, LV_EINVAL, "pool size must be in (0, 128 GiB]");
+    }
+    cudaError_t e = p->arena.reserve(units * kSlotUnit);
+    if (e != cudaSuccess)
+    {
+        delete p;
+        return cuda_fail(ctx, e, "brick pool allocation");
+    }
+    p->capacity_units = units;
+    ctx->pool = p;
+    return LV_OK;
+}
+
+lv_status ensure_renderer(lv_ctx* ctx)
+{
+    if (ctx->renderer)
+        return LV_OK;
+    Renderer* r = new Renderer();
+    cudaEventCreateWithFlags(&r->pending_event, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->render_event, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->upload_event, cudaEventDisableTiming);
+    cudaEventCreate(&r->t_sel0);
+    cudaEventCreate(&r->t_sel1);
+    cudaEventCreate(&r->t_ray0);
+    cudaEventCreate(&r->t_ray1);
+    ctx->renderer = r;
+    LV_CUDA(ctx, r->sel_result.reserve(sizeof(uint32_t) * LV_SELECT_RESULT_WORDS));
+    LV_CUDA(ctx, r->counters.reserve(sizeof(uint32_t) * FC_WORDS));
+    LV_CUDA(ctx, r->h_counters.reserve(sizeof(uint32_t) * (FC_WORDS + LV_SELECT_RESULT_WORDS)));
+    return LV_OK;
+}
+
+lv_status reserve_selection(lv_ctx* ctx, const lv_volume_info& info,
+                            cudaStream_t s)
+{
+    const uint64_t need = max_frontier(info);
+    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(need, 64), 1u << 24);
+    SelectScratch& S = ctx->sel;
+    if (S.frontier_capacity >= cap)
+        return LV_OK;
+    LV_CUDA(ctx, cudaStreamSynchronize(s));
+    for (int i = 0; i < 2; ++i)
+    {
+        LV_CUDA(ctx, S.ids[i].reserve(sizeof(uint64_t) * cap));
+        LV_CUDA(ctx, S.view[i].reserve(sizeof(uint32_t) * cap));
+    }
+    LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 2)));
+    S.frontier_capacity = uint32_t(cap);
+    return LV_OK;
+}
+
+/* Frees one slot of `units` for a new brick, evicting the oldest resident
+ * brick of the same size that is not in use (stamp < protect_frame).
+ * Returns false when every candidate is in use. */
+bool pool_alloc(lv_ctx* ctx, uint32_t units, uint32_t protect_frame,
+                std::unordered_map<lv_volume*, std::vector<uint32_t>>& stamps,
+                std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>>& updates,
+                uint32_t& out_unit)
+{
+    Pool& P = *ctx->pool;
+    auto& fl = P.free_by_units[units];
+    if (!fl.empty())
+    {
+        out_unit = fl.back();
+        fl.pop_back();
+        return true;
+    }
+    if (P.bump + units <= P.capacity_units)
+    {
+        out_unit = uint32_t(P.bump);
+        P.bump += units;
+        return true;
+    }
+    for (auto it = P.lru.begin(); it != P.lru.end(); ++it)
+    {
+        if (it->units != units)
+            continue;
+        lv_volume* v = it->vol;
+        auto st = stamps.find(v);
+        if (st == stamps.end())
+        {
+            std::vector<uint32_t> h(v->n_nodes);
+            if (cudaMemcpy(h.data(), v->node_stamp.ptr, sizeof(uint32_t) * v->n_nodes,
+                           cudaMemcpyDeviceToHost) != cudaSuccess)
+                return false;
+            st = stamps.emplace(v, std::move(h)).first;
+        }
+        const uint32_t stamp = st->second[it->node_idx];
+        if (stamp != 0 && stamp >= protect_frame)
+            continue; /* in use: Cache.cpp:148 skips referenced objects */
+        out_unit = it->unit;
+        v->host_table[it->node_idx] = -1;
+        updates.push_back({v, {it->node_idx, -1}});
+        P.resident_bytes -= uint64_t(units) * kSlotUnit;
+        P.lru.erase(it);
+        return true;
+    }
+    return false;
+}
+
+lv_status apply_updates(
+    lv_ctx* ctx,
+    std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>>& updates,
+    cudaStream_t s)
+{
+    if (updates.empty())
+        return LV_OK;
+    Renderer& R = *ctx->renderer;
+    std::map<lv_volume*, std::vector<int64_t>> per;
+    for (auto& u : updates)
+    {
+        per[u.first].push_back(int64_t(u.second.first));
+        per[u.first].push_back(int64_t(u.second.second));
+    }
+    size_t total = 0;
+    for (auto& kv : per)
+        total += kv.second.size();
+    LV_CUDA(ctx, cudaStreamSynchronize(s));
+    LV_CUDA(ctx, R.h_pairs.reserve(sizeof(int64_t) * total));
+    LV_CUDA(ctx, R.pairs.reserve(sizeof(int64_t) * total));
+    size_t off = 0;
+    for (auto& kv : per)
+    {
+        std::memcpy(R.h_pairs.as<int64_t>() + off, kv.second.data(),
+                    sizeof(int64_t) * kv.second.size());
+        off += kv.second.size();
+    }
+    LV_CUDA(ctx, cudaMemcpyAsync(R.pairs.ptr, R.h_pairs.ptr, sizeof(int64_t) * total,
+                                 cudaMemcpyHostToDevice, s));
+    off = 0;
+    for (auto& kv : per)
+    {
+        const uint32_t n = uint32_t(kv.second.size() / 2);
+        scatter_kernel<<<(n + 255) / 256, 256, 0, s>>>(
+            kv.first->node_table.as<int32_t>(), R.pairs.as<int64_t>() + off, n);
+        off += kv.second.size();
+    }
+    LV_CUDA(ctx, cudaGetLastError());
+    updates.clear();
+    return LV_OK;
+}
+
+/* Streams bricks `ids` of `vol` into the pool (DataUploadFilter::load):
+ * allocate / evict, fetch from the source, copy on the upload stream, then
+ * publish the node-table entries; `render` waits for all of it. */
+lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
+                        uint32_t n, uint32_t protect_frame, cudaStream_t render,
+                        uint32_t& n_loaded, uint64_t& bytes_loaded)
+{
+    Renderer& R = *ctx->renderer;
+    Pool& P = *ctx->pool;
+    cudaStream_t up = ctx->upload_stream;
+    n_loaded = 0;
+    bytes_loaded = 0;
+    if (n == 0)
+        return LV_OK;
+    /* new copies may overwrite evicted slots still read by queued work */
+    LV_CUDA(ctx, cudaEventRecord(R.render_event, render));
+    LV_CUDA(ctx, cudaStreamWaitEvent(up, R.render_event, 0));
+    std::unordered_map<lv_volume*, std::vector<uint32_t>> stamps;
+    std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>> updates;
+    std::vector<uint64_t> gen_ids, gen_offsets;
+    uint8_t* arena = P.arena.as<uint8_t>();
+    size_t ring = 0;
+    lv_status st = LV_OK;
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const uint64_t id = ids[i];
+        if (nid_level(id) >= vol->info.depth)
+            continue;
+        const uint64_t idx = node_index(vol->level_offset, vol->info.root_blocks, id);
+        if (idx >= vol->n_nodes || vol->host_table[idx] >= 0)
+            continue;
+        uint32_t unit = 0;
+        if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit))
+        {
+            st = fail(ctx, LV_EAGAIN, "brick pool full of bricks in use");
+            break;
+        }
+        uint8_t* dst = arena + uint64_t(unit) * kSlotUnit;
+        if (vol->kind == SRC_BLOB_HOST)
+        {
+            const uint8_t* src = vol->host_store.as<uint8_t>() + idx * vol->brick_bytes;
+            LV_CUDA(ctx, cudaMemcpyAsync(dst, src, vol->brick_bytes,
+                                         cudaMemcpyHostToDevice, up));
+            bytes_loaded += vol->brick_bytes;
+        }
+        else if (vol->kind == SRC_BLOB_DEVICE)
+        {
+            gen_ids.push_back(id);
+            gen_offsets.push_back(uint64_t(unit) * kSlotUnit);
+        }
+        else
+        {
+            PinnedBuffer* buf = vol->staging[ring];
+            LV_CUDA(ctx, cudaEventSynchronize(vol->staging_ev[ring]));
+            const int rc = vol->fn(vol->user, id, buf->ptr, vol->brick_bytes);
+            if (rc != 0)
+            {
+                /* null MemoryUnitPtr: the brick is skipped
+                 * (DataUploadFilter.cpp:56-64); give the slot back */
+                P.free_by_units[vol->slot_units].push_back(unit);
+                continue;
+            }
+            LV_CUDA(ctx, cudaMemcpyAsync(dst, buf->ptr, vol->brick_bytes,
+                                         cudaMemcpyHostToDevice, up));
+            LV_CUDA(ctx, cudaEventRecord(vol->staging_ev[ring], up));
+            ring = (ring + 1) % vol->staging.size();
+            bytes_loaded += vol->brick_bytes;
+        }
+        vol->host_table[idx] = int32_t(unit);
+        updates.push_back({vol, {idx, int32_t(unit)}});
+        P.lru.push_back(Resident{vol, idx, unit, vol->slot_units});
+        P.resident_bytes += uint64_t(vol->slot_units) * kSlotUnit;
+        ++n_loaded;
+    }
+    if (!gen_ids.empty())
+    {
+        DeviceBuffer dids;
+        LV_CUDA(ctx, dids.reserve(sizeof(uint64_t) * 2 * gen_ids.size()));
+        PinnedBuffer h;
+        LV_CUDA(ctx, h.reserve(sizeof(uint64_t) * 2 * gen_ids.size()));
+        std::memcpy(h.ptr, gen_ids.data(), sizeof(uint64_t) * gen_ids.size());
+        std::memcpy(h.as<uint64_t>() + gen_ids.size(), gen_offsets.data(),
+                    sizeof(uint64_t) * gen_offsets.size());
+        LV_CUDA(ctx, cudaMemcpyAsync(dids.ptr, h.ptr, sizeof(uint64_t) * 2 * gen_ids.size(),
+                                     cudaMemcpyHostToDevice, up));
+        lv_status g = launch_blob_bricks(ctx, vol->info, vol->blob,
+                                         vol->d_blobs.as<Blob>(), dids.as<uint64_t>(),
+                                         uint32_t(gen_ids.size()), arena,
+                                         dids.as<uint64_t>() + gen_ids.size(), up);
+        if (g != LV_OK)
+            return g;
+        /* temporaries die at scope exit */
+        LV_CUDA(ctx, cudaStreamSynchronize(up));
+    }
+    lv_status u = apply_updates(ctx, updates, up);
+    if (u != LV_OK)
+        return u;
+    LV_CUDA(ctx, cudaEventRecord(R.upload_event, up));
+    LV_CUDA(ctx, cudaStreamWaitEvent(render, R.upload_event, 0));
+    return st;
+}
+
+void volume_layout(lv_volume* v)
+{
+    uint64_t off = 0;
+    for (uint32_t L = 0; L <= kMaxLevels; ++L)
+    {
+        v->level_offset[L] = off;
+        if (L < v->info.depth)
+            off += (uint64_t(v->info.root_blocks[0]) << L) *
+                   (uint64_t(v->info.root_blocks[1]) << L) *
+                   (uint64_t(v->info.root_blocks[2]) << L);
+    }
+    v->n_nodes = off;
+    v->brick_bytes = uint64_t(v->info.max_block[0]) * v->info.max_block[1] *
+                     v->info.max_block[2] * bytes_per_voxel(v->info.dtype) *
+                     v->info.comp_count;
+    v->slot_units = uint32_t(round_units(v->brick_bytes));
+}
+
+lv_status volume_init(lv_ctx* ctx, lv_volume* v)
+{
+    if (v->info.depth == 0 || v->info.depth > kMaxLevels)
+        return fail(ctx, LV_EINVAL, "volume depth must be 1..15 (fill the info first)");
+    if (bytes_per_voxel(v->info.dtype) == 0 || v->info.comp_count != 1)
+        return fail(ctx, LV_EINVAL, "unsupported voxel type or component count");
+    volume_layout(v);
+    if (v->n_nodes > (uint64_t(1) << 28))
+        return fail(ctx, LV_EINVAL, "octree too large for a dense page table");
+    lv_status st = ensure_pool(ctx);
+    if (st != LV_OK)
+        return st;
+    st = ensure_renderer(ctx);
+    if (st != LV_OK)
+        return st;
+    LV_CUDA(ctx, v->node_table.reserve(sizeof(int32_t) * v->n_nodes));
+    LV_CUDA(ctx, v->node_stamp.reserve(sizeof(uint32_t) * v->n_nodes));
+    fill_i32_kernel<<<256, 256, 0, ctx->upload_stream>>>(v->node_table.as<int32_t>(),
+                                                         v->n_nodes, -1);
+    LV_CUDA(ctx, cudaMemsetAsync(v->node_stamp.ptr, 0, sizeof(uint32_t) * v->n_nodes,
+                                 ctx->upload_stream));
+    LV_CUDA(ctx, cudaStreamSynchronize(ctx->upload_stream));
+    v->host_table.assign(v->n_nodes, -1);
+    return LV_OK;
+}
+
+void drop_volume_residency(lv_ctx* ctx, lv_volume* v)
+{
+    if (!ctx->pool)
+        return;
+    Pool& P = *ctx->pool;
+    for (auto it = P.lru.begin(); it != P.lru.end();)
+    {
+        if (it->vol == v)
+        {
+            P.free_by_units[it->units].push_back(it->unit);
+            P.resident_bytes -= uint64_t(it->units) * kSlotUnit;
+            it = P.lru.erase(it);
+        }
+        else
+            ++it;
+    }
+}
+
+} // namespace
+} // namespace lv
+
+/* ================================================================ C ABI */
+using namespace lv;
+
+extern "C" uint32_t lv_abi_version(void) { return LV_ABI_VERSION; }
+
+extern "C" lv_status lv_fill_regular_volume_info(lv_volume_info* info)
+{
+    /* livre/data/DataSourcePlugin.cpp:73-95 */
+    if (!info)
+        return LV_EINVAL;
+    const uint32_t maxv =
+        std::max(info->voxels[0], std::max(info->voxels[1], info->voxels[2]));
+    if (maxv == 0)
+        return LV_EINVAL;
+    info->world_space_per_voxel = 1.0f / float(maxv);
+    uint32_t bs[3], lod[3];
+    for (int i = 0; i < 3; ++i)
+    {
+        info->world_size[i] = float(info->voxels[i]) * info->world_space_per_voxel;
+        if (info->max_block[i] <= 2u * info->overlap[i])
+            return LV_EINVAL;
+        bs[i] = info->max_block[i] - 2u * info->overlap[i];
+        const uint32_t nb = uint32_t(std::ceil(float(info->voxels[i]) / float(bs[i])));
+        lod[i] = uint32_t(std::ceil(std::log2(double(nb))));
+    }
+    const uint32_t depth = std::min(lod[0], std::min(lod[1], lod[2]));
+    for (int i = 0; i < 3; ++i)
+        info->root_blocks[i] =
+            uint32_t(std::ceil(float(info->voxels[i] >> depth) / float(bs[i])));
+    info->depth = depth + 1;
+    if (info->comp_count == 0)
+        info->comp_count = 1;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_ctx_create(int device, lv_ctx** out)
+{
+    if (!out)
+        return LV_EINVAL;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+        return LV_EDEVICE;
+    if (cudaSetDevice(device) != cudaSuccess)
+        return LV_EDEVICE;
+    lv_ctx* ctx = new lv_ctx();
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->upload_stream, cudaStreamNonBlocking) !=
+        cudaSuccess)
+    {
+        delete ctx;
+        return LV_EDEVICE;
+    }
+    *out = ctx;
+    return LV_OK;
+}
+
+extern "C" void lv_ctx_destroy(lv_ctx* ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    if (ctx->renderer)
+    {
+        cudaEventDestroy(ctx->renderer->pending_event);
+        cudaEventDestroy(ctx->renderer->render_event);
+        cudaEventDestroy(ctx->renderer->upload_event);
+        cudaEventDestroy(ctx->renderer->t_sel0);
+        cudaEventDestroy(ctx->renderer->t_sel1);
+        cudaEventDestroy(ctx->renderer->t_ray0);
+        cudaEventDestroy(ctx->renderer->t_ray1);
+        delete ctx->renderer;
+    }
+    delete ctx->pool;
+    if (ctx->upload_stream)
+        cudaStreamDestroy(ctx->upload_stream);
+    delete ctx;
+}
+
+extern "C" const char* lv_last_error(const lv_ctx* ctx)
+{
+    return ctx ? ctx->error.c_str() : "null context";
+}
+
+extern "C" lv_status lv_pool_configure(lv_ctx* ctx, size_t bytes)
+{
+    if (!ctx)
+        return LV_EINVAL;
+    if (ctx->pool)
+        return fail(ctx, LV_EINVAL, "pool already allocated");
+    if (bytes < kSlotUnit || bytes / kSlotUnit > (uint64_t(1) << kLeafSlotBits))
+        return fail(ctx, LV_EINVAL, "pool size must be in [1 KiB, 128 GiB]");
+    ctx->pool_bytes = bytes;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_pool_purge(lv_ctx* ctx)
+{
+    if (!ctx)
+        return LV_EINVAL;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    if (!ctx->pool)
+        return LV_OK;
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    LV_CUDA(ctx, cudaDeviceSynchronize());
+    Pool& P = *ctx->pool;
+    std::vector<lv_volume*> vols;
+    for (auto& r : P.lru)
+        if (std::find(vols.begin(), vols.end(), r.vol) == vols.end())
+            vols.push_back(r.vol);
+    for (lv_volume* v : vols)
+    {
+        std::fill(v->host_table.begin(), v->host_table.end(), -1);
+        fill_i32_kernel<<<256, 256, 0, ctx->upload_stream>>>(v->node_table.as<int32_t>(),
+                                                             v->n_nodes, -1);
+    }
+    LV_CUDA(ctx, cudaStreamSynchronize(ctx->upload_stream));
+    P.lru.clear();
+    P.free_by_units.clear();
+    P.bump = 0;
+    P.resident_bytes = 0;
+    if (ctx->renderer)
+        ctx->renderer->pending_vol = nullptr;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_volume_create(lv_ctx* ctx, const lv_volume_info* info,
+                                      lv_get_data_fn get_data, void* user,
+                                      lv_volume** out)
+{
+    if (!ctx || !info || !get_data || !out)
+        return fail(ctx, LV_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    lv_volume* v = new lv_volume();
+    v->ctx = ctx;
+    v->info = *info;
+    v->kind = SRC_CALLBACK;
+    v->fn = get_data;
+    v->user = user;
+    lv_status st = volume_init(ctx, v);
+    if (st == LV_OK)
+    {
+        for (int i = 0; i < 4; ++i)
+        {
+            PinnedBuffer* b = new PinnedBuffer();
+            v->staging.push_back(b);
+            cudaEvent_t e;
+            cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            v->staging_ev.push_back(e);
+            if (b->reserve(v->brick_bytes) != cudaSuccess)
+            {
+                st = fail(ctx, LV_ENOMEM, "pinned staging allocation");
+                break;
+            }
+        }
+    }
+    if (st != LV_OK)
+    {
+        delete v;
+        return st;
+    }
+    *out = v;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_volume_create_blob(lv_ctx* ctx, const lv_volume_info* info,
+                                           const lv_blob_desc* blob,
+                                           uint32_t placement, lv_volume** out)
+{
+    if (!ctx || !info || !blob || !out)
+        return fail(ctx, LV_EINVAL, "null argument");
+    if (info->dtype != LV_DT_UINT8 && info->dtype != LV_DT_UINT16)
+        return fail(ctx, LV_EINVAL, "blob volumes are uint8 or uint16");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    lv_volume* v = new lv_volume();
+    v->ctx = ctx;
+    v->info = *info;
+    v->blob = *blob;
+    v->kind = placement == LV_BLOB_HOST ? SRC_BLOB_HOST : SRC_BLOB_DEVICE;
+    lv_status st = volume_init(ctx, v);
+    if (st != LV_OK)
+    {
+        delete v;
+        return st;
+    }
+    const std::vector<Blob> blobs = make_blobs(*info, *blob);
+    cudaStream_t s = ctx->upload_stream;
+    if (v->d_blobs.reserve(sizeof(Blob) * (blobs.size() + 1)) != cudaSuccess ||
+        cudaMemcpy(v->d_blobs.ptr, blobs.data(), sizeof(Blob) * blobs.size(),
+                   cudaMemcpyHostToDevice) != cudaSuccess)
+    {
+        delete v;
+        return fail(ctx, LV_ENOMEM, "blob table");
+    }
+    if (v->kind == SRC_BLOB_HOST)
+    {
+        /* materialise every brick once into page-locked host memory */
+        if (v->host_store.reserve(v->n_nodes * v->brick_bytes) != cudaSuccess)
+        {
+            delete v;
+            return fail(ctx, LV_ENOMEM, "host brick store allocation");
+        }
+        const uint64_t batch = std::max<uint64_t>(1, (uint64_t(256) << 20) / v->brick_bytes);
+        DeviceBuffer tmp, dids;
+        PinnedBuffer hids;
+        if (tmp.reserve(batch * v->brick_bytes) != cudaSuccess ||
+            dids.reserve(sizeof(uint64_t) * batch) != cudaSuccess ||
+            hids.reserve(sizeof(uint64_t) * batch) != cudaSuccess)
+        {
+            delete v;
+            return fail(ctx, LV_ENOMEM, "generation buffers");
+        }
+        uint64_t idx = 0;
+        for (uint32_t L = 0; L < info->depth; ++L)
+        {
+            const uint32_t bx = info->root_blocks[0] << L, by = info->root_blocks[1] << L,
+                           bz = info->root_blocks[2] << L;
+            const uint64_t nl = uint64_t(bx) * by * bz;
+            for (uint64_t first = 0; first < nl; first += batch)
+            {
+                const uint64_t cnt = std::min(batch, nl - first);
+                if (cudaStreamSynchronize(s) != cudaSuccess)
+                {
+                    delete v;
+                    return fail(ctx, LV_EDEVICE, "generation");
+                }
+                for (uint64_t k = 0; k < cnt; ++k)
+                {
+                    const uint64_t lin = first + k; /* (x * by + y) * bz + z */
+                    const uint32_t z = uint32_t(lin % bz), y = uint32_t((lin / bz) % by),
+                                   x = uint32_t(lin / (uint64_t(by) * bz));
+                    hids.as<uint64_t>()[k] = nid_make(L, x, y, z, 0);
+                }
+                cudaMemcpyAsync(dids.ptr, hids.ptr, sizeof(uint64_t) * cnt,
+                                cudaMemcpyHostToDevice, s);
+                st = launch_blob_bricks(ctx, *info, *blob, v->d_blobs.as<Blob>(),
+                                        dids.as<uint64_t>(), uint32_t(cnt),
+                                        tmp.as<uint8_t>(), nullptr, s);
+                if (st != LV_OK)
+                {
+                    delete v;
+                    return st;
+                }
+                cudaMemcpyAsync(v->host_store.as<uint8_t>() + (idx + first) * v->brick_bytes,
+                                tmp.ptr, cnt * v->brick_bytes, cudaMemcpyDeviceToHost, s);
+            }
+            idx += nl;
+        }
+        if (cudaStreamSynchronize(s) != cudaSuccess)
+        {
+            delete v;
+            return fail(ctx, LV_EDEVICE, "generation");
+        }
+    }
+    *out = v;
+    return LV_OK;
+}
+
+extern "C" void lv_volume_destroy(lv_volume* v)
+{
+    if (!v)
+        return;
+    lv_ctx* ctx = v->ctx;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mutex);
+        cudaSetDevice(ctx->device);
+        cudaDeviceSynchronize();
+        drop_volume_residency(ctx, v);
+        if (ctx->renderer && ctx->renderer->pending_vol == v)
+            ctx->renderer->pending_vol = nullptr;
+    }
+    delete v;
+}
+
+extern "C" lv_status lv_volume_load(lv_volume* v, const uint64_t* ids, uint32_t n,
+                                    uint32_t* n_loaded)
+{
+    if (!v || (n && !ids))
+        return LV_EINVAL;
+    lv_ctx* ctx = v->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->upload_stream;
+    LV_CUDA(ctx, cudaDeviceSynchronize());
+    uint32_t loaded = 0;
+    uint64_t bytes = 0;
+    /* nothing is in flight: no brick is protected from eviction */
+    const uint32_t protect = ctx->renderer->frame + 1u;
+    lv_status st = stream_bricks(ctx, v, ids, n, protect, s, loaded, bytes);
+    LV_CUDA(ctx, cudaStreamSynchronize(s));
+    if (n_loaded)
+        *n_loaded = loaded;
+    return st;
+}
+
+extern "C" lv_status lv_volume_resident(const lv_volume* v, uint64_t* ids,
+                                        uint32_t capacity, uint32_t* n)
+{
+    if (!v || !n || (capacity && !ids))
+        return LV_EINVAL;
+    lv_ctx* ctx = v->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    uint32_t k = 0;
+    for (const Resident& r : ctx->pool->lru)
+    {
+        if (r.vol != v)
+            continue;
+        if (k < capacity)
+        {
+            uint32_t L = 0;
+            while (L + 1 < v->info.depth && v->level_offset[L + 1] <= r.node_idx)
+                ++L;
+            const uint64_t local = r.node_idx - v->level_offset[L];
+            const uint64_t by = uint64_t(v->info.root_blocks[1]) << L;
+            const uint64_t bz = uint64_t(v->info.root_blocks[2]) << L;
+            const uint32_t z = uint32_t(local % bz), y = uint32_t((local / bz) % by),
+                           x = uint32_t(local / (by * bz));
+            ids[k] = nid_make(L, x, y, z, v->time_step);
+        }
+        ++k;
+    }
+    *n = k;
+    return k > capacity ? LV_ENOMEM : LV_OK;
+}
+
+extern "C" lv_status lv_volume_get_info(const lv_volume* v, lv_volume_info* out)
+{
+    if (!v || !out)
+        return LV_EINVAL;
+    *out = v->info;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_tf_create(lv_ctx* ctx, const float* rgba, uint32_t n,
+                                  lv_tf** out)
+{
+    if (!ctx || !rgba || !out || n == 0)
+        return fail(ctx, LV_EINVAL, "empty transfer function");
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    lv_tf* tf = new lv_tf();
+    tf->ctx = ctx;
+    tf->n = n;
+    if (tf->rgba.reserve(sizeof(float) * 4 * n) != cudaSuccess ||
+        cudaMemcpy(tf->rgba.ptr, rgba, sizeof(float) * 4 * n, cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+    {
+        delete tf;
+        return fail(ctx, LV_ENOMEM, "transfer function upload");
+    }
+    *out = tf;
+    return LV_OK;
+}
+
+extern "C" void lv_tf_destroy(lv_tf* tf)
+{
+    if (!tf)
+        return;
+    cudaSetDevice(tf->ctx->device);
+    cudaDeviceSynchronize();
+    delete tf;
+}
+
+namespace lv
+{
+namespace
+{
+/* Streams up to `max` misses of the previous async frame. */
+lv_status process_pending(lv_ctx* ctx, cudaStream_t s)
+{
+    Renderer& R = *ctx->renderer;
+    if (!R.pending_vol)
+        return LV_OK;
+    LV_CUDA(ctx, cudaEventSynchronize(R.pending_event));
+    lv_volume* v = R.pending_vol;
+    R.pending_vol = nullptr;
+    const uint32_t* hc = R.h_counters.as<uint32_t>();
+    const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING],
+                                                uint32_t(R.h_missing.bytes / sizeof(uint64_t)));
+    const uint32_t n = std::min(missing, R.pending_max);
+    uint32_t loaded = 0;
+    uint64_t bytes = 0;
+    lv_status st = stream_bricks(ctx, v, R.h_missing.as<uint64_t>(), n, R.pending_frame,
+                                 s, loaded, bytes);
+    R.stats.n_uploaded += loaded;
+    R.stats.bytes_uploaded += bytes;
+    return st == LV_EAGAIN ? LV_OK : st;
+}
+} // namespace
+} // namespace lv
+
+extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
+                               const lv_render_desc* desc, float* d_rgba,
+                               void* stream)
+{
+    if (!ctx || !vol || !tf || !desc || !d_rgba)
+        return fail(ctx, LV_EINVAL, "null argument");
+    if (desc->width == 0 || desc->height == 0)
+        return fail(ctx, LV_EINVAL, "empty viewport");
+    if (vol->ctx != ctx || tf->ctx != ctx)
+        return fail(ctx, LV_EINVAL, "volume or transfer function of another context");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    Renderer& R = *ctx->renderer;
+    const lv_volume_info& info = vol->info;
+
+    lv_frame_stats stats{};
+    R.stats = stats;
+    /* async: bricks missed by the previous frame are streamed now */
+    if (!desc->synchronous)
+    {
+        lv_status st = process_pending(ctx, s);
+        if (st != LV_OK)
+            return st;
+    }
+    else
+        R.pending_vol = nullptr;
+    const uint32_t frame = ++R.frame;
+
+    if (desc->lod.time_step != vol->time_step)
+    {
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        drop_volume_residency(ctx, vol);
+        std::fill(vol->host_table.begin(), vol->host_table.end(), -1);
+        fill_i32_kernel<<<256, 256, 0, s>>>(vol->node_table.as<int32_t>(), vol->n_nodes, -1);
+        vol->time_step = desc->lod.time_step;
+    }
+
+    /* buffers */
+    if (R.visible_capacity < vol->n_nodes)
+    {
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        const uint64_t cap = vol->n_nodes;
+        LV_CUDA(ctx, R.visible.reserve(sizeof(uint64_t) * cap));
+        LV_CUDA(ctx, R.render_ids.reserve(sizeof(uint64_t) * cap));
+        LV_CUDA(ctx, R.render_slots.reserve(sizeof(uint32_t) * cap));
+        LV_CUDA(ctx, R.missing.reserve(sizeof(uint64_t) * cap));
+        LV_CUDA(ctx, R.h_missing.reserve(sizeof(uint64_t) * cap));
+        R.visible_capacity = cap;
+    }
+    uint32_t dims[3];
+    const uint32_t Lf = info.depth - 1u;
+    for (int a = 0; a < 3; ++a)
+        dims[a] = info.root_blocks[a] << Lf;
+    const uint64_t cells = uint64_t(dims[0]) * dims[1] * dims[2];
+    if (R.leaf.bytes < cells * sizeof(uint32_t))
+    {
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        LV_CUDA(ctx, R.leaf.reserve(cells * sizeof(uint32_t)));
+    }
+    lv_status st = reserve_selection(ctx, info, s);
+    if (st != LV_OK)
+        return st;
+
+    /* 1. LOD selection */
+    lv_lod_params lod = desc->lod;
+    if (lod.window_height == 0)
+        lod.window_height = desc->height;
+    LodView LV;
+    st = make_lod_view(ctx, info, desc->camera, lod, LV);
+    if (st != LV_OK)
+        return st;
+    LV.out_ids = R.visible.as<uint64_t>();
+    LV.capacity = uint32_t(std::min<uint64_t>(R.visible_capacity, 0xFFFFFFFFu));
+    LV.result = R.sel_result.as<uint32_t>();
+    /* kernels: roots + one per level + finish, resolve (x2 on a sync miss),
+     * leaf fill, step, ray cast */
+    R.launches = info.depth + 2u + 4u;
+    LV_CUDA(ctx, cudaEventRecord(R.t_sel0, s));
+    st = run_selection(ctx, &LV, 1, info.depth, s);
+    if (st != LV_OK)
+        return st;
+    LV_CUDA(ctx, cudaEventRecord(R.t_sel1, s));
+    if (!(lod.range[0] == 0.0f && lod.range[1] == 1.0f))
+    {
+        st = range_slice(ctx, info, lod.range, R.visible.as<uint64_t>(),
+                         R.sel_result.as<uint32_t>(), s);
+        if (st != LV_OK)
+            return st;
+    }
+
+    /* 2. residency */
+    ResolveView RV;
+    std::memset(&RV, 0, sizeof(RV));
+    RV.visible = R.visible.as<uint64_t>();
+    RV.n_visible_ptr = R.sel_result.as<uint32_t>() + LV_SEL_WRITTEN;
+    RV.node_table = vol->node_table.as<int32_t>();
+    RV.node_stamp = vol->node_stamp.as<uint32_t>();
+    RV.frame = frame;
+    RV.depth = info.depth;
+    for (int a = 0; a < 3; ++a)
+    {
+        RV.root_blocks[a] = info.root_blocks[a];
+        RV.dims[a] = dims[a];
+    }
+    std::memcpy(RV.level_offset, vol->level_offset, sizeof(RV.level_offset));
+    RV.synchronous = desc->synchronous ? 1u : 0u;
+    RV.render_ids = R.render_ids.as<uint64_t>();
+    RV.render_slots = R.render_slots.as<uint32_t>();
+    RV.render_capacity = uint32_t(R.visible_capacity);
+    RV.missing = R.missing.as<uint64_t>();
+    RV.missing_capacity = uint32_t(R.visible_capacity);
+    RV.counters = R.counters.as<uint32_t>();
+    RV.leaf = R.leaf.as<uint32_t>();
+    RV.Lf = Lf;
+    LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
+    st = launch_resolve(ctx, RV, s);
+    if (st != LV_OK)
+        return st;
+    if (desc->synchronous)
+    {
+        uint32_t* hc = R.h_counters.as<uint32_t>();
+        LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
+                                     cudaMemcpyDeviceToHost, s));
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
+        if (missing)
+        {
+            LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
+                                         sizeof(uint64_t) * missing,
+                                         cudaMemcpyDeviceToHost, s));
+            LV_CUDA(ctx, cudaStreamSynchronize(s));
+            uint32_t loaded = 0;
+            uint64_t bytes = 0;
+            st = stream_bricks(ctx, vol, R.h_missing.as<uint64_t>(), missing, frame, s,
+                               loaded, bytes);
+            R.stats.n_uploaded += loaded;
+            R.stats.bytes_uploaded += bytes;
+            if (st != LV_OK && st != LV_EAGAIN)
+                return st;
+            /* resolve again with the streamed bricks; what still misses
+             * (pool too small) is not rendered */
+            LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
+            st = launch_resolve(ctx, RV, s);
+            if (st != LV_OK)
+                return st;
+            R.launches += 1u;
+        }
+    }
+
+    /* 3. leaf grid */
+    LV_CUDA(ctx, cudaMemsetAsync(R.leaf.ptr, 0xFF, cells * sizeof(uint32_t), s));
+    st = launch_leaf_fill(ctx, RV, s);
+    if (st != LV_OK)
+        return st;
+
+    /* 4. ray cast */
+    RayView V;
+    std::memset(&V, 0, sizeof(V));
+    float lim[6], planes[6][4], eye[3], dir[3];
+    bool ok = false;
+    frustum_setup(desc->camera.modelview, desc->camera.projection, V.inv_mv, V.inv_p,
+                  lim, planes, eye, dir, &ok);
+    if (!ok)
+        return fail(ctx, LV_EINVAL, "singular camera");
+    const uint32_t bm = std::max(dims[0], std::max(dims[1], dims[2]));
+    for (int a = 0; a < 3; ++a)
+    {
+        V.eye[a] = eye[a];
+        const float half = info.world_size[a] / 2.0f;
+        V.gmin[a] = -half;
+        V.gmax[a] = half;
+        V.gscale[a] = float(bm) / info.world_size[a];
+        V.dims[a] = dims[a];
+        V.N[a] = info.max_block[a];
+        V.O[a] = info.overlap[a];
+        V.B[a] = info.max_block[a] - 2u * info.overlap[a];
+    }
+    V.nearp = lim[4];
+    V.n_clip = lod.n_clip_planes;
+    std::memcpy(V.clip, lod.clip_planes, sizeof(V.clip));
+    V.Lf = Lf;
+    V.dtype = info.dtype;
+    V.filter = desc->filter;
+    float lo = desc->data_range[0], hi = desc->data_range[1];
+    if (!(hi > lo))
+        type_range(info.dtype, lo, hi);
+    V.dmul = 1.0f / (hi - lo);
+    V.dadd = -lo / (hi - lo);
+    V.early = desc->early_exit;
+    V.W = desc->width;
+    V.H = desc->height;
+    V.samples_fixed = desc->samples_per_ray;
+    V.step_policy = desc->step_policy;
+    V.max_voxel_dim = std::max(info.voxels[0], std::max(info.voxels[1], info.voxels[2]));
+    V.depth = info.depth;
+    V.leaf = R.leaf.as<uint32_t>();
+    V.pool = ctx->pool->arena.as<uint8_t>();
+    V.tf = tf->rgba.as<float4>();
+    V.tfn = tf->n;
+    V.out = reinterpret_cast<float4*>(d_rgba);
+    V.counters = R.counters.as<uint32_t>();
+    LV_CUDA(ctx, cudaEventRecord(R.t_ray0, s));
+    st = launch_raycast(ctx, V, s);
+    if (st != LV_OK)
+        return st;
+    LV_CUDA(ctx, cudaEventRecord(R.t_ray1, s));
+
+    /* 5. copy back counters (+ misses in async mode) */
+    uint32_t* hc = R.h_counters.as<uint32_t>();
+    LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
+                                 cudaMemcpyDeviceToHost, s));
+    LV_CUDA(ctx, cudaMemcpyAsync(hc + FC_WORDS, R.sel_result.ptr,
+                                 sizeof(uint32_t) * LV_SELECT_RESULT_WORDS,
+                                 cudaMemcpyDeviceToHost, s));
+    if (!desc->synchronous)
+    {
+        LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
+                                     sizeof(uint64_t) * std::min<uint64_t>(R.visible_capacity, 4096),
+                                     cudaMemcpyDeviceToHost, s));
+        LV_CUDA(ctx, cudaEventRecord(R.pending_event, s));
+        R.pending_vol = vol;
+        R.pending_max = desc->max_uploads;
+        R.pending_frame = frame;
+    }
+    R.last_stream = s;
+    R.have_last = true;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)
+{
+    if (!ctx || !out)
+        return LV_EINVAL;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    if (!ctx->renderer || !ctx->renderer->have_last)
+        return fail(ctx, LV_EINVAL, "no frame rendered");
+    Renderer& R = *ctx->renderer;
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    LV_CUDA(ctx, cudaStreamSynchronize(R.last_stream));
+    const uint32_t* hc = R.h_counters.as<uint32_t>();
+    const uint32_t* sel = hc + FC_WORDS;
+    lv_frame_stats s = R.stats;
+    s.n_visible = sel[LV_SEL_WRITTEN];
+    s.n_visited = sel[LV_SEL_VISITED];
+    s.n_rendered = hc[FC_RENDERED];
+    s.n_available = hc[FC_AVAILABLE];
+    s.n_not_available = hc[FC_NOT_AVAILABLE];
+    s.max_level = hc[FC_MAX_LEVEL] ? hc[FC_MAX_LEVEL] - 1u : 0u;
+    s.samples_per_ray = hc[FC_SAMPLES_PER_RAY];
+    s.n_samples = uint64_t(hc[FC_SAMPLES_LO]) | (uint64_t(hc[FC_SAMPLES_HI]) << 32);
+    s.n_launches = R.launches;
+    cudaEventElapsedTime(&s.select_ms, R.t_sel0, R.t_sel1);
+    cudaEventElapsedTime(&s.raycast_ms, R.t_ray0, R.t_ray1);
+    *out = s;
+    if (hc[FC_ERROR])
+        return fail(ctx, LV_ENOMEM, "rendering set overflowed its buffer");
+    return LV_OK;
+}
