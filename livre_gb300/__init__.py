@@ -320,6 +320,7 @@ def make_lod(window_height, sse, min_lod=0, max_lod=100, rng=(0.0, 1.0), time_st
 class Volume:
     def __init__(self, ctx, handle, info, keepalive=None):
         self.ctx, self.handle, self.info, self._keep = ctx, handle, info, keepalive
+        ctx._children.add(self)
 
     def load(self, node_ids):
         """Cache::load of explicit bricks; returns how many were streamed."""
@@ -342,6 +343,7 @@ class Volume:
         if self.handle:
             lib().lv_volume_destroy(self.handle)
             self.handle = None
+            self.ctx._children.discard(self)
 
     def __del__(self):
         try:
@@ -358,11 +360,13 @@ class TransferFunction:
         check(lib().lv_tf_create(ctx.handle, self.rgba.ctypes.data_as(C.POINTER(C.c_float)),
                                  self.rgba.shape[0], C.byref(h)), ctx.handle)
         self.handle = h
+        ctx._children.add(self)
 
     def close(self):
         if self.handle:
             lib().lv_tf_destroy(self.handle)
             self.handle = None
+            self.ctx._children.discard(self)
 
     def __del__(self):
         try:
@@ -375,6 +379,9 @@ class Context:
     """One CUDA device; owns the brick pool (lv_ctx)."""
 
     def __init__(self, device=0, pool_bytes=None):
+        import weakref
+        self._children = weakref.WeakSet()
+        self.handle = None
         h = C.c_void_p()
         check(lib().lv_ctx_create(int(device), C.byref(h)))
         self.handle = h
@@ -383,7 +390,11 @@ class Context:
             check(lib().lv_pool_configure(h, int(pool_bytes)), h)
 
     def close(self):
+        """Destroys the volumes and transfer functions of this context, then it
+        (the C ABI requires children to go first)."""
         if self.handle:
+            for child in list(self._children):
+                child.close()
             lib().lv_ctx_destroy(self.handle)
             self.handle = None
 

@@ -102,6 +102,8 @@ enum FrameCounter
     FC_SAMPLES_LO = 6,    /* 64-bit composited-sample counter */
     FC_SAMPLES_HI = 7,
     FC_ERROR = 8,         /* nonzero: an index check failed in a kernel */
+    FC_KEPT = 9,          /* rendering-set entries left after dropping the
+                             ones with an ancestor in the set */
     FC_WORDS = 16
 };
 

@@ -46,7 +46,6 @@ __device__ __forceinline__ void emit_render(const ResolveView& R, uint64_t id,
     }
     else
         atomicExch(&R.counters[FC_ERROR], 1u);
-    atomicMax(&R.counters[FC_MAX_LEVEL], nid_level(id) + 1u);
 }
 
 /* For each visible id: resident -> rendering set; missing -> missing list
@@ -91,6 +90,38 @@ __global__ void resolve_kernel(ResolveView R)
     }
 }
 
+/* Drops rendering-set entries that have an ancestor in the set, as
+ * RenderingSetGenerator::generateRenderingSet does (RenderingSetGeneratorFilter
+ * .cpp:63-79): every entry of this frame carries node_stamp == frame. */
+__global__ void prune_kernel(ResolveView R)
+{
+    const uint32_t n = min(R.counters[FC_RENDERED], R.render_capacity);
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += gridDim.x * blockDim.x)
+    {
+        const uint64_t id = R.render_ids[e];
+        uint64_t cur = id;
+        bool shadowed = false;
+        while (nid_level(cur) > 0)
+        {
+            cur = nid_make(nid_level(cur) - 1u, nid_x(cur) >> 1, nid_y(cur) >> 1,
+                           nid_z(cur) >> 1, nid_t(cur));
+            if (R.node_stamp[node_index(R.level_offset, R.root_blocks, cur)] == R.frame)
+            {
+                shadowed = true;
+                break;
+            }
+        }
+        if (shadowed)
+            R.render_ids[e] = kInvalidNode;
+        else
+        {
+            atomicAdd(&R.counters[FC_KEPT], 1u);
+            atomicMax(&R.counters[FC_MAX_LEVEL], nid_level(id) + 1u);
+        }
+    }
+}
+
 /* Splats the rendering set into the leaf grid; one warp per entry. */
 __global__ void leaf_fill_kernel(ResolveView R)
 {
@@ -101,6 +132,8 @@ __global__ void leaf_fill_kernel(ResolveView R)
     for (uint32_t e = warp; e < n; e += nwarps)
     {
         const uint64_t id = R.render_ids[e];
+        if (id == kInvalidNode)
+            continue;
         const uint32_t slot = R.render_slots[e];
         const uint32_t L = nid_level(id);
         const uint32_t sh = R.Lf - L;
@@ -424,6 +457,8 @@ lv_status launch_leaf_fill(lv_ctx* ctx, const ResolveView& R, cudaStream_t s)
 {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    prune_kernel<<<sms, 256, 0, s>>>(R);
+    LV_CUDA(ctx, cudaGetLastError());
     leaf_fill_kernel<<<2 * sms, 256, 0, s>>>(R);
     LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;

@@ -978,8 +978,8 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     LV.capacity = uint32_t(std::min<uint64_t>(R.visible_capacity, 0xFFFFFFFFu));
     LV.result = R.sel_result.as<uint32_t>();
     /* kernels: roots + one per level + finish, resolve (x2 on a sync miss),
-     * leaf fill, step, ray cast */
-    R.launches = info.depth + 2u + 4u;
+     * prune, leaf fill, step, ray cast */
+    R.launches = info.depth + 2u + 5u;
     LV_CUDA(ctx, cudaEventRecord(R.t_sel0, s));
     st = run_selection(ctx, &LV, 1, info.depth, s);
     if (st != LV_OK)
@@ -1147,7 +1147,7 @@ extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)
     lv_frame_stats s = R.stats;
     s.n_visible = sel[LV_SEL_WRITTEN];
     s.n_visited = sel[LV_SEL_VISITED];
-    s.n_rendered = hc[FC_RENDERED];
+    s.n_rendered = hc[FC_KEPT];
     s.n_available = hc[FC_AVAILABLE];
     s.n_not_available = hc[FC_NOT_AVAILABLE];
     s.max_level = hc[FC_MAX_LEVEL] ? hc[FC_MAX_LEVEL] - 1u : 0u;
