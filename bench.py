@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--config", default="plain2048", choices=sorted(CONFIGS))
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-rows", type=int, default=12)
+    p.add_argument("--pool-gib", type=int, default=None,
+                   help="brick pool size (default: the config's)")
     return p.parse_args()
 
 
@@ -197,7 +199,7 @@ def gb300_arm(args, cfg):
     stream = torch.cuda.current_stream(dev)
     W, H = cfg["width"], cfg["height"]
 
-    ctx = lv.Context(local, pool_bytes=cfg["pool_gib"] << 30)
+    ctx = lv.Context(local, pool_bytes=(args.pool_gib or cfg["pool_gib"]) << 30)
     vi = lv.VolumeInformation(cfg["voxels"], cfg["block"], cfg["overlap"])
     t0 = time.time()
     vol = ctx.blob_volume(vi, cfg["n_blobs"], cfg["seed"], cfg["noise"], placement=lv.BLOB_HOST)

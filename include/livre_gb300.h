@@ -264,6 +264,58 @@ lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
  * its stream). */
 lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out);
 
+/* --------------------------------------------------------- batched mode */
+
+typedef struct lv_batch lv_batch;
+
+/* One view of a batch. desc.synchronous is ignored: a batch renders the
+ * nearest resident ancestor of a missing brick and streams up to
+ * desc.max_uploads misses per view before the next launch (the reference's
+ * asynchronous mode, livre/lib/pipeline/RenderPipeline.cpp:160-225).
+ * desc.lod.range must be {0, 1}. */
+typedef struct lv_batch_view
+{
+    lv_volume* volume;
+    lv_tf* tf;
+    lv_render_desc desc;
+    float* d_rgba; /* width*height RGBA32F on the device */
+} lv_batch_view;
+
+/* Launch shape of the persistent ray-cast kernel. */
+typedef struct lv_batch_config
+{
+    uint32_t tile_w, tile_h; /* pixels per work item = threads per CTA
+                                (a multiple of 32, at most 256) */
+    uint32_t ctas_per_sm;    /* persistent grid = SMs * ctas_per_sm */
+    uint32_t tf_shared;      /* 1: transfer function staged in shared memory */
+    uint32_t use_graph;      /* 1: replay the batch as one CUDA graph */
+} lv_batch_config;
+
+/* A batch renderer on ctx (its own stream, graphs and per-view buffers).
+ * No reference counterpart: Livre renders one view per channel. */
+lv_status lv_batch_create(lv_ctx* ctx, lv_batch** out);
+void lv_batch_destroy(lv_batch* batch);
+lv_status lv_batch_set_config(lv_batch* batch, const lv_batch_config* cfg);
+lv_status lv_batch_get_config(const lv_batch* batch, lv_batch_config* cfg);
+/* Renders n views: one multi-view LOD selection, one residency pass and
+ * one persistent ray-cast launch per voxel type, fed by a device work queue
+ * of (view, tile) items and replayed as a CUDA graph. Ordered after the work
+ * already queued on `stream`; `stream` waits for the batch. */
+lv_status lv_batch_render(lv_batch* batch, const lv_batch_view* views,
+                          uint32_t n, void* stream);
+/* Per-view statistics of the last lv_batch_render (synchronises with it);
+ * select_ms / raycast_ms (nullable) receive the device time of the
+ * selection + residency passes and of the persistent ray cast. */
+lv_status lv_batch_stats(lv_batch* batch, lv_frame_stats* out, uint32_t n,
+                         float* select_ms, float* raycast_ms);
+/* Times the persistent kernel on this batch for every tile shape in
+ * {8x8, 16x8, 8x16, 16x16, 32x4, 32x8}, CTAs per SM in {2, 4, 8} and
+ * transfer-function staging on/off (reps timed launches each), keeps the
+ * fastest configuration and returns it in `chosen`. */
+lv_status lv_batch_autotune(lv_batch* batch, const lv_batch_view* views,
+                            uint32_t n, void* stream, uint32_t reps,
+                            lv_batch_config* chosen);
+
 /* RGBA32F -> RGBA8 (alpha forced to 255 like the framebuffer copy of
  * livre/eq/render/shaders/fragTexCopy.glsl:11-15 onto the RGB window of
  * livre/eq/Window.cpp:122-124), truncating x * 255 after clamping to [0,1]. */

@@ -504,3 +504,68 @@ class Context:
         check(lib().lv_frame_to_rgba8(self.handle, _ptr(rgba), w, h, _ptr(out),
                                       _stream(stream)), self.handle)
         return out
+
+
+class Batch:
+    """Batched renderer (lv_batch): many views per persistent launch, replayed
+    as a CUDA graph."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib().lv_batch_create(ctx.handle, C.byref(h)), ctx.handle)
+        self.handle = h
+        ctx._children.add(self)
+        self._views = None
+
+    def close(self):
+        if self.handle:
+            lib().lv_batch_destroy(self.handle)
+            self.handle = None
+            self.ctx._children.discard(self)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def config(self):
+        c = _abi.BatchConfig()
+        check(lib().lv_batch_get_config(self.handle, C.byref(c)), self.ctx.handle)
+        return c.as_dict()
+
+    def set_config(self, tile_w=16, tile_h=8, ctas_per_sm=4, tf_shared=0, use_graph=1):
+        c = _abi.BatchConfig(tile_w, tile_h, ctas_per_sm, tf_shared, use_graph)
+        check(lib().lv_batch_set_config(self.handle, C.byref(c)), self.ctx.handle)
+
+    @staticmethod
+    def _pack(items):
+        """items: sequence of (Volume, TransferFunction, RenderDesc, out tensor)."""
+        arr = (_abi.BatchView * len(items))()
+        for i, (vol, tf, desc, out) in enumerate(items):
+            arr[i].volume = vol.handle.value
+            arr[i].tf = tf.handle.value
+            arr[i].desc = desc
+            arr[i].d_rgba = out.data_ptr()
+        return arr
+
+    def render(self, items, stream=None):
+        arr = self._pack(items)
+        self._views = (arr, items)  # keep tensors alive until the next call
+        check(lib().lv_batch_render(self.handle, arr, len(items), _stream(stream)),
+              self.ctx.handle)
+
+    def stats(self, n):
+        out = (_abi.FrameStats * max(n, 1))()
+        sel, ray = C.c_float(), C.c_float()
+        check(lib().lv_batch_stats(self.handle, out, n, C.byref(sel), C.byref(ray)),
+              self.ctx.handle)
+        return [out[i].as_dict() for i in range(n)], sel.value, ray.value
+
+    def autotune(self, items, reps=3, stream=None):
+        arr = self._pack(items)
+        c = _abi.BatchConfig()
+        check(lib().lv_batch_autotune(self.handle, arr, len(items), _stream(stream), reps,
+                                      C.byref(c)), self.ctx.handle)
+        return c.as_dict()

@@ -66,6 +66,19 @@ class FrameStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchView(C.Structure):
+    _fields_ = [("volume", C.c_void_p), ("tf", C.c_void_p), ("desc", RenderDesc),
+                ("d_rgba", C.c_void_p)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("ctas_per_sm", C.c_uint32),
+                ("tf_shared", C.c_uint32), ("use_graph", C.c_uint32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 GET_DATA_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_size_t)
 
 P = C.POINTER
@@ -94,6 +107,15 @@ _SIGNATURES = {
     "lv_render": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, P(RenderDesc), C.c_void_p,
                             C.c_void_p]),
     "lv_last_stats": (C.c_int, [C.c_void_p, P(FrameStats)]),
+    "lv_batch_create": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
+    "lv_batch_destroy": (None, [C.c_void_p]),
+    "lv_batch_set_config": (C.c_int, [C.c_void_p, P(BatchConfig)]),
+    "lv_batch_get_config": (C.c_int, [C.c_void_p, P(BatchConfig)]),
+    "lv_batch_render": (C.c_int, [C.c_void_p, P(BatchView), C.c_uint32, C.c_void_p]),
+    "lv_batch_stats": (C.c_int, [C.c_void_p, P(FrameStats), C.c_uint32, P(C.c_float),
+                                 P(C.c_float)]),
+    "lv_batch_autotune": (C.c_int, [C.c_void_p, P(BatchView), C.c_uint32, C.c_void_p,
+                                    C.c_uint32, P(BatchConfig)]),
     "lv_frame_to_rgba8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                     C.c_void_p, C.c_void_p]),
 }

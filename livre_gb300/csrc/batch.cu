@@ -1,0 +1,663 @@
+/*
+ * Batched rendering: many views (different volumes, transfer functions,
+ * viewports and LOD thresholds) in one pass.
+ *
+ *  - one multi-view LOD selection (every view's frontier in the same queues),
+ *  - one residency pass, prune and leaf-grid splat over all views
+ *    (blockIdx.y = view),
+ *  - one persistent ray-cast launch per voxel type / filter, whose CTAs pop
+ *    (view, tile) items from a device work queue,
+ *  - the whole sequence is captured once into a CUDA graph and replayed; the
+ *    per-view constants travel in one host->device copy inside the graph.
+ *
+ * Residency follows the reference's asynchronous mode (RenderPipeline::
+ * renderAsync, livre/lib/pipeline/RenderPipeline.cpp:160-225): missing bricks
+ * are replaced by their nearest resident ancestor and streamed before the next
+ * launch (up to desc.max_uploads per view), since a graph cannot wait on the
+ * host.
+ *
+ * An autotuner times the persistent kernel over tile shapes, CTAs per SM and
+ * transfer-function staging (shared memory or L1) on the batch itself.
+ */
+#include <algorithm>
+#include <map>
+#include <tuple>
+#include <vector>
+
+#include "lv_runtime.h"
+
+namespace lv
+{
+lv_status launch_views_pipeline(lv_ctx* ctx, const ResolveView* d_resolve,
+                                const RayView* d_rays, uint32_t n, cudaStream_t s);
+lv_status launch_persistent(lv_ctx* ctx, int dtype, int filter, int tf_shared,
+                            const RayView* d_rays, const TileQueue& Q, uint32_t ctas,
+                            uint32_t tfn_max, cudaStream_t s);
+void type_range(uint32_t dt, float& lo, float& hi);
+} // namespace lv
+
+namespace
+{
+struct Group
+{
+    int dtype, filter;
+    std::vector<uint32_t> views;
+};
+
+/* byte offsets of one view's device regions */
+struct ViewSlots
+{
+    uint64_t visible, render_ids, render_slots, missing, view_stamp, leaf;
+};
+} // namespace
+
+struct lv_batch
+{
+    lv_ctx* ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr, user_ready = nullptr;
+    cudaEvent_t t_sel0 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
+    lv_batch_config cfg{16, 8, 4, 0, 1};
+    /* per-view region strides (grow-only) */
+    uint64_t nodes_stride = 0, cells_stride = 0, missing_stride = 0;
+    uint32_t views_cap = 0;
+    uint32_t depth_max = 0;
+    lv::DeviceBuffer params, zeroed, leafs, lists;
+    lv::PinnedBuffer h_params, h_out;
+    uint64_t params_bytes = 0;
+    uint32_t generation = 0;
+    std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
+                        uint32_t, uintptr_t>,
+             cudaGraphExec_t>
+        graphs;
+    uint32_t launch_id = 0;
+    uint32_t frame = 0;
+    /* previous launch, for the async misses and for statistics */
+    std::vector<lv_batch_view> last;
+    bool pending = false;
+    uint64_t uploaded_bytes = 0;
+    uint32_t uploaded = 0;
+    uint32_t launches = 0;
+
+    ~lv_batch()
+    {
+        for (auto& kv : graphs)
+            cudaGraphExecDestroy(kv.second);
+        if (done)
+            cudaEventDestroy(done);
+        if (user_ready)
+            cudaEventDestroy(user_ready);
+        if (t_sel0)
+            cudaEventDestroy(t_sel0);
+        if (t_ray0)
+            cudaEventDestroy(t_ray0);
+        if (t_ray1)
+            cudaEventDestroy(t_ray1);
+        if (stream)
+            cudaStreamDestroy(stream);
+    }
+};
+
+namespace
+{
+using namespace lv;
+
+constexpr uint32_t kOutWords = FC_WORDS + LV_SELECT_RESULT_WORDS;
+
+/* params layout: LodView[n] | ResolveView[n] | RayView[n] | queue tables */
+struct ParamLayout
+{
+    uint64_t lod, resolve, ray, tables, bytes;
+};
+
+ParamLayout param_layout(uint32_t n)
+{
+    auto al = [](uint64_t x) { return (x + 255) & ~uint64_t(255); };
+    ParamLayout L;
+    L.lod = 0;
+    L.resolve = al(L.lod + sizeof(LodView) * n);
+    L.ray = al(L.resolve + sizeof(ResolveView) * n);
+    L.tables = al(L.ray + sizeof(RayView) * n);
+    /* 4 groups x (view ids n + tile starts n + 1) */
+    L.bytes = al(L.tables + sizeof(uint32_t) * 4 * (2 * n + 1));
+    return L;
+}
+
+int group_index(int dtype, int filter)
+{
+    return (dtype == LV_DT_UINT16 ? 2 : 0) + (filter == LV_FILTER_TRILINEAR ? 1 : 0);
+}
+
+lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
+                         cudaStream_t user)
+{
+    lv_ctx* ctx = b->ctx;
+    uint64_t nodes = b->nodes_stride, cells = b->cells_stride;
+    uint32_t depth = b->depth_max;
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const lv_volume_info& vi = views[i].volume->info;
+        nodes = std::max(nodes, views[i].volume->n_nodes);
+        uint64_t c = 1;
+        for (int a = 0; a < 3; ++a)
+            c *= uint64_t(vi.root_blocks[a]) << (vi.depth - 1);
+        cells = std::max(cells, c);
+        depth = std::max(depth, vi.depth);
+    }
+    const uint32_t vcap = std::max(b->views_cap, n);
+    const bool grow = nodes > b->nodes_stride || cells > b->cells_stride ||
+                      vcap > b->views_cap;
+    b->depth_max = depth;
+    if (!grow)
+        return LV_OK;
+    LV_CUDA(ctx, cudaStreamSynchronize(b->stream));
+    LV_CUDA(ctx, cudaStreamSynchronize(user));
+    b->nodes_stride = (nodes + 63) & ~uint64_t(63);
+    b->cells_stride = (cells + 63) & ~uint64_t(63);
+    b->missing_stride = std::min<uint64_t>(b->nodes_stride, 4096);
+    b->views_cap = vcap;
+    const ParamLayout PL = param_layout(vcap);
+    b->params_bytes = PL.bytes;
+    LV_CUDA(ctx, b->params.reserve(PL.bytes));
+    LV_CUDA(ctx, b->h_params.reserve(PL.bytes));
+    LV_CUDA(ctx, b->zeroed.reserve(sizeof(uint32_t) * (kOutWords * vcap + 64)));
+    LV_CUDA(ctx, b->leafs.reserve(sizeof(uint32_t) * b->cells_stride * vcap));
+    /* visible + render ids (u64) + render slots + view stamps (u32) + missing */
+    const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
+    b->lists.release();
+    LV_CUDA(ctx, b->lists.reserve(per_view * vcap));
+    LV_CUDA(ctx, b->h_out.reserve(sizeof(uint32_t) * kOutWords * vcap +
+                                  sizeof(uint64_t) * b->missing_stride * vcap));
+    /* view stamps start at 0; launch ids start at 1 */
+    LV_CUDA(ctx, cudaMemset(b->lists.ptr, 0, per_view * vcap));
+    for (auto& kv : b->graphs)
+        cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+    ++b->generation;
+    return LV_OK;
+}
+
+ViewSlots view_slots(const lv_batch* b, uint32_t i)
+{
+    const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
+    const uint64_t base = per_view * i;
+    ViewSlots s;
+    s.visible = base;
+    s.render_ids = base + b->nodes_stride * 8;
+    s.render_slots = s.render_ids + b->nodes_stride * 8;
+    s.view_stamp = s.render_slots + b->nodes_stride * 4;
+    s.missing = s.view_stamp + b->nodes_stride * 4;
+    s.leaf = uint64_t(i) * b->cells_stride * 4;
+    return s;
+}
+
+/* Streams the previous launch's misses (async mode). */
+lv_status process_misses(lv_batch* b)
+{
+    if (!b->pending)
+        return LV_OK;
+    lv_ctx* ctx = b->ctx;
+    LV_CUDA(ctx, cudaEventSynchronize(b->done));
+    b->pending = false;
+    const uint32_t* out = b->h_out.as<uint32_t>();
+    const uint64_t* miss = reinterpret_cast<const uint64_t*>(
+        b->h_out.as<uint8_t>() + sizeof(uint32_t) * kOutWords * b->views_cap);
+    for (uint32_t i = 0; i < b->last.size(); ++i)
+    {
+        const uint32_t* c = out + kOutWords * i;
+        const uint32_t m = std::min<uint32_t>(
+            std::min<uint32_t>(c[FC_MISSING], uint32_t(b->missing_stride)),
+            b->last[i].desc.max_uploads);
+        if (!m)
+            continue;
+        uint32_t loaded = 0;
+        uint64_t bytes = 0;
+        lv_status st = stream_bricks(ctx, b->last[i].volume, miss + b->missing_stride * i, m,
+                                     b->frame, b->stream, loaded, bytes);
+        b->uploaded += loaded;
+        b->uploaded_bytes += bytes;
+        if (st != LV_OK && st != LV_EAGAIN)
+            return st;
+    }
+    return LV_OK;
+}
+
+lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n,
+                      std::vector<Group>& groups, uint32_t& total_roots,
+                      uint32_t& tfn_max)
+{
+    lv_ctx* ctx = b->ctx;
+    const ParamLayout PL = param_layout(b->views_cap);
+    uint8_t* h = b->h_params.as<uint8_t>();
+    LodView* lods = reinterpret_cast<LodView*>(h + PL.lod);
+    ResolveView* res = reinterpret_cast<ResolveView*>(h + PL.resolve);
+    RayView* rays = reinterpret_cast<RayView*>(h + PL.ray);
+    uint8_t* dlists = b->lists.as<uint8_t>();
+    uint32_t* dz = b->zeroed.as<uint32_t>();
+    uint32_t* dleaf = b->leafs.as<uint32_t>();
+    total_roots = 0;
+    tfn_max = 0;
+    groups.assign(4, Group{});
+    for (int g = 0; g < 4; ++g)
+    {
+        groups[g].dtype = g >= 2 ? LV_DT_UINT16 : LV_DT_UINT8;
+        groups[g].filter = (g & 1) ? LV_FILTER_TRILINEAR : LV_FILTER_NEAREST;
+    }
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        const lv_batch_view& bv = views[i];
+        lv_volume* vol = bv.volume;
+        const lv_volume_info& info = vol->info;
+        const lv_render_desc& d = bv.desc;
+        const ViewSlots S = view_slots(b, i);
+        uint32_t* counters = dz + kOutWords * i;
+        uint32_t* selres = counters + FC_WORDS;
+        lv_lod_params lod = d.lod;
+        if (lod.window_height == 0)
+            lod.window_height = d.height;
+        if (!(lod.range[0] == 0.0f && lod.range[1] == 1.0f))
+            return fail(ctx, LV_EINVAL, "batched views render the full range {0, 1}");
+        if (lod.time_step != vol->time_step)
+            return fail(ctx, LV_EINVAL, "batched views render the volume's current time step");
+        lv_status st = make_lod_view(ctx, info, d.camera, lod, lods[i]);
+        if (st != LV_OK)
+            return st;
+        lods[i].out_ids = reinterpret_cast<uint64_t*>(dlists + S.visible);
+        lods[i].capacity = uint32_t(b->nodes_stride);
+        lods[i].result = selres;
+        lods[i].root_offset = total_roots;
+        total_roots += info.root_blocks[0] * info.root_blocks[1] * info.root_blocks[2];
+
+        uint32_t dims[3];
+        const uint32_t Lf = info.depth - 1u;
+        for (int a = 0; a < 3; ++a)
+            dims[a] = info.root_blocks[a] << Lf;
+        ResolveView& R = res[i];
+        std::memset(&R, 0, sizeof(R));
+        R.visible = lods[i].out_ids;
+        R.n_visible_ptr = selres + LV_SEL_WRITTEN;
+        R.node_table = vol->node_table.as<int32_t>();
+        R.node_stamp = vol->node_stamp.as<uint32_t>();
+        R.view_stamp = reinterpret_cast<uint32_t*>(dlists + S.view_stamp);
+        R.frame = b->frame;
+        R.view_frame = b->launch_id;
+        R.depth = info.depth;
+        for (int a = 0; a < 3; ++a)
+        {
+            R.root_blocks[a] = info.root_blocks[a];
+            R.dims[a] = dims[a];
+        }
+        std::memcpy(R.level_offset, vol->level_offset, sizeof(R.level_offset));
+        R.synchronous = 0;
+        R.render_ids = reinterpret_cast<uint64_t*>(dlists + S.render_ids);
+        R.render_slots = reinterpret_cast<uint32_t*>(dlists + S.render_slots);
+        R.render_capacity = uint32_t(b->nodes_stride);
+        R.missing = reinterpret_cast<uint64_t*>(dlists + S.missing);
+        R.missing_capacity = uint32_t(b->missing_stride);
+        R.counters = counters;
+        R.leaf = dleaf + S.leaf / 4;
+        R.Lf = Lf;
+
+        RayView& V = rays[i];
+        std::memset(&V, 0, sizeof(V));
+        float lim[6], planes[6][4], eye[3], dir[3];
+        bool ok = false;
+        frustum_setup(d.camera.modelview, d.camera.projection, V.inv_mv, V.inv_p, lim,
+                      planes, eye, dir, &ok);
+        if (!ok)
+            return fail(ctx, LV_EINVAL, "singular camera");
+        const uint32_t bm = std::max(dims[0], std::max(dims[1], dims[2]));
+        for (int a = 0; a < 3; ++a)
+        {
+            V.eye[a] = eye[a];
+            const float half = info.world_size[a] / 2.0f;
+            V.gmin[a] = -half;
+            V.gmax[a] = half;
+            V.gscale[a] = float(bm) / info.world_size[a];
+            V.dims[a] = dims[a];
+            V.N[a] = info.max_block[a];
+            V.O[a] = info.overlap[a];
+            V.B[a] = info.max_block[a] - 2u * info.overlap[a];
+        }
+        V.nearp = lim[4];
+        V.n_clip = lod.n_clip_planes;
+        std::memcpy(V.clip, lod.clip_planes, sizeof(V.clip));
+        V.Lf = Lf;
+        V.dtype = info.dtype;
+        V.filter = d.filter;
+        float lo = d.data_range[0], hi = d.data_range[1];
+        if (!(hi > lo))
+            type_range(info.dtype, lo, hi);
+        V.dmul = 1.0f / (hi - lo);
+        V.dadd = -lo / (hi - lo);
+        V.early = d.early_exit;
+        V.W = d.width;
+        V.H = d.height;
+        V.samples_fixed = d.samples_per_ray;
+        V.step_policy = d.step_policy;
+        V.max_voxel_dim = std::max(info.voxels[0], std::max(info.voxels[1], info.voxels[2]));
+        V.depth = info.depth;
+        V.leaf = R.leaf;
+        V.pool = ctx->pool->arena.as<uint8_t>();
+        V.tf = bv.tf->rgba.as<float4>();
+        V.tfn = bv.tf->n;
+        V.out = reinterpret_cast<float4*>(bv.d_rgba);
+        V.counters = counters;
+        tfn_max = std::max(tfn_max, bv.tf->n);
+        if (info.dtype != LV_DT_UINT8 && info.dtype != LV_DT_UINT16)
+            return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
+        groups[group_index(int(info.dtype), int(d.filter))].views.push_back(i);
+    }
+    /* queue tables */
+    uint32_t* tables = reinterpret_cast<uint32_t*>(h + PL.tables);
+    const uint32_t stride = 2 * b->views_cap + 1;
+    for (int g = 0; g < 4; ++g)
+    {
+        uint32_t* ids = tables + stride * g;
+        uint32_t* starts = ids + b->views_cap;
+        uint32_t acc = 0;
+        for (uint32_t k = 0; k < groups[g].views.size(); ++k)
+        {
+            const uint32_t v = groups[g].views[k];
+            ids[k] = v;
+            starts[k] = acc;
+            const uint32_t tw = b->cfg.tile_w, th = b->cfg.tile_h;
+            acc += ((rays[v].W + tw - 1) / tw) * ((rays[v].H + th - 1) / th);
+        }
+        starts[groups[g].views.size()] = acc;
+    }
+    return LV_OK;
+}
+
+lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& groups,
+                        uint32_t total_roots, uint32_t tfn_max)
+{
+    lv_ctx* ctx = b->ctx;
+    cudaStream_t s = b->stream;
+    const ParamLayout PL = param_layout(b->views_cap);
+    uint8_t* d = b->params.as<uint8_t>();
+    LV_CUDA(ctx, cudaMemcpyAsync(d, b->h_params.ptr, PL.bytes, cudaMemcpyHostToDevice, s));
+    LV_CUDA(ctx, cudaMemsetAsync(b->zeroed.ptr, 0, sizeof(uint32_t) * (kOutWords * n + 64), s));
+    LV_CUDA(ctx, cudaMemsetAsync(b->leafs.ptr, 0xFF, sizeof(uint32_t) * b->cells_stride * n, s));
+    LV_CUDA(ctx, cudaEventRecord(b->t_sel0, s));
+    lv_status st = enqueue_selection(ctx, reinterpret_cast<LodView*>(d + PL.lod), n,
+                                     total_roots, b->depth_max, s);
+    if (st != LV_OK)
+        return st;
+    st = launch_views_pipeline(ctx, reinterpret_cast<ResolveView*>(d + PL.resolve),
+                               reinterpret_cast<RayView*>(d + PL.ray), n, s);
+    if (st != LV_OK)
+        return st;
+    LV_CUDA(ctx, cudaEventRecord(b->t_ray0, s));
+    uint32_t* heads = b->zeroed.as<uint32_t>() + kOutWords * n;
+    const uint32_t* tables = reinterpret_cast<const uint32_t*>(d + PL.tables);
+    const uint32_t stride = 2 * b->views_cap + 1;
+    for (int g = 0; g < 4; ++g)
+    {
+        if (groups[g].views.empty())
+            continue;
+        TileQueue Q;
+        Q.view_ids = tables + stride * g;
+        Q.tile_start = Q.view_ids + b->views_cap;
+        Q.n_views = uint32_t(groups[g].views.size());
+        Q.tile_w = b->cfg.tile_w;
+        Q.tile_h = b->cfg.tile_h;
+        Q.head = heads + g;
+        st = launch_persistent(ctx, groups[g].dtype, groups[g].filter, b->cfg.tf_shared,
+                               reinterpret_cast<RayView*>(d + PL.ray), Q, b->cfg.ctas_per_sm,
+                               tfn_max, s);
+        if (st != LV_OK)
+            return st;
+    }
+    LV_CUDA(ctx, cudaEventRecord(b->t_ray1, s));
+    LV_CUDA(ctx, cudaMemcpyAsync(b->h_out.ptr, b->zeroed.ptr, sizeof(uint32_t) * kOutWords * n,
+                                 cudaMemcpyDeviceToHost, s));
+    /* missing lists, one strided copy */
+    uint8_t* hmiss = b->h_out.as<uint8_t>() + sizeof(uint32_t) * kOutWords * b->views_cap;
+    const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
+    LV_CUDA(ctx, cudaMemcpy2DAsync(hmiss, b->missing_stride * 8,
+                                   b->lists.as<uint8_t>() + view_slots(b, 0).missing, per_view,
+                                   b->missing_stride * 8, n, cudaMemcpyDeviceToHost, s));
+    return LV_OK;
+}
+
+} // namespace
+
+/* ================================================================ C ABI */
+extern "C" lv_status lv_batch_create(lv_ctx* ctx, lv_batch** out)
+{
+    if (!ctx || !out)
+        return fail(ctx, LV_EINVAL, "null argument");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    lv_status st = ensure_renderer(ctx);
+    if (st != LV_OK)
+        return st;
+    lv_batch* b = new lv_batch();
+    b->ctx = ctx;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->user_ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->t_sel0) != cudaSuccess || cudaEventCreate(&b->t_ray0) != cudaSuccess ||
+        cudaEventCreate(&b->t_ray1) != cudaSuccess)
+    {
+        delete b;
+        return fail(ctx, LV_EDEVICE, "batch stream/events");
+    }
+    *out = b;
+    return LV_OK;
+}
+
+extern "C" void lv_batch_destroy(lv_batch* b)
+{
+    if (!b)
+        return;
+    {
+        std::lock_guard<std::mutex> lock(b->ctx->mutex);
+        cudaSetDevice(b->ctx->device);
+        cudaStreamSynchronize(b->stream);
+    }
+    delete b;
+}
+
+extern "C" lv_status lv_batch_set_config(lv_batch* b, const lv_batch_config* cfg)
+{
+    if (!b || !cfg)
+        return LV_EINVAL;
+    const uint32_t threads = cfg->tile_w * cfg->tile_h;
+    if (threads == 0 || threads > 256 || threads % 32 != 0 || cfg->ctas_per_sm == 0 ||
+        cfg->ctas_per_sm > 16)
+        return fail(b->ctx, LV_EINVAL, "tile_w * tile_h must be a multiple of 32 up to 256; "
+                                       "ctas_per_sm in 1..16");
+    std::lock_guard<std::mutex> lock(b->ctx->mutex);
+    b->cfg = *cfg;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_batch_get_config(const lv_batch* b, lv_batch_config* cfg)
+{
+    if (!b || !cfg)
+        return LV_EINVAL;
+    *cfg = b->cfg;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, uint32_t n,
+                                     void* stream)
+{
+    if (!b || (n && !views))
+        return fail(b ? b->ctx : nullptr, LV_EINVAL, "null argument");
+    lv_ctx* ctx = b->ctx;
+    for (uint32_t i = 0; i < n; ++i)
+        if (!views[i].volume || !views[i].tf || !views[i].d_rgba || views[i].volume->ctx != ctx ||
+            views[i].tf->ctx != ctx || !views[i].desc.width || !views[i].desc.height)
+            return fail(ctx, LV_EINVAL, "invalid batch view");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t user = static_cast<cudaStream_t>(stream);
+    b->uploaded = 0;
+    b->uploaded_bytes = 0;
+    lv_status st = process_misses(b);
+    if (st != LV_OK)
+        return st;
+    if (n == 0)
+        return LV_OK;
+    /* the host staging is read by the previous launch until it completes */
+    LV_CUDA(ctx, cudaEventSynchronize(b->done));
+    st = ensure_regions(b, views, n, user);
+    if (st != LV_OK)
+        return st;
+    uint64_t frontier = 0;
+    for (uint32_t i = 0; i < n; ++i)
+        frontier += max_frontier(views[i].volume->info);
+    st = reserve_frontier(ctx, frontier, b->stream);
+    if (st != LV_OK)
+        return st;
+    b->frame = ++ctx->renderer->frame;
+    ++b->launch_id;
+    std::vector<Group> groups;
+    uint32_t total_roots = 0, tfn_max = 0;
+    st = fill_params(b, views, n, groups, total_roots, tfn_max);
+    if (st != LV_OK)
+        return st;
+    if (b->cfg.tf_shared && tfn_max > 4096)
+        return fail(ctx, LV_EINVAL, "shared-memory transfer functions hold at most 4096 entries");
+    uint32_t mask = 0;
+    for (int g = 0; g < 4; ++g)
+        if (!groups[g].views.empty())
+            mask |= 1u << g;
+    LV_CUDA(ctx, cudaEventRecord(b->user_ready, user));
+    LV_CUDA(ctx, cudaStreamWaitEvent(b->stream, b->user_ready, 0));
+    if (b->cfg.use_graph)
+    {
+        const auto key = std::make_tuple(n, mask, b->cfg.tile_w, b->cfg.tile_h, b->cfg.ctas_per_sm,
+                                         b->cfg.tf_shared ? tfn_max : 0u, b->depth_max,
+                                         b->generation, uintptr_t(ctx->sel.ids[0].ptr));
+        auto it = b->graphs.find(key);
+        if (it == b->graphs.end())
+        {
+            if (b->graphs.size() >= 16)
+            {
+                cudaGraphExecDestroy(b->graphs.begin()->second);
+                b->graphs.erase(b->graphs.begin());
+            }
+            cudaGraph_t g = nullptr;
+            LV_CUDA(ctx, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            st = enqueue_batch(b, n, groups, total_roots, tfn_max);
+            const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+            if (st != LV_OK)
+            {
+                if (g)
+                    cudaGraphDestroy(g);
+                return st;
+            }
+            LV_CUDA(ctx, ce);
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            LV_CUDA(ctx, ie);
+            it = b->graphs.emplace(key, exec).first;
+        }
+        LV_CUDA(ctx, cudaGraphLaunch(it->second, b->stream));
+    }
+    else
+    {
+        st = enqueue_batch(b, n, groups, total_roots, tfn_max);
+        if (st != LV_OK)
+            return st;
+    }
+    LV_CUDA(ctx, cudaEventRecord(b->done, b->stream));
+    LV_CUDA(ctx, cudaStreamWaitEvent(user, b->done, 0));
+    b->last.assign(views, views + n);
+    b->pending = true;
+    /* selection: roots + levels + finish; resolve, prune, leaf, step;
+     * one persistent launch per non-empty group */
+    b->launches = b->depth_max + 2u + 4u + uint32_t(__builtin_popcount(mask));
+    return LV_OK;
+}
+
+extern "C" lv_status lv_batch_stats(lv_batch* b, lv_frame_stats* out, uint32_t n,
+                                    float* select_ms, float* raycast_ms)
+{
+    if (!b || (n && !out))
+        return LV_EINVAL;
+    lv_ctx* ctx = b->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaEventSynchronize(b->done));
+    const uint32_t m = std::min<uint32_t>(n, uint32_t(b->last.size()));
+    const uint32_t* h = b->h_out.as<uint32_t>();
+    for (uint32_t i = 0; i < m; ++i)
+    {
+        const uint32_t* c = h + kOutWords * i;
+        const uint32_t* sel = c + FC_WORDS;
+        lv_frame_stats s{};
+        s.n_visible = sel[LV_SEL_WRITTEN];
+        s.n_visited = sel[LV_SEL_VISITED];
+        s.n_rendered = c[FC_KEPT];
+        s.n_available = c[FC_AVAILABLE];
+        s.n_not_available = c[FC_NOT_AVAILABLE];
+        s.max_level = c[FC_MAX_LEVEL] ? c[FC_MAX_LEVEL] - 1u : 0u;
+        s.samples_per_ray = c[FC_SAMPLES_PER_RAY];
+        s.n_samples = uint64_t(c[FC_SAMPLES_LO]) | (uint64_t(c[FC_SAMPLES_HI]) << 32);
+        if (i == 0)
+        {
+            s.n_uploaded = b->uploaded;
+            s.bytes_uploaded = b->uploaded_bytes;
+            s.n_launches = b->launches;
+        }
+        out[i] = s;
+    }
+    if (select_ms)
+        cudaEventElapsedTime(select_ms, b->t_sel0, b->t_ray0);
+    if (raycast_ms)
+        cudaEventElapsedTime(raycast_ms, b->t_ray0, b->t_ray1);
+    return LV_OK;
+}
+
+extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, uint32_t n,
+                                       void* stream, uint32_t reps, lv_batch_config* chosen)
+{
+    if (!b || !views || n == 0)
+        return LV_EINVAL;
+    static const uint32_t shapes[][2] = {{8, 8}, {16, 8}, {8, 16}, {16, 16}, {32, 4}, {32, 8}};
+    static const uint32_t ctas[] = {2, 4, 8};
+    const lv_batch_config start = b->cfg;
+    lv_batch_config best = start;
+    float best_ms = 1e30f;
+    reps = reps ? reps : 3;
+    for (const auto& sh : shapes)
+        for (uint32_t c : ctas)
+            for (uint32_t tfs = 0; tfs < 2; ++tfs)
+            {
+                lv_batch_config cfg = start;
+                cfg.tile_w = sh[0];
+                cfg.tile_h = sh[1];
+                cfg.ctas_per_sm = c;
+                cfg.tf_shared = tfs;
+                if (lv_batch_set_config(b, &cfg) != LV_OK)
+                    continue;
+                float total = 0.f;
+                bool ok = true;
+                for (uint32_t r = 0; r <= reps && ok; ++r)
+                {
+                    if (lv_batch_render(b, views, n, stream) != LV_OK)
+                    {
+                        ok = false;
+                        break;
+                    }
+                    float sel = 0.f, ray = 0.f;
+                    lv_batch_stats(b, nullptr, 0, &sel, &ray);
+                    if (r > 0)
+                        total += ray;
+                }
+                if (ok && total / reps < best_ms)
+                {
+                    best_ms = total / reps;
+                    best = cfg;
+                }
+            }
+    lv_batch_set_config(b, &best);
+    if (chosen)
+        *chosen = best;
+    return best_ms < 1e30f ? LV_OK : fail(b->ctx, LV_EINVAL, "no configuration ran");
+}

@@ -479,7 +479,6 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
     SelectScratch& S = ctx->sel;
     if (S.frontier_capacity == 0)
         return fail(ctx, LV_EINVAL, "selection scratch not reserved");
-    const uint32_t cap = S.frontier_capacity;
     LV_CUDA(ctx, S.staging.reserve(sizeof(LodView) * n_views));
     LV_CUDA(ctx, S.views.reserve(sizeof(LodView) * n_views));
     /* The pinned staging copy may still be read by a previous in-flight
@@ -494,12 +493,21 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                        host_views[v].root_blocks[1] *
                        host_views[v].root_blocks[2];
     }
-    if (total_roots > cap)
-        return fail(ctx, LV_ENOMEM, "root frontier exceeds scratch capacity");
     LV_CUDA(ctx, cudaMemcpyAsync(S.views.ptr, S.staging.ptr,
                                  sizeof(LodView) * n_views,
                                  cudaMemcpyHostToDevice, stream));
-    const LodView* dviews = S.views.as<LodView>();
+    return enqueue_selection(ctx, S.views.as<LodView>(), n_views, total_roots,
+                             max_depth, stream);
+}
+
+lv_status enqueue_selection(lv_ctx* ctx, const LodView* dviews, uint32_t n_views,
+                            uint32_t total_roots, uint32_t max_depth,
+                            cudaStream_t stream)
+{
+    SelectScratch& S = ctx->sel;
+    const uint32_t cap = S.frontier_capacity;
+    if (total_roots > cap)
+        return fail(ctx, LV_ENOMEM, "root frontier exceeds scratch capacity");
     uint32_t* counts = S.counts.as<uint32_t>();
     const uint32_t n_counts = kMaxLevels + 2;
     uint32_t* overflow = counts + kMaxLevels + 1;
@@ -521,6 +529,23 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
     lod_finish_kernel<<<(n_views + 127) / 128, 128, 0, stream>>>(dviews, n_views,
                                                                  overflow);
     LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+lv_status reserve_frontier(lv_ctx* ctx, uint64_t nodes, cudaStream_t s)
+{
+    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(nodes, 64), 1u << 24);
+    SelectScratch& S = ctx->sel;
+    if (S.frontier_capacity >= cap)
+        return LV_OK;
+    LV_CUDA(ctx, cudaStreamSynchronize(s));
+    for (int i = 0; i < 2; ++i)
+    {
+        LV_CUDA(ctx, S.ids[i].reserve(sizeof(uint64_t) * cap));
+        LV_CUDA(ctx, S.view[i].reserve(sizeof(uint32_t) * cap));
+    }
+    LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 2)));
+    S.frontier_capacity = uint32_t(cap);
     return LV_OK;
 }
 
@@ -575,20 +600,9 @@ extern "C" lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
     V.out_ids = d_out_ids;
     V.capacity = capacity;
     V.result = d_result;
-    const uint64_t need = max_frontier(*vol);
-    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(need, 64), 1u << 24);
-    SelectScratch& S = ctx->sel;
-    if (S.frontier_capacity < cap)
-    {
-        LV_CUDA(ctx, cudaStreamSynchronize(s));
-        for (int i = 0; i < 2; ++i)
-        {
-            LV_CUDA(ctx, S.ids[i].reserve(sizeof(uint64_t) * cap));
-            LV_CUDA(ctx, S.view[i].reserve(sizeof(uint32_t) * cap));
-        }
-        LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 2)));
-        S.frontier_capacity = uint32_t(cap);
-    }
+    st = reserve_frontier(ctx, max_frontier(*vol), s);
+    if (st != LV_OK)
+        return st;
     st = run_selection(ctx, &V, 1, vol->depth, s);
     if (st != LV_OK)
         return st;

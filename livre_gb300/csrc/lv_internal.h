@@ -114,7 +114,9 @@ struct ResolveView
     const uint32_t* n_visible_ptr; /* LV_SEL_WRITTEN word of the selection */
     const int32_t* node_table;     /* slot unit per node (-1 = not resident) */
     uint32_t* node_stamp;          /* last frame a node was rendered (in use) */
-    uint32_t frame;
+    uint32_t* view_stamp;          /* per-view stamps: rendering-set membership */
+    uint32_t frame;                /* stamp written to node_stamp */
+    uint32_t view_frame;           /* stamp written to view_stamp */
     uint32_t depth;
     uint32_t root_blocks[3];
     uint64_t level_offset[kMaxLevels + 1];
@@ -128,6 +130,17 @@ struct ResolveView
     uint32_t* leaf;           /* leaf grid */
     uint32_t dims[3];
     uint32_t Lf;
+};
+
+/* Work queue of the persistent ray-cast kernel: the views of one voxel
+ * type / filter group and the prefix sums of their tile counts. */
+struct TileQueue
+{
+    const uint32_t* view_ids;   /* n_views entries: index into the RayView array */
+    const uint32_t* tile_start; /* n_views + 1 prefix sums */
+    uint32_t n_views;
+    uint32_t tile_w, tile_h;
+    uint32_t* head;             /* zeroed before the launch */
 };
 
 LV_HD uint64_t node_index(const uint64_t* level_offset,

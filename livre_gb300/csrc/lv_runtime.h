@@ -8,6 +8,8 @@
 
 #include <cstdio>
 #include <cstring>
+#include <list>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -155,6 +157,15 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                         uint32_t n_views, uint32_t max_depth,
                         cudaStream_t stream);
 
+/* Enqueues the selection kernels for n views whose constants are already
+ * on the device (capturable: no host synchronisation). */
+lv_status enqueue_selection(lv_ctx* ctx, const LodView* d_views, uint32_t n_views,
+                            uint32_t total_roots, uint32_t max_depth,
+                            cudaStream_t stream);
+/* Grows the frontier queues to hold `nodes` per level (synchronises `s`
+ * when it reallocates). */
+lv_status reserve_frontier(lv_ctx* ctx, uint64_t nodes, cudaStream_t s);
+
 /* Frontier size needed for a full traversal of a volume. */
 uint64_t max_frontier(const lv_volume_info& vol);
 
@@ -165,3 +176,103 @@ lv_status range_slice(lv_ctx* ctx, const lv_volume_info& vol,
                       cudaStream_t stream);
 
 } // namespace lv
+
+namespace lv
+{
+enum SourceKind
+{
+    SRC_CALLBACK = 0,
+    SRC_BLOB_DEVICE = 1,
+    SRC_BLOB_HOST = 2
+};
+
+/* One resident brick. */
+struct Resident
+{
+    lv_volume* vol;
+    uint64_t node_idx;
+    uint32_t unit;
+    uint32_t units;
+};
+
+struct Pool
+{
+    DeviceBuffer arena;
+    uint64_t capacity_units = 0;
+    uint64_t bump = 0;
+    std::map<uint32_t, std::vector<uint32_t>> free_by_units;
+    std::list<Resident> lru; /* front = oldest load */
+    uint64_t resident_bytes = 0;
+};
+
+struct Renderer
+{
+    DeviceBuffer visible, sel_result, render_ids, render_slots, missing,
+        counters, leaf, pairs;
+    PinnedBuffer h_counters, h_missing, h_pairs;
+    uint64_t visible_capacity = 0;
+    uint32_t frame = 0;
+    lv_frame_stats stats{};
+    cudaStream_t last_stream = nullptr;
+    bool have_last = false;
+    /* async mode: misses of the previous frame, copied back */
+    cudaEvent_t pending_event = nullptr;
+    lv_volume* pending_vol = nullptr;
+    uint32_t pending_max = 0;
+    uint32_t pending_frame = 0;
+    cudaEvent_t render_event = nullptr;
+    cudaEvent_t upload_event = nullptr;
+    /* timing of the last frame: selection and ray cast */
+    cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
+    uint32_t launches = 0;
+};
+
+
+
+/* Streams bricks `ids` of `vol` into the pool (allocate / evict bricks whose
+ * node stamp is below protect_frame, fetch, copy on the upload stream,
+ * publish page-table entries); `render` waits for the copies. */
+lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
+                        uint32_t n, uint32_t protect_frame, cudaStream_t render,
+                        uint32_t& n_loaded, uint64_t& bytes_loaded);
+lv_status ensure_renderer(lv_ctx* ctx);
+lv_status launch_resolve_views(lv_ctx* ctx, const ResolveView* d_views,
+                               uint32_t n_views, cudaStream_t s);
+} // namespace lv
+
+struct lv_tf
+{
+    lv_ctx* ctx;
+    lv::DeviceBuffer rgba;
+    uint32_t n;
+};
+
+struct lv_volume
+{
+    lv_ctx* ctx = nullptr;
+    lv_volume_info info{};
+    int kind = lv::SRC_CALLBACK;
+    lv_get_data_fn fn = nullptr;
+    void* user = nullptr;
+    lv_blob_desc blob{};
+    lv::DeviceBuffer d_blobs;
+    lv::PinnedBuffer host_store;
+    uint64_t brick_bytes = 0;
+    uint32_t slot_units = 0;
+    uint64_t level_offset[lv::kMaxLevels + 1] = {};
+    uint64_t n_nodes = 0;
+    lv::DeviceBuffer node_table, node_stamp;
+    std::vector<int32_t> host_table;
+    uint32_t time_step = 0;
+    /* pinned staging ring for callback sources */
+    std::vector<lv::PinnedBuffer*> staging;
+    std::vector<cudaEvent_t> staging_ev;
+    ~lv_volume()
+    {
+        for (auto* p : staging)
+            delete p;
+        for (auto e : staging_ev)
+            cudaEventDestroy(e);
+    }
+};
+

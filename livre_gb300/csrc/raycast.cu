@@ -49,12 +49,11 @@ __device__ __forceinline__ void emit_render(const ResolveView& R, uint64_t id,
 }
 
 /* For each visible id: resident -> rendering set; missing -> missing list
- * and (async mode) the nearest resident ancestor, once per frame. */
-__global__ void resolve_kernel(ResolveView R)
+ * and (async mode) the nearest resident ancestor, once per view. */
+__device__ void resolve_body(const ResolveView& R, uint32_t first, uint32_t stride)
 {
     const uint32_t n = *R.n_visible_ptr;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += gridDim.x * blockDim.x)
+    for (uint32_t i = first; i < n; i += stride)
     {
         const uint64_t id = R.visible[i];
         const uint64_t idx = node_index(R.level_offset, R.root_blocks, id);
@@ -62,6 +61,7 @@ __global__ void resolve_kernel(ResolveView R)
         if (slot >= 0)
         {
             R.node_stamp[idx] = R.frame;
+            R.view_stamp[idx] = R.view_frame;
             atomicAdd(&R.counters[FC_AVAILABLE], 1u);
             emit_render(R, id, uint32_t(slot));
             continue;
@@ -82,7 +82,8 @@ __global__ void resolve_kernel(ResolveView R)
             const int32_t ps = R.node_table[pidx];
             if (ps >= 0)
             {
-                if (atomicExch(&R.node_stamp[pidx], R.frame) != R.frame)
+                R.node_stamp[pidx] = R.frame;
+                if (atomicExch(&R.view_stamp[pidx], R.view_frame) != R.view_frame)
                     emit_render(R, cur, uint32_t(ps));
                 break;
             }
@@ -92,12 +93,11 @@ __global__ void resolve_kernel(ResolveView R)
 
 /* Drops rendering-set entries that have an ancestor in the set, as
  * RenderingSetGenerator::generateRenderingSet does (RenderingSetGeneratorFilter
- * .cpp:63-79): every entry of this frame carries node_stamp == frame. */
-__global__ void prune_kernel(ResolveView R)
+ * .cpp:63-79): every entry of this view carries view_stamp == view_frame. */
+__device__ void prune_body(const ResolveView& R, uint32_t first, uint32_t stride)
 {
     const uint32_t n = min(R.counters[FC_RENDERED], R.render_capacity);
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < n;
-         e += gridDim.x * blockDim.x)
+    for (uint32_t e = first; e < n; e += stride)
     {
         const uint64_t id = R.render_ids[e];
         uint64_t cur = id;
@@ -106,7 +106,7 @@ __global__ void prune_kernel(ResolveView R)
         {
             cur = nid_make(nid_level(cur) - 1u, nid_x(cur) >> 1, nid_y(cur) >> 1,
                            nid_z(cur) >> 1, nid_t(cur));
-            if (R.node_stamp[node_index(R.level_offset, R.root_blocks, cur)] == R.frame)
+            if (R.view_stamp[node_index(R.level_offset, R.root_blocks, cur)] == R.view_frame)
             {
                 shadowed = true;
                 break;
@@ -123,12 +123,10 @@ __global__ void prune_kernel(ResolveView R)
 }
 
 /* Splats the rendering set into the leaf grid; one warp per entry. */
-__global__ void leaf_fill_kernel(ResolveView R)
+__device__ void leaf_fill_body(const ResolveView& R, uint32_t warp, uint32_t nwarps)
 {
     const uint32_t n = min(R.counters[FC_RENDERED], R.render_capacity);
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t e = warp; e < n; e += nwarps)
     {
         const uint64_t id = R.render_ids[e];
@@ -154,10 +152,40 @@ __global__ void leaf_fill_kernel(ResolveView R)
     }
 }
 
+__global__ void resolve_kernel(ResolveView R)
+{
+    resolve_body(R, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+__global__ void prune_kernel(ResolveView R)
+{
+    prune_body(R, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+__global__ void leaf_fill_kernel(ResolveView R)
+{
+    leaf_fill_body(R, (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                   (gridDim.x * blockDim.x) >> 5);
+}
+/* multi-view variants: blockIdx.y selects the view */
+__global__ void resolve_views_kernel(const ResolveView* __restrict__ Rs)
+{
+    resolve_body(Rs[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x,
+                 gridDim.x * blockDim.x);
+}
+__global__ void prune_views_kernel(const ResolveView* __restrict__ Rs)
+{
+    prune_body(Rs[blockIdx.y], blockIdx.x * blockDim.x + threadIdx.x,
+               gridDim.x * blockDim.x);
+}
+__global__ void leaf_fill_views_kernel(const ResolveView* __restrict__ Rs)
+{
+    leaf_fill_body(Rs[blockIdx.y], (blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                   (gridDim.x * blockDim.x) >> 5);
+}
+
 /* nSamplesPerRay from the finest rendered level (RayCastRenderer.cpp:
  * 216-233 for LV_STEP_REFERENCE; half a voxel for LV_STEP_HALF_VOXEL). */
-__global__ void step_kernel(uint32_t* counters, uint32_t fixed, uint32_t policy,
-                            uint32_t max_voxel_dim, uint32_t depth)
+__device__ void step_body(uint32_t* counters, uint32_t fixed, uint32_t policy,
+                          uint32_t max_voxel_dim, uint32_t depth)
 {
     uint32_t n = fixed;
     if (n == 0)
@@ -176,6 +204,20 @@ __global__ void step_kernel(uint32_t* counters, uint32_t fixed, uint32_t policy,
             n = 1;
     }
     counters[FC_SAMPLES_PER_RAY] = n;
+}
+
+__global__ void step_kernel(uint32_t* counters, uint32_t fixed, uint32_t policy,
+                            uint32_t max_voxel_dim, uint32_t depth)
+{
+    step_body(counters, fixed, policy, max_voxel_dim, depth);
+}
+
+__global__ void step_views_kernel(const RayView* __restrict__ views, uint32_t n)
+{
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n)
+        step_body(views[v].counters, views[v].samples_fixed, views[v].step_policy,
+                  views[v].max_voxel_dim, views[v].depth);
 }
 
 template <int DT>
@@ -221,6 +263,7 @@ __device__ __forceinline__ float sample_brick(const RayView& V,
     return fmaf(b1 - b0, fz, b0);
 }
 
+template <int TFS>
 __device__ __forceinline__ float4 tf_lookup(const RayView& V, float d)
 {
     const float s = fmaf(d, float(V.tfn), -0.5f);
@@ -229,7 +272,9 @@ __device__ __forceinline__ float4 tf_lookup(const RayView& V, float d)
     const int last = int(V.tfn) - 1;
     const int i0 = min(max(int(fl), 0), last);
     const int i1 = min(max(int(fl) + 1, 0), last);
-    const float4 a = __ldg(V.tf + i0), b = __ldg(V.tf + i1);
+    /* TFS: the table is in shared memory (generic loads), else read-only global */
+    const float4 a = TFS ? V.tf[i0] : __ldg(V.tf + i0);
+    const float4 b = TFS ? V.tf[i1] : __ldg(V.tf + i1);
     return make_float4(fmaf(b.x - a.x, f, a.x), fmaf(b.y - a.y, f, a.y),
                        fmaf(b.z - a.z, f, a.z), fmaf(b.w - a.w, f, a.w));
 }
@@ -325,7 +370,7 @@ __device__ __forceinline__ RayGeom ray_setup(const RayView& V, uint32_t px,
     return g;
 }
 
-template <int DT, int FILTER>
+template <int DT, int FILTER, int TFS>
 __device__ float4 march(const RayView& V, const RayGeom& g, float step,
                         float ac, uint32_t& nsamp)
 {
@@ -389,7 +434,7 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
                                  __uint2float_rn(V.O[a]));
         const float value = sample_brick<DT, FILTER>(V, brick, local);
         const float dens = fmaf(value, V.dmul, V.dadd);
-        const float4 src = tf_lookup(V, dens);
+        const float4 src = tf_lookup<TFS>(V, dens);
         const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
         const float alpha = 1.0f - exp2f(ac * __log2f(1.0f - am));
         const float w = alpha * (1.0f - dst.w);
@@ -416,7 +461,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
     if (px < V.W && py < V.H)
     {
         const RayGeom g = ray_setup(V, px, py);
-        const float4 r = march<DT, FILTER>(V, g, step, ac, nsamp);
+        const float4 r = march<DT, FILTER, 0>(V, g, step, ac, nsamp);
         V.out[uint64_t(py) * V.W + px] = r;
     }
     /* warp-aggregated 64-bit sample count */
@@ -426,6 +471,86 @@ __global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
         s += __shfl_down_sync(0xFFFFFFFFu, s, o);
     if ((threadIdx.x + threadIdx.y * blockDim.x) % 32 == 0 && s)
         atomicAdd(reinterpret_cast<unsigned long long*>(V.counters + FC_SAMPLES_LO), s);
+}
+
+/* Batched mode: one persistent launch renders the tiles of many views. Each
+ * CTA pops (view, tile) work items from a device queue (one atomic per
+ * tile), keeps the current view's constants (and optionally its transfer
+ * function) in shared memory, and ray casts tile_w x tile_h pixels. */
+template <int DT, int FILTER, int TF_SHARED>
+__global__ void __launch_bounds__(256)
+    raycast_persistent_kernel(const RayView* __restrict__ views, TileQueue Q)
+{
+    __shared__ RayView sV;
+    __shared__ uint32_t s_item, s_view;
+    extern __shared__ float4 s_tf[];
+    const uint32_t total = Q.tile_start[Q.n_views];
+    uint32_t cached = 0xFFFFFFFFu;
+    float step = 0.f, ac = 0.f;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+        {
+            const uint32_t item = atomicAdd(Q.head, 1u);
+            uint32_t lo = 0, hi = Q.n_views;
+            if (item < total)
+                while (hi - lo > 1)
+                {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (Q.tile_start[mid] <= item)
+                        lo = mid;
+                    else
+                        hi = mid;
+                }
+            s_item = item;
+            s_view = lo;
+        }
+        __syncthreads();
+        const uint32_t item = s_item;
+        const uint32_t gv = s_view;
+        if (item >= total)
+            break;
+        const uint32_t v = Q.view_ids[gv];
+        if (v != cached)
+        {
+            const uint32_t* src = reinterpret_cast<const uint32_t*>(views + v);
+            uint32_t* dst = reinterpret_cast<uint32_t*>(&sV);
+            for (uint32_t w = threadIdx.x; w < sizeof(RayView) / 4; w += blockDim.x)
+                dst[w] = src[w];
+            __syncthreads();
+            if (TF_SHARED)
+            {
+                for (uint32_t i = threadIdx.x; i < sV.tfn; i += blockDim.x)
+                    s_tf[i] = sV.tf[i];
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    sV.tf = s_tf;
+                __syncthreads();
+            }
+            cached = v;
+            const uint32_t n = sV.counters[FC_SAMPLES_PER_RAY];
+            step = __fdiv_rn(1.0f, __uint2float_rn(n));
+            ac = __fdiv_rn(32.0f, __uint2float_rn(n));
+        }
+        const uint32_t t = item - Q.tile_start[gv];
+        const uint32_t tiles_x = (sV.W + Q.tile_w - 1) / Q.tile_w;
+        const uint32_t px = (t % tiles_x) * Q.tile_w + threadIdx.x % Q.tile_w;
+        const uint32_t py = (t / tiles_x) * Q.tile_h + threadIdx.x / Q.tile_w;
+        uint32_t nsamp = 0;
+        if (px < sV.W && py < sV.H && threadIdx.x < Q.tile_w * Q.tile_h)
+        {
+            const RayGeom g = ray_setup(sV, px, py);
+            const float4 r = march<DT, FILTER, TF_SHARED>(sV, g, step, ac, nsamp);
+            sV.out[uint64_t(py) * sV.W + px] = r;
+        }
+        unsigned long long sum = nsamp;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+        if ((threadIdx.x & 31u) == 0 && sum)
+            atomicAdd(reinterpret_cast<unsigned long long*>(sV.counters + FC_SAMPLES_LO), sum);
+        __syncthreads();
+    }
 }
 
 __global__ void to_rgba8_kernel(const float4* __restrict__ in,
@@ -483,6 +608,57 @@ lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
         return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
     LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;
+}
+
+lv_status launch_views_pipeline(lv_ctx* ctx, const ResolveView* d_resolve,
+                                const RayView* d_rays, uint32_t n, cudaStream_t s)
+{
+    resolve_views_kernel<<<dim3(8, n), 256, 0, s>>>(d_resolve);
+    prune_views_kernel<<<dim3(8, n), 256, 0, s>>>(d_resolve);
+    leaf_fill_views_kernel<<<dim3(16, n), 256, 0, s>>>(d_resolve);
+    step_views_kernel<<<(n + 127) / 128, 128, 0, s>>>(d_rays, n);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+namespace
+{
+template <int DT, int F, int TFS>
+lv_status persistent_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
+                              uint32_t grid, size_t smem, cudaStream_t s)
+{
+    auto k = raycast_persistent_kernel<DT, F, TFS>;
+    if (smem > 48 * 1024)
+        LV_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          int(smem)));
+    k<<<grid, Q.tile_w * Q.tile_h, smem, s>>>(d_rays, Q);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+} // namespace
+
+lv_status launch_persistent(lv_ctx* ctx, int dtype, int filter, int tf_shared,
+                            const RayView* d_rays, const TileQueue& Q, uint32_t ctas,
+                            uint32_t tfn_max, cudaStream_t s)
+{
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const uint32_t grid = uint32_t(sms) * ctas;
+    const size_t smem = tf_shared ? size_t(tfn_max) * sizeof(float4) : 0;
+    const bool u16 = dtype == LV_DT_UINT16, tri = filter == LV_FILTER_TRILINEAR;
+    if (tf_shared)
+    {
+        if (u16)
+            return tri ? persistent_dispatch<LV_DT_UINT16, 1, 1>(ctx, d_rays, Q, grid, smem, s)
+                       : persistent_dispatch<LV_DT_UINT16, 0, 1>(ctx, d_rays, Q, grid, smem, s);
+        return tri ? persistent_dispatch<LV_DT_UINT8, 1, 1>(ctx, d_rays, Q, grid, smem, s)
+                   : persistent_dispatch<LV_DT_UINT8, 0, 1>(ctx, d_rays, Q, grid, smem, s);
+    }
+    if (u16)
+        return tri ? persistent_dispatch<LV_DT_UINT16, 1, 0>(ctx, d_rays, Q, grid, smem, s)
+                   : persistent_dispatch<LV_DT_UINT16, 0, 0>(ctx, d_rays, Q, grid, smem, s);
+    return tri ? persistent_dispatch<LV_DT_UINT8, 1, 0>(ctx, d_rays, Q, grid, smem, s)
+               : persistent_dispatch<LV_DT_UINT8, 0, 0>(ctx, d_rays, Q, grid, smem, s);
 }
 
 } // namespace lv

@@ -42,13 +42,6 @@ lv_status launch_resolve(lv_ctx* ctx, const ResolveView& R, cudaStream_t s);
 lv_status launch_leaf_fill(lv_ctx* ctx, const ResolveView& R, cudaStream_t s);
 lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s);
 
-enum SourceKind
-{
-    SRC_CALLBACK = 0,
-    SRC_BLOB_DEVICE = 1,
-    SRC_BLOB_HOST = 2
-};
-
 namespace
 {
 __global__ void scatter_kernel(int32_t* __restrict__ table,
@@ -72,88 +65,9 @@ uint64_t round_units(uint64_t bytes)
 }
 } // namespace
 
-/* One resident brick. */
-struct Resident
-{
-    lv_volume* vol;
-    uint64_t node_idx;
-    uint32_t unit;
-    uint32_t units;
-};
-
-struct Pool
-{
-    DeviceBuffer arena;
-    uint64_t capacity_units = 0;
-    uint64_t bump = 0;
-    std::map<uint32_t, std::vector<uint32_t>> free_by_units;
-    std::list<Resident> lru; /* front = oldest load */
-    uint64_t resident_bytes = 0;
-};
-
-struct Renderer
-{
-    DeviceBuffer visible, sel_result, render_ids, render_slots, missing,
-        counters, leaf, pairs;
-    PinnedBuffer h_counters, h_missing, h_pairs;
-    uint64_t visible_capacity = 0;
-    uint32_t frame = 0;
-    lv_frame_stats stats{};
-    cudaStream_t last_stream = nullptr;
-    bool have_last = false;
-    /* async mode: misses of the previous frame, copied back */
-    cudaEvent_t pending_event = nullptr;
-    lv_volume* pending_vol = nullptr;
-    uint32_t pending_max = 0;
-    uint32_t pending_frame = 0;
-    cudaEvent_t render_event = nullptr;
-    cudaEvent_t upload_event = nullptr;
-    /* timing of the last frame: selection and ray cast */
-    cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
-    uint32_t launches = 0;
-};
-
 } // namespace lv
 
-struct lv_tf
-{
-    lv_ctx* ctx;
-    lv::DeviceBuffer rgba;
-    uint32_t n;
-};
-
-struct lv_volume
-{
-    lv_ctx* ctx = nullptr;
-    lv_volume_info info{};
-    int kind = lv::SRC_CALLBACK;
-    lv_get_data_fn fn = nullptr;
-    void* user = nullptr;
-    lv_blob_desc blob{};
-    lv::DeviceBuffer d_blobs;
-    lv::PinnedBuffer host_store;
-    uint64_t brick_bytes = 0;
-    uint32_t slot_units = 0;
-    uint64_t level_offset[lv::kMaxLevels + 1] = {};
-    uint64_t n_nodes = 0;
-    lv::DeviceBuffer node_table, node_stamp;
-    std::vector<int32_t> host_table;
-    uint32_t time_step = 0;
-    /* pinned staging ring for callback sources */
-    std::vector<lv::PinnedBuffer*> staging;
-    std::vector<cudaEvent_t> staging_ev;
-    ~lv_volume()
-    {
-        for (auto* p : staging)
-            delete p;
-        for (auto e : staging_ev)
-            cudaEventDestroy(e);
-    }
-};
-
 namespace lv
-{
-namespace
 {
 uint32_t bytes_per_voxel(uint32_t dt)
 {
@@ -235,20 +149,7 @@ lv_status ensure_renderer(lv_ctx* ctx)
 lv_status reserve_selection(lv_ctx* ctx, const lv_volume_info& info,
                             cudaStream_t s)
 {
-    const uint64_t need = max_frontier(info);
-    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(need, 64), 1u << 24);
-    SelectScratch& S = ctx->sel;
-    if (S.frontier_capacity >= cap)
-        return LV_OK;
-    LV_CUDA(ctx, cudaStreamSynchronize(s));
-    for (int i = 0; i < 2; ++i)
-    {
-        LV_CUDA(ctx, S.ids[i].reserve(sizeof(uint64_t) * cap));
-        LV_CUDA(ctx, S.view[i].reserve(sizeof(uint32_t) * cap));
-    }
-    LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 2)));
-    S.frontier_capacity = uint32_t(cap);
-    return LV_OK;
+    return reserve_frontier(ctx, max_frontier(info), s);
 }
 
 /* Frees one slot of `units` for a new brick, evicting the oldest resident
@@ -506,7 +407,6 @@ void drop_volume_residency(lv_ctx* ctx, lv_volume* v)
     }
 }
 
-} // namespace
 } // namespace lv
 
 /* ================================================================ C ABI */
@@ -1000,7 +900,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     RV.n_visible_ptr = R.sel_result.as<uint32_t>() + LV_SEL_WRITTEN;
     RV.node_table = vol->node_table.as<int32_t>();
     RV.node_stamp = vol->node_stamp.as<uint32_t>();
+    RV.view_stamp = vol->node_stamp.as<uint32_t>();
     RV.frame = frame;
+    RV.view_frame = frame;
     RV.depth = info.depth;
     for (int a = 0; a < 3; ++a)
     {
