@@ -304,10 +304,11 @@ lv_status lv_batch_get_config(const lv_batch* batch, lv_batch_config* cfg);
 lv_status lv_batch_render(lv_batch* batch, const lv_batch_view* views,
                           uint32_t n, void* stream);
 /* Per-view statistics of the last lv_batch_render (synchronises with it);
- * select_ms / raycast_ms (nullable) receive the device time of the
- * selection + residency passes and of the persistent ray cast. */
+ * batch_ms / raycast_ms (nullable) receive the device time of the whole
+ * batch (CUDA events around it) and of the persistent ray-cast launches
+ * (device global timer, first CTA start to last CTA end). */
 lv_status lv_batch_stats(lv_batch* batch, lv_frame_stats* out, uint32_t n,
-                         float* select_ms, float* raycast_ms);
+                         float* batch_ms, float* raycast_ms);
 /* Times the persistent kernel on this batch for every tile shape in
  * {8x8, 16x8, 8x16, 16x16, 32x4, 32x8}, CTAs per SM in {2, 4, 8} and
  * transfer-function staging on/off (reps timed launches each), keeps the

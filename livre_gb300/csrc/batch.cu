@@ -30,19 +30,17 @@ namespace lv
 {
 lv_status launch_views_pipeline(lv_ctx* ctx, const ResolveView* d_resolve,
                                 const RayView* d_rays, uint32_t n, cudaStream_t s);
-lv_status launch_persistent(lv_ctx* ctx, int dtype, int filter, int tf_shared,
-                            const RayView* d_rays, const TileQueue& Q, uint32_t ctas,
-                            uint32_t tfn_max, cudaStream_t s);
 void type_range(uint32_t dt, float& lo, float& hi);
 } // namespace lv
 
 namespace
 {
+/* Views rendered by one instantiation of the persistent kernel. */
 struct Group
 {
-    int dtype, filter;
     std::vector<uint32_t> views;
 };
+constexpr int kGroups = 8;
 
 /* byte offsets of one view's device regions */
 struct ViewSlots
@@ -78,6 +76,7 @@ struct lv_batch
     uint64_t uploaded_bytes = 0;
     uint32_t uploaded = 0;
     uint32_t launches = 0;
+    uint32_t last_n = 0;
 
     ~lv_batch()
     {
@@ -118,14 +117,9 @@ ParamLayout param_layout(uint32_t n)
     L.resolve = al(L.lod + sizeof(LodView) * n);
     L.ray = al(L.resolve + sizeof(ResolveView) * n);
     L.tables = al(L.ray + sizeof(RayView) * n);
-    /* 4 groups x (view ids n + tile starts n + 1) */
-    L.bytes = al(L.tables + sizeof(uint32_t) * 4 * (2 * n + 1));
+    /* kGroups x (view ids n + tile starts n + 1) */
+    L.bytes = al(L.tables + sizeof(uint32_t) * kGroups * (2 * n + 1));
     return L;
-}
-
-int group_index(int dtype, int filter)
-{
-    return (dtype == LV_DT_UINT16 ? 2 : 0) + (filter == LV_FILTER_TRILINEAR ? 1 : 0);
 }
 
 lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
@@ -166,7 +160,7 @@ lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
     const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
     b->lists.release();
     LV_CUDA(ctx, b->lists.reserve(per_view * vcap));
-    LV_CUDA(ctx, b->h_out.reserve(sizeof(uint32_t) * kOutWords * vcap +
+    LV_CUDA(ctx, b->h_out.reserve(sizeof(uint32_t) * (kOutWords * vcap + 64) +
                                   sizeof(uint64_t) * b->missing_stride * vcap));
     /* view stamps start at 0; launch ids start at 1 */
     LV_CUDA(ctx, cudaMemset(b->lists.ptr, 0, per_view * vcap));
@@ -201,7 +195,7 @@ lv_status process_misses(lv_batch* b)
     b->pending = false;
     const uint32_t* out = b->h_out.as<uint32_t>();
     const uint64_t* miss = reinterpret_cast<const uint64_t*>(
-        b->h_out.as<uint8_t>() + sizeof(uint32_t) * kOutWords * b->views_cap);
+        b->h_out.as<uint8_t>() + sizeof(uint32_t) * (kOutWords * b->views_cap + 64));
     for (uint32_t i = 0; i < b->last.size(); ++i)
     {
         const uint32_t* c = out + kOutWords * i;
@@ -237,12 +231,7 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n,
     uint32_t* dleaf = b->leafs.as<uint32_t>();
     total_roots = 0;
     tfn_max = 0;
-    groups.assign(4, Group{});
-    for (int g = 0; g < 4; ++g)
-    {
-        groups[g].dtype = g >= 2 ? LV_DT_UINT16 : LV_DT_UINT8;
-        groups[g].filter = (g & 1) ? LV_FILTER_TRILINEAR : LV_FILTER_NEAREST;
-    }
+    groups.assign(kGroups, Group{});
     for (uint32_t i = 0; i < n; ++i)
     {
         const lv_batch_view& bv = views[i];
@@ -299,59 +288,16 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n,
         R.Lf = Lf;
 
         RayView& V = rays[i];
-        std::memset(&V, 0, sizeof(V));
-        float lim[6], planes[6][4], eye[3], dir[3];
-        bool ok = false;
-        frustum_setup(d.camera.modelview, d.camera.projection, V.inv_mv, V.inv_p, lim,
-                      planes, eye, dir, &ok);
-        if (!ok)
-            return fail(ctx, LV_EINVAL, "singular camera");
-        const uint32_t bm = std::max(dims[0], std::max(dims[1], dims[2]));
-        for (int a = 0; a < 3; ++a)
-        {
-            V.eye[a] = eye[a];
-            const float half = info.world_size[a] / 2.0f;
-            V.gmin[a] = -half;
-            V.gmax[a] = half;
-            V.gscale[a] = float(bm) / info.world_size[a];
-            V.dims[a] = dims[a];
-            V.N[a] = info.max_block[a];
-            V.O[a] = info.overlap[a];
-            V.B[a] = info.max_block[a] - 2u * info.overlap[a];
-        }
-        V.nearp = lim[4];
-        V.n_clip = lod.n_clip_planes;
-        std::memcpy(V.clip, lod.clip_planes, sizeof(V.clip));
-        V.Lf = Lf;
-        V.dtype = info.dtype;
-        V.filter = d.filter;
-        float lo = d.data_range[0], hi = d.data_range[1];
-        if (!(hi > lo))
-            type_range(info.dtype, lo, hi);
-        V.dmul = 1.0f / (hi - lo);
-        V.dadd = -lo / (hi - lo);
-        V.early = d.early_exit;
-        V.W = d.width;
-        V.H = d.height;
-        V.samples_fixed = d.samples_per_ray;
-        V.step_policy = d.step_policy;
-        V.max_voxel_dim = std::max(info.voxels[0], std::max(info.voxels[1], info.voxels[2]));
-        V.depth = info.depth;
-        V.leaf = R.leaf;
-        V.pool = ctx->pool->arena.as<uint8_t>();
-        V.tf = bv.tf->rgba.as<float4>();
-        V.tfn = bv.tf->n;
-        V.out = reinterpret_cast<float4*>(bv.d_rgba);
-        V.counters = counters;
+        st = make_ray_view(ctx, vol, bv.tf, d, lod, bv.d_rgba, R.leaf, counters, V);
+        if (st != LV_OK)
+            return st;
         tfn_max = std::max(tfn_max, bv.tf->n);
-        if (info.dtype != LV_DT_UINT8 && info.dtype != LV_DT_UINT16)
-            return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
-        groups[group_index(int(info.dtype), int(d.filter))].views.push_back(i);
+        groups[kernel_variant(V.dtype, V.filter, V.edge)].views.push_back(i);
     }
     /* queue tables */
     uint32_t* tables = reinterpret_cast<uint32_t*>(h + PL.tables);
     const uint32_t stride = 2 * b->views_cap + 1;
-    for (int g = 0; g < 4; ++g)
+    for (int g = 0; g < kGroups; ++g)
     {
         uint32_t* ids = tables + stride * g;
         uint32_t* starts = ids + b->views_cap;
@@ -379,7 +325,6 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     LV_CUDA(ctx, cudaMemcpyAsync(d, b->h_params.ptr, PL.bytes, cudaMemcpyHostToDevice, s));
     LV_CUDA(ctx, cudaMemsetAsync(b->zeroed.ptr, 0, sizeof(uint32_t) * (kOutWords * n + 64), s));
     LV_CUDA(ctx, cudaMemsetAsync(b->leafs.ptr, 0xFF, sizeof(uint32_t) * b->cells_stride * n, s));
-    LV_CUDA(ctx, cudaEventRecord(b->t_sel0, s));
     lv_status st = enqueue_selection(ctx, reinterpret_cast<LodView*>(d + PL.lod), n,
                                      total_roots, b->depth_max, s);
     if (st != LV_OK)
@@ -388,11 +333,11 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
                                reinterpret_cast<RayView*>(d + PL.ray), n, s);
     if (st != LV_OK)
         return st;
-    LV_CUDA(ctx, cudaEventRecord(b->t_ray0, s));
-    uint32_t* heads = b->zeroed.as<uint32_t>() + kOutWords * n;
+    uint32_t* heads = b->zeroed.as<uint32_t>() + kOutWords * n; /* kGroups words */
+    unsigned long long* clock = reinterpret_cast<unsigned long long*>(heads + kGroups);
     const uint32_t* tables = reinterpret_cast<const uint32_t*>(d + PL.tables);
     const uint32_t stride = 2 * b->views_cap + 1;
-    for (int g = 0; g < 4; ++g)
+    for (int g = 0; g < kGroups; ++g)
     {
         if (groups[g].views.empty())
             continue;
@@ -403,17 +348,18 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         Q.tile_w = b->cfg.tile_w;
         Q.tile_h = b->cfg.tile_h;
         Q.head = heads + g;
-        st = launch_persistent(ctx, groups[g].dtype, groups[g].filter, b->cfg.tf_shared,
+        Q.clock = clock;
+        st = launch_persistent(ctx, g, b->cfg.tf_shared,
                                reinterpret_cast<RayView*>(d + PL.ray), Q, b->cfg.ctas_per_sm,
                                tfn_max, s);
         if (st != LV_OK)
             return st;
     }
-    LV_CUDA(ctx, cudaEventRecord(b->t_ray1, s));
-    LV_CUDA(ctx, cudaMemcpyAsync(b->h_out.ptr, b->zeroed.ptr, sizeof(uint32_t) * kOutWords * n,
+    LV_CUDA(ctx, cudaMemcpyAsync(b->h_out.ptr, b->zeroed.ptr,
+                                 sizeof(uint32_t) * (kOutWords * n + kGroups + 4),
                                  cudaMemcpyDeviceToHost, s));
     /* missing lists, one strided copy */
-    uint8_t* hmiss = b->h_out.as<uint8_t>() + sizeof(uint32_t) * kOutWords * b->views_cap;
+    uint8_t* hmiss = b->h_out.as<uint8_t>() + sizeof(uint32_t) * (kOutWords * b->views_cap + 64);
     const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
     LV_CUDA(ctx, cudaMemcpy2DAsync(hmiss, b->missing_stride * 8,
                                    b->lists.as<uint8_t>() + view_slots(b, 0).missing, per_view,
@@ -520,14 +466,15 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     st = fill_params(b, views, n, groups, total_roots, tfn_max);
     if (st != LV_OK)
         return st;
-    if (b->cfg.tf_shared && tfn_max > 4096)
-        return fail(ctx, LV_EINVAL, "shared-memory transfer functions hold at most 4096 entries");
+    if (b->cfg.tf_shared && tfn_max > 2048)
+        return fail(ctx, LV_EINVAL, "shared-memory transfer functions hold at most 2048 entries");
     uint32_t mask = 0;
-    for (int g = 0; g < 4; ++g)
+    for (int g = 0; g < kGroups; ++g)
         if (!groups[g].views.empty())
             mask |= 1u << g;
     LV_CUDA(ctx, cudaEventRecord(b->user_ready, user));
     LV_CUDA(ctx, cudaStreamWaitEvent(b->stream, b->user_ready, 0));
+    LV_CUDA(ctx, cudaEventRecord(b->t_sel0, b->stream));
     if (b->cfg.use_graph)
     {
         const auto key = std::make_tuple(n, mask, b->cfg.tile_w, b->cfg.tile_h, b->cfg.ctas_per_sm,
@@ -566,8 +513,10 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
         if (st != LV_OK)
             return st;
     }
+    LV_CUDA(ctx, cudaEventRecord(b->t_ray1, b->stream));
     LV_CUDA(ctx, cudaEventRecord(b->done, b->stream));
     LV_CUDA(ctx, cudaStreamWaitEvent(user, b->done, 0));
+    b->last_n = n;
     b->last.assign(views, views + n);
     b->pending = true;
     /* selection: roots + levels + finish; resolve, prune, leaf, step;
@@ -577,7 +526,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
 }
 
 extern "C" lv_status lv_batch_stats(lv_batch* b, lv_frame_stats* out, uint32_t n,
-                                    float* select_ms, float* raycast_ms)
+                                    float* batch_ms, float* raycast_ms)
 {
     if (!b || (n && !out))
         return LV_EINVAL;
@@ -607,10 +556,20 @@ extern "C" lv_status lv_batch_stats(lv_batch* b, lv_frame_stats* out, uint32_t n
         }
         out[i] = s;
     }
-    if (select_ms)
-        cudaEventElapsedTime(select_ms, b->t_sel0, b->t_ray0);
+    if (batch_ms)
+    {
+        if (cudaEventElapsedTime(batch_ms, b->t_sel0, b->t_ray1) != cudaSuccess)
+        {
+            cudaGetLastError();
+            *batch_ms = 0.f;
+        }
+    }
     if (raycast_ms)
-        cudaEventElapsedTime(raycast_ms, b->t_ray0, b->t_ray1);
+    {
+        const unsigned long long* clock = reinterpret_cast<const unsigned long long*>(
+            h + kOutWords * b->last_n + kGroups);
+        *raycast_ms = clock[1] > clock[0] ? float(double(clock[1] - clock[0]) * 1e-6) : 0.f;
+    }
     return LV_OK;
 }
 
@@ -645,8 +604,8 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
                         ok = false;
                         break;
                     }
-                    float sel = 0.f, ray = 0.f;
-                    lv_batch_stats(b, nullptr, 0, &sel, &ray);
+                    float all = 0.f, ray = 0.f;
+                    lv_batch_stats(b, nullptr, 0, &all, &ray);
                     if (r > 0)
                         total += ray;
                 }

@@ -68,6 +68,7 @@ struct RayView
     float eye[3];
     float nearp;
     float gmin[3], gmax[3], gscale[3];
+    float goff[3];    /* half world size * gscale: f = fma(p, gscale, goff) */
     float clip[6][4];
     uint32_t n_clip;
     uint32_t dims[3]; /* leaf grid (finest level) */
@@ -75,6 +76,7 @@ struct RayView
     uint32_t N[3], B[3], O[3];
     uint32_t dtype;   /* lv_dtype */
     uint32_t filter;
+    uint32_t edge;    /* 1: some overlap is 0, clamp every trilinear tap */
     float dmul, dadd; /* density = value * dmul + dadd */
     float early;
     uint32_t W, H;
@@ -84,7 +86,7 @@ struct RayView
     uint32_t depth;
     const uint32_t* leaf;
     const uint8_t* pool; /* brick = pool + slot * kSlotUnit */
-    const float4* tf;
+    const float4* tf; /* tfn (value, next - value) pairs */
     uint32_t tfn;
     float4* out;
     uint32_t* counters; /* FrameCounters */
@@ -141,6 +143,7 @@ struct TileQueue
     uint32_t n_views;
     uint32_t tile_w, tile_h;
     uint32_t* head;             /* zeroed before the launch */
+    unsigned long long* clock;  /* [first CTA start, last CTA end] in ns (%globaltimer) */
 };
 
 LV_HD uint64_t node_index(const uint64_t* level_offset,

@@ -236,6 +236,15 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                         uint32_t n, uint32_t protect_frame, cudaStream_t render,
                         uint32_t& n_loaded, uint64_t& bytes_loaded);
 lv_status ensure_renderer(lv_ctx* ctx);
+/* Ray-cast constants of one view (shared by the plain and batched paths). */
+lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
+                        const lv_render_desc& desc, const lv_lod_params& lod, float* d_rgba,
+                        uint32_t* leaf, uint32_t* counters, RayView& V);
+/* Index of the ray-cast kernel instantiation for a view. */
+int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge);
+lv_status launch_persistent(lv_ctx* ctx, int variant, int tf_shared, const RayView* d_rays,
+                            const TileQueue& Q, uint32_t ctas, uint32_t tfn_max,
+                            cudaStream_t s);
 lv_status launch_resolve_views(lv_ctx* ctx, const ResolveView* d_views,
                                uint32_t n_views, cudaStream_t s);
 } // namespace lv

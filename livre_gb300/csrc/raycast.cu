@@ -220,40 +220,94 @@ __global__ void step_views_kernel(const RayView* __restrict__ views, uint32_t n)
                   views[v].max_voxel_dim, views[v].depth);
 }
 
-template <int DT>
-__device__ __forceinline__ float voxel(const uint8_t* brick, uint32_t i)
+/* Hardware base-2 exponential / logarithm (PTX ex2/lg2, approximate, FTZ). */
+__device__ __forceinline__ float ex2_approx(float x)
 {
-    if (DT == LV_DT_UINT16)
-        return float(__ldg(reinterpret_cast<const uint16_t*>(brick) + i));
-    return float(__ldg(brick + i));
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg2_approx(float x)
+{
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
-template <int DT, int FILTER>
+__device__ __forceinline__ unsigned long long globaltimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <int DT>
+__device__ __forceinline__ float ldv(const uint8_t* p)
+{
+    if (DT == LV_DT_UINT16)
+        return float(__ldg(reinterpret_cast<const uint16_t*>(p)));
+    return float(__ldg(p));
+}
+
+/* Voxel value at slot coordinate s (nearest: s = local position; trilinear:
+ * s = local position - 0.5, texel centres on integers). EDGE = 1 clamps every
+ * tap to the brick (GL_CLAMP_TO_EDGE, needed without overlap); EDGE = 0 uses
+ * one base address and immediate offsets, valid when every overlap >= 1
+ * keeps both taps inside the brick (the base is still clamped so no access
+ * can leave the slot). */
+template <int DT, int FILTER, int EDGE>
 __device__ __forceinline__ float sample_brick(const RayView& V,
                                               const uint8_t* brick,
-                                              const float local[3])
+                                              const float s[3])
 {
+    constexpr int bpv = DT == LV_DT_UINT16 ? 2 : 1;
     const int n0 = int(V.N[0]), n1 = int(V.N[1]), n2 = int(V.N[2]);
     if (FILTER == LV_FILTER_NEAREST)
     {
-        const int x = min(max(int(floorf(local[0])), 0), n0 - 1);
-        const int y = min(max(int(floorf(local[1])), 0), n1 - 1);
-        const int z = min(max(int(floorf(local[2])), 0), n2 - 1);
-        return voxel<DT>(brick, uint32_t((z * n1 + y) * n0 + x));
+        const int x = min(max(int(floorf(s[0])), 0), n0 - 1);
+        const int y = min(max(int(floorf(s[1])), 0), n1 - 1);
+        const int z = min(max(int(floorf(s[2])), 0), n2 - 1);
+        return ldv<DT>(brick + ((z * n1 + y) * n0 + x) * bpv);
     }
-    const float sx = local[0] - 0.5f, sy = local[1] - 0.5f, sz = local[2] - 0.5f;
-    const float fx0 = floorf(sx), fy0 = floorf(sy), fz0 = floorf(sz);
-    const float fx = sx - fx0, fy = sy - fy0, fz = sz - fz0;
-    const int ix = int(fx0), iy = int(fy0), iz = int(fz0);
-    const int x0 = min(max(ix, 0), n0 - 1), x1 = min(max(ix + 1, 0), n0 - 1);
-    const int y0 = min(max(iy, 0), n1 - 1), y1 = min(max(iy + 1, 0), n1 - 1);
-    const int z0 = min(max(iz, 0), n2 - 1), z1 = min(max(iz + 1, 0), n2 - 1);
-    const int r00 = (z0 * n1 + y0) * n0, r01 = (z0 * n1 + y1) * n0;
-    const int r10 = (z1 * n1 + y0) * n0, r11 = (z1 * n1 + y1) * n0;
-    const float c000 = voxel<DT>(brick, r00 + x0), c001 = voxel<DT>(brick, r00 + x1);
-    const float c010 = voxel<DT>(brick, r01 + x0), c011 = voxel<DT>(brick, r01 + x1);
-    const float c100 = voxel<DT>(brick, r10 + x0), c101 = voxel<DT>(brick, r10 + x1);
-    const float c110 = voxel<DT>(brick, r11 + x0), c111 = voxel<DT>(brick, r11 + x1);
+    const float fx0 = floorf(s[0]), fy0 = floorf(s[1]), fz0 = floorf(s[2]);
+    const float fx = s[0] - fx0, fy = s[1] - fy0, fz = s[2] - fz0;
+    int ix = int(fx0), iy = int(fy0), iz = int(fz0);
+    float c000, c001, c010, c011, c100, c101, c110, c111;
+    if (EDGE)
+    {
+        const int x0 = min(max(ix, 0), n0 - 1), x1 = min(max(ix + 1, 0), n0 - 1);
+        const int y0 = min(max(iy, 0), n1 - 1), y1 = min(max(iy + 1, 0), n1 - 1);
+        const int z0 = min(max(iz, 0), n2 - 1), z1 = min(max(iz + 1, 0), n2 - 1);
+        const int r00 = (z0 * n1 + y0) * n0, r01 = (z0 * n1 + y1) * n0;
+        const int r10 = (z1 * n1 + y0) * n0, r11 = (z1 * n1 + y1) * n0;
+        c000 = ldv<DT>(brick + (r00 + x0) * bpv);
+        c001 = ldv<DT>(brick + (r00 + x1) * bpv);
+        c010 = ldv<DT>(brick + (r01 + x0) * bpv);
+        c011 = ldv<DT>(brick + (r01 + x1) * bpv);
+        c100 = ldv<DT>(brick + (r10 + x0) * bpv);
+        c101 = ldv<DT>(brick + (r10 + x1) * bpv);
+        c110 = ldv<DT>(brick + (r11 + x0) * bpv);
+        c111 = ldv<DT>(brick + (r11 + x1) * bpv);
+    }
+    else
+    {
+        ix = min(max(ix, 0), n0 - 2);
+        iy = min(max(iy, 0), n1 - 2);
+        iz = min(max(iz, 0), n2 - 2);
+        const int dy = n0 * bpv, dz = n0 * n1 * bpv;
+        const uint8_t* p00 = brick + ((iz * n1 + iy) * n0 + ix) * bpv;
+        const uint8_t* p01 = p00 + dy;
+        const uint8_t* p10 = p00 + dz;
+        const uint8_t* p11 = p10 + dy;
+        c000 = ldv<DT>(p00);
+        c001 = ldv<DT>(p00 + bpv);
+        c010 = ldv<DT>(p01);
+        c011 = ldv<DT>(p01 + bpv);
+        c100 = ldv<DT>(p10);
+        c101 = ldv<DT>(p10 + bpv);
+        c110 = ldv<DT>(p11);
+        c111 = ldv<DT>(p11 + bpv);
+    }
     const float a0 = fmaf(c001 - c000, fx, c000);
     const float a1 = fmaf(c011 - c010, fx, c010);
     const float a2 = fmaf(c101 - c100, fx, c100);
@@ -263,20 +317,20 @@ __device__ __forceinline__ float sample_brick(const RayView& V,
     return fmaf(b1 - b0, fz, b0);
 }
 
+/* Linear, clamp-to-edge lookup of the transfer function, stored as
+ * interleaved (value_i, value_{i+1} - value_i) pairs (last difference 0). */
 template <int TFS>
 __device__ __forceinline__ float4 tf_lookup(const RayView& V, float d)
 {
     const float s = fmaf(d, float(V.tfn), -0.5f);
-    const float fl = floorf(s);
-    const float f = s - fl;
-    const int last = int(V.tfn) - 1;
-    const int i0 = min(max(int(fl), 0), last);
-    const int i1 = min(max(int(fl) + 1, 0), last);
+    const int i0 = min(max(int(floorf(s)), 0), int(V.tfn) - 1);
+    const float f = fmaxf(s - float(i0), 0.0f);
     /* TFS: the table is in shared memory (generic loads), else read-only global */
-    const float4 a = TFS ? V.tf[i0] : __ldg(V.tf + i0);
-    const float4 b = TFS ? V.tf[i1] : __ldg(V.tf + i1);
-    return make_float4(fmaf(b.x - a.x, f, a.x), fmaf(b.y - a.y, f, a.y),
-                       fmaf(b.z - a.z, f, a.z), fmaf(b.w - a.w, f, a.w));
+    const float4* e = V.tf + 2 * i0;
+    const float4 a = TFS ? e[0] : __ldg(e);
+    const float4 b = TFS ? e[1] : __ldg(e + 1);
+    return make_float4(fmaf(b.x, f, a.x), fmaf(b.y, f, a.y), fmaf(b.z, f, a.z),
+                       fmaf(b.w, f, a.w));
 }
 
 __device__ __forceinline__ float Md(const float* m, int r, int c)
@@ -370,7 +424,7 @@ __device__ __forceinline__ RayGeom ray_setup(const RayView& V, uint32_t px,
     return g;
 }
 
-template <int DT, int FILTER, int TFS>
+template <int DT, int FILTER, int TFS, int EDGE>
 __device__ float4 march(const RayView& V, const RayGeom& g, float step,
                         float ac, uint32_t& nsamp)
 {
@@ -384,11 +438,14 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
                            __uint2float_rn(V.dims[2])};
     uint32_t cur = 0xFFFFFFFFu, entry = kLeafEmpty;
     const uint8_t* brick = nullptr;
-    float vs[3] = {0.f, 0.f, 0.f}, base[3] = {0.f, 0.f, 0.f};
+    float vs[3] = {0.f, 0.f, 0.f}, off[3] = {0.f, 0.f, 0.f};
     const float early = V.early;
+    const float half_texel = FILTER == LV_FILTER_TRILINEAR ? 0.5f : 0.0f;
     for (;; ++k)
     {
-        const float t = __fadd_rn(g.tg, __fmul_rn(__int2float_rn(k), step));
+        /* sample position, cell and slot coordinate: single-rounding FMAs in
+         * a fixed order (the CPU oracle evaluates the same fmaf chain) */
+        const float t = fmaf(__int2float_rn(k), step, g.tg);
         if (!(t < g.thi))
             break;
         float f[3];
@@ -397,8 +454,8 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
 #pragma unroll
         for (int a = 0; a < 3; ++a)
         {
-            const float p = __fadd_rn(V.eye[a], __fmul_rn(g.dir[a], t));
-            f[a] = __fmul_rn(__fsub_rn(p, V.gmin[a]), V.gscale[a]);
+            const float p = fmaf(g.dir[a], t, V.eye[a]);
+            f[a] = fmaf(p, V.gscale[a], V.goff[a]);
             const float fl = floorf(f[a]);
             inside = inside && (fl >= 0.0f) && (fl < dimf[a]);
             c[a] = int(fl);
@@ -417,26 +474,28 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
                 const uint32_t slot = entry & kLeafSlotMask;
                 const uint32_t sh = V.Lf - L;
                 brick = V.pool + uint64_t(slot) * kSlotUnit;
+                const float inv_side = __int_as_float(int(127u - sh) << 23); /* 2^-sh */
 #pragma unroll
                 for (int a = 0; a < 3; ++a)
                 {
-                    vs[a] = __fdiv_rn(__uint2float_rn(V.B[a]), __uint2float_rn(1u << sh));
-                    base[a] = __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a]);
+                    vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
+                    off[a] = (__uint2float_rn(V.O[a]) -
+                              __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a])) -
+                             half_texel; /* exact */
                 }
             }
         }
         if (entry == kLeafEmpty)
             continue;
-        float local[3];
+        float sc[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a)
-            local[a] = __fadd_rn(__fsub_rn(__fmul_rn(f[a], vs[a]), base[a]),
-                                 __uint2float_rn(V.O[a]));
-        const float value = sample_brick<DT, FILTER>(V, brick, local);
+            sc[a] = fmaf(f[a], vs[a], off[a]);
+        const float value = sample_brick<DT, FILTER, EDGE>(V, brick, sc);
         const float dens = fmaf(value, V.dmul, V.dadd);
         const float4 src = tf_lookup<TFS>(V, dens);
         const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
-        const float alpha = 1.0f - exp2f(ac * __log2f(1.0f - am));
+        const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
         const float w = alpha * (1.0f - dst.w);
         dst.x = fmaf(src.x, w, dst.x);
         dst.y = fmaf(src.y, w, dst.y);
@@ -449,7 +508,7 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
     return dst;
 }
 
-template <int DT, int FILTER>
+template <int DT, int FILTER, int EDGE>
 __global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
 {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
@@ -461,7 +520,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
     if (px < V.W && py < V.H)
     {
         const RayGeom g = ray_setup(V, px, py);
-        const float4 r = march<DT, FILTER, 0>(V, g, step, ac, nsamp);
+        const float4 r = march<DT, FILTER, 0, EDGE>(V, g, step, ac, nsamp);
         V.out[uint64_t(py) * V.W + px] = r;
     }
     /* warp-aggregated 64-bit sample count */
@@ -477,7 +536,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
  * CTA pops (view, tile) work items from a device queue (one atomic per
  * tile), keeps the current view's constants (and optionally its transfer
  * function) in shared memory, and ray casts tile_w x tile_h pixels. */
-template <int DT, int FILTER, int TF_SHARED>
+template <int DT, int FILTER, int TF_SHARED, int EDGE>
 __global__ void __launch_bounds__(256)
     raycast_persistent_kernel(const RayView* __restrict__ views, TileQueue Q)
 {
@@ -485,6 +544,8 @@ __global__ void __launch_bounds__(256)
     __shared__ uint32_t s_item, s_view;
     extern __shared__ float4 s_tf[];
     const uint32_t total = Q.tile_start[Q.n_views];
+    if (threadIdx.x == 0)
+        atomicCAS(Q.clock, 0ull, globaltimer());
     uint32_t cached = 0xFFFFFFFFu;
     float step = 0.f, ac = 0.f;
     for (;;)
@@ -520,7 +581,7 @@ __global__ void __launch_bounds__(256)
             __syncthreads();
             if (TF_SHARED)
             {
-                for (uint32_t i = threadIdx.x; i < sV.tfn; i += blockDim.x)
+                for (uint32_t i = threadIdx.x; i < 2u * sV.tfn; i += blockDim.x)
                     s_tf[i] = sV.tf[i];
                 __syncthreads();
                 if (threadIdx.x == 0)
@@ -540,7 +601,7 @@ __global__ void __launch_bounds__(256)
         if (px < sV.W && py < sV.H && threadIdx.x < Q.tile_w * Q.tile_h)
         {
             const RayGeom g = ray_setup(sV, px, py);
-            const float4 r = march<DT, FILTER, TF_SHARED>(sV, g, step, ac, nsamp);
+            const float4 r = march<DT, FILTER, TF_SHARED, EDGE>(sV, g, step, ac, nsamp);
             sV.out[uint64_t(py) * sV.W + px] = r;
         }
         unsigned long long sum = nsamp;
@@ -551,6 +612,8 @@ __global__ void __launch_bounds__(256)
             atomicAdd(reinterpret_cast<unsigned long long*>(sV.counters + FC_SAMPLES_LO), sum);
         __syncthreads();
     }
+    if (threadIdx.x == 0)
+        atomicMax(Q.clock + 1, globaltimer());
 }
 
 __global__ void to_rgba8_kernel(const float4* __restrict__ in,
@@ -589,25 +652,75 @@ lv_status launch_leaf_fill(lv_ctx* ctx, const ResolveView& R, cudaStream_t s)
     return LV_OK;
 }
 
+namespace
+{
+/* One instantiation per (voxel type, filter, TF staging, edge clamping). */
+template <int DT, int F, int TFS, int EDGE>
+lv_status persistent_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
+                              uint32_t grid, size_t smem, cudaStream_t s)
+{
+    auto k = raycast_persistent_kernel<DT, F, TFS, EDGE>;
+    if (smem > 48 * 1024)
+        LV_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          int(smem)));
+    k<<<grid, Q.tile_w * Q.tile_h, smem, s>>>(d_rays, Q);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+template <int DT, int F, int EDGE>
+lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, dim3 grid, dim3 block, cudaStream_t s)
+{
+    raycast_kernel<DT, F, EDGE><<<grid, block, 0, s>>>(V);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+/* combination index: dtype (u8 0 / u16 1), filter, edge */
+template <int TFS>
+lv_status persistent_by_index(int idx, lv_ctx* ctx, const RayView* d, const TileQueue& Q,
+                              uint32_t grid, size_t smem, cudaStream_t s)
+{
+    switch (idx)
+    {
+    case 0: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 0>(ctx, d, Q, grid, smem, s);
+    case 1: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 1>(ctx, d, Q, grid, smem, s);
+    case 2: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 0>(ctx, d, Q, grid, smem, s);
+    case 3: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 1>(ctx, d, Q, grid, smem, s);
+    case 4: return persistent_dispatch<LV_DT_UINT16, 0, TFS, 0>(ctx, d, Q, grid, smem, s);
+    case 5: return persistent_dispatch<LV_DT_UINT16, 0, TFS, 1>(ctx, d, Q, grid, smem, s);
+    case 6: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 0>(ctx, d, Q, grid, smem, s);
+    default: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 1>(ctx, d, Q, grid, smem, s);
+    }
+}
+} // namespace
+
+int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge)
+{
+    return (dtype == LV_DT_UINT16 ? 4 : 0) + (filter == LV_FILTER_TRILINEAR ? 2 : 0) +
+           (edge ? 1 : 0);
+}
+
 lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
 {
+    if (V.dtype != LV_DT_UINT8 && V.dtype != LV_DT_UINT16)
+        return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
     step_kernel<<<1, 1, 0, s>>>(V.counters, V.samples_fixed, V.step_policy,
                                 V.max_voxel_dim, V.depth);
     LV_CUDA(ctx, cudaGetLastError());
-    const dim3 block(16, 8);
+    const dim3 block(8, 16);
     const dim3 grid((V.W + block.x - 1) / block.x, (V.H + block.y - 1) / block.y);
-    if (V.dtype == LV_DT_UINT8 && V.filter == LV_FILTER_TRILINEAR)
-        raycast_kernel<LV_DT_UINT8, LV_FILTER_TRILINEAR><<<grid, block, 0, s>>>(V);
-    else if (V.dtype == LV_DT_UINT8)
-        raycast_kernel<LV_DT_UINT8, LV_FILTER_NEAREST><<<grid, block, 0, s>>>(V);
-    else if (V.dtype == LV_DT_UINT16 && V.filter == LV_FILTER_TRILINEAR)
-        raycast_kernel<LV_DT_UINT16, LV_FILTER_TRILINEAR><<<grid, block, 0, s>>>(V);
-    else if (V.dtype == LV_DT_UINT16)
-        raycast_kernel<LV_DT_UINT16, LV_FILTER_NEAREST><<<grid, block, 0, s>>>(V);
-    else
-        return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
-    LV_CUDA(ctx, cudaGetLastError());
-    return LV_OK;
+    switch (kernel_variant(V.dtype, V.filter, V.edge))
+    {
+    case 0: return plain_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, grid, block, s);
+    case 1: return plain_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, grid, block, s);
+    case 2: return plain_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, grid, block, s);
+    case 3: return plain_dispatch<LV_DT_UINT8, 1, 1>(ctx, V, grid, block, s);
+    case 4: return plain_dispatch<LV_DT_UINT16, 0, 0>(ctx, V, grid, block, s);
+    case 5: return plain_dispatch<LV_DT_UINT16, 0, 1>(ctx, V, grid, block, s);
+    case 6: return plain_dispatch<LV_DT_UINT16, 1, 0>(ctx, V, grid, block, s);
+    default: return plain_dispatch<LV_DT_UINT16, 1, 1>(ctx, V, grid, block, s);
+    }
 }
 
 lv_status launch_views_pipeline(lv_ctx* ctx, const ResolveView* d_resolve,
@@ -621,44 +734,17 @@ lv_status launch_views_pipeline(lv_ctx* ctx, const ResolveView* d_resolve,
     return LV_OK;
 }
 
-namespace
-{
-template <int DT, int F, int TFS>
-lv_status persistent_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
-                              uint32_t grid, size_t smem, cudaStream_t s)
-{
-    auto k = raycast_persistent_kernel<DT, F, TFS>;
-    if (smem > 48 * 1024)
-        LV_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          int(smem)));
-    k<<<grid, Q.tile_w * Q.tile_h, smem, s>>>(d_rays, Q);
-    LV_CUDA(ctx, cudaGetLastError());
-    return LV_OK;
-}
-} // namespace
-
-lv_status launch_persistent(lv_ctx* ctx, int dtype, int filter, int tf_shared,
-                            const RayView* d_rays, const TileQueue& Q, uint32_t ctas,
-                            uint32_t tfn_max, cudaStream_t s)
+lv_status launch_persistent(lv_ctx* ctx, int variant, int tf_shared, const RayView* d_rays,
+                            const TileQueue& Q, uint32_t ctas, uint32_t tfn_max,
+                            cudaStream_t s)
 {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     const uint32_t grid = uint32_t(sms) * ctas;
-    const size_t smem = tf_shared ? size_t(tfn_max) * sizeof(float4) : 0;
-    const bool u16 = dtype == LV_DT_UINT16, tri = filter == LV_FILTER_TRILINEAR;
+    const size_t smem = tf_shared ? size_t(tfn_max) * 2 * sizeof(float4) : 0;
     if (tf_shared)
-    {
-        if (u16)
-            return tri ? persistent_dispatch<LV_DT_UINT16, 1, 1>(ctx, d_rays, Q, grid, smem, s)
-                       : persistent_dispatch<LV_DT_UINT16, 0, 1>(ctx, d_rays, Q, grid, smem, s);
-        return tri ? persistent_dispatch<LV_DT_UINT8, 1, 1>(ctx, d_rays, Q, grid, smem, s)
-                   : persistent_dispatch<LV_DT_UINT8, 0, 1>(ctx, d_rays, Q, grid, smem, s);
-    }
-    if (u16)
-        return tri ? persistent_dispatch<LV_DT_UINT16, 1, 0>(ctx, d_rays, Q, grid, smem, s)
-                   : persistent_dispatch<LV_DT_UINT16, 0, 0>(ctx, d_rays, Q, grid, smem, s);
-    return tri ? persistent_dispatch<LV_DT_UINT8, 1, 0>(ctx, d_rays, Q, grid, smem, s)
-               : persistent_dispatch<LV_DT_UINT8, 0, 0>(ctx, d_rays, Q, grid, smem, s);
+        return persistent_by_index<1>(variant, ctx, d_rays, Q, grid, smem, s);
+    return persistent_by_index<0>(variant, ctx, d_rays, Q, grid, smem, s);
 }
 
 } // namespace lv

@@ -407,6 +407,68 @@ void drop_volume_residency(lv_ctx* ctx, lv_volume* v)
     }
 }
 
+lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
+                        const lv_render_desc& desc, const lv_lod_params& lod, float* d_rgba,
+                        uint32_t* leaf, uint32_t* counters, RayView& V)
+{
+    const lv_volume_info& info = vol->info;
+    if (info.dtype != LV_DT_UINT8 && info.dtype != LV_DT_UINT16)
+        return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
+    std::memset(&V, 0, sizeof(V));
+    float lim[6], planes[6][4], eye[3], dir[3];
+    bool ok = false;
+    frustum_setup(desc.camera.modelview, desc.camera.projection, V.inv_mv, V.inv_p, lim,
+                  planes, eye, dir, &ok);
+    if (!ok)
+        return fail(ctx, LV_EINVAL, "singular camera");
+    const uint32_t Lf = info.depth - 1u;
+    uint32_t dims[3];
+    for (int a = 0; a < 3; ++a)
+        dims[a] = info.root_blocks[a] << Lf;
+    const uint32_t bm = std::max(dims[0], std::max(dims[1], dims[2]));
+    V.edge = 0;
+    for (int a = 0; a < 3; ++a)
+    {
+        V.eye[a] = eye[a];
+        const float half = info.world_size[a] / 2.0f;
+        V.gmin[a] = -half;
+        V.gmax[a] = half;
+        V.gscale[a] = float(bm) / info.world_size[a];
+        V.goff[a] = half * V.gscale[a];
+        V.dims[a] = dims[a];
+        V.N[a] = info.max_block[a];
+        V.O[a] = info.overlap[a];
+        V.B[a] = info.max_block[a] - 2u * info.overlap[a];
+        if (info.overlap[a] == 0 || V.N[a] < 2)
+            V.edge = 1;
+    }
+    V.nearp = lim[4];
+    V.n_clip = lod.n_clip_planes;
+    std::memcpy(V.clip, lod.clip_planes, sizeof(V.clip));
+    V.Lf = Lf;
+    V.dtype = info.dtype;
+    V.filter = desc.filter == LV_FILTER_TRILINEAR ? LV_FILTER_TRILINEAR : LV_FILTER_NEAREST;
+    float lo = desc.data_range[0], hi = desc.data_range[1];
+    if (!(hi > lo))
+        type_range(info.dtype, lo, hi);
+    V.dmul = 1.0f / (hi - lo);
+    V.dadd = -lo / (hi - lo);
+    V.early = desc.early_exit;
+    V.W = desc.width;
+    V.H = desc.height;
+    V.samples_fixed = desc.samples_per_ray;
+    V.step_policy = desc.step_policy;
+    V.max_voxel_dim = std::max(info.voxels[0], std::max(info.voxels[1], info.voxels[2]));
+    V.depth = info.depth;
+    V.leaf = leaf;
+    V.pool = ctx->pool->arena.as<uint8_t>();
+    V.tf = tf->rgba.as<float4>();
+    V.tfn = tf->n;
+    V.out = reinterpret_cast<float4*>(d_rgba);
+    V.counters = counters;
+    return LV_OK;
+}
+
 } // namespace lv
 
 /* ================================================================ C ABI */
@@ -751,12 +813,22 @@ extern "C" lv_status lv_tf_create(lv_ctx* ctx, const float* rgba, uint32_t n,
     if (!ctx || !rgba || !out || n == 0)
         return fail(ctx, LV_EINVAL, "empty transfer function");
     LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    /* device layout: (value_i, value_{i+1} - value_i) pairs, last difference 0 */
+    std::vector<float> pairs(size_t(8) * n);
+    for (uint32_t i = 0; i < n; ++i)
+        for (int c = 0; c < 4; ++c)
+        {
+            const float v = rgba[size_t(4) * i + c];
+            const float nx = i + 1 < n ? rgba[size_t(4) * (i + 1) + c] : v;
+            pairs[size_t(8) * i + c] = v;
+            pairs[size_t(8) * i + 4 + c] = nx - v;
+        }
     lv_tf* tf = new lv_tf();
     tf->ctx = ctx;
     tf->n = n;
-    if (tf->rgba.reserve(sizeof(float) * 4 * n) != cudaSuccess ||
-        cudaMemcpy(tf->rgba.ptr, rgba, sizeof(float) * 4 * n, cudaMemcpyHostToDevice) !=
-            cudaSuccess)
+    if (tf->rgba.reserve(sizeof(float) * pairs.size()) != cudaSuccess ||
+        cudaMemcpy(tf->rgba.ptr, pairs.data(), sizeof(float) * pairs.size(),
+                   cudaMemcpyHostToDevice) != cudaSuccess)
     {
         delete tf;
         return fail(ctx, LV_ENOMEM, "transfer function upload");
@@ -962,50 +1034,10 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
 
     /* 4. ray cast */
     RayView V;
-    std::memset(&V, 0, sizeof(V));
-    float lim[6], planes[6][4], eye[3], dir[3];
-    bool ok = false;
-    frustum_setup(desc->camera.modelview, desc->camera.projection, V.inv_mv, V.inv_p,
-                  lim, planes, eye, dir, &ok);
-    if (!ok)
-        return fail(ctx, LV_EINVAL, "singular camera");
-    const uint32_t bm = std::max(dims[0], std::max(dims[1], dims[2]));
-    for (int a = 0; a < 3; ++a)
-    {
-        V.eye[a] = eye[a];
-        const float half = info.world_size[a] / 2.0f;
-        V.gmin[a] = -half;
-        V.gmax[a] = half;
-        V.gscale[a] = float(bm) / info.world_size[a];
-        V.dims[a] = dims[a];
-        V.N[a] = info.max_block[a];
-        V.O[a] = info.overlap[a];
-        V.B[a] = info.max_block[a] - 2u * info.overlap[a];
-    }
-    V.nearp = lim[4];
-    V.n_clip = lod.n_clip_planes;
-    std::memcpy(V.clip, lod.clip_planes, sizeof(V.clip));
-    V.Lf = Lf;
-    V.dtype = info.dtype;
-    V.filter = desc->filter;
-    float lo = desc->data_range[0], hi = desc->data_range[1];
-    if (!(hi > lo))
-        type_range(info.dtype, lo, hi);
-    V.dmul = 1.0f / (hi - lo);
-    V.dadd = -lo / (hi - lo);
-    V.early = desc->early_exit;
-    V.W = desc->width;
-    V.H = desc->height;
-    V.samples_fixed = desc->samples_per_ray;
-    V.step_policy = desc->step_policy;
-    V.max_voxel_dim = std::max(info.voxels[0], std::max(info.voxels[1], info.voxels[2]));
-    V.depth = info.depth;
-    V.leaf = R.leaf.as<uint32_t>();
-    V.pool = ctx->pool->arena.as<uint8_t>();
-    V.tf = tf->rgba.as<float4>();
-    V.tfn = tf->n;
-    V.out = reinterpret_cast<float4*>(d_rgba);
-    V.counters = R.counters.as<uint32_t>();
+    st = make_ray_view(ctx, vol, tf, *desc, lod, d_rgba, R.leaf.as<uint32_t>(),
+                       R.counters.as<uint32_t>(), V);
+    if (st != LV_OK)
+        return st;
     LV_CUDA(ctx, cudaEventRecord(R.t_ray0, s));
     st = launch_raycast(ctx, V, s);
     if (st != LV_OK)
@@ -1056,8 +1088,12 @@ extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)
     s.samples_per_ray = hc[FC_SAMPLES_PER_RAY];
     s.n_samples = uint64_t(hc[FC_SAMPLES_LO]) | (uint64_t(hc[FC_SAMPLES_HI]) << 32);
     s.n_launches = R.launches;
-    cudaEventElapsedTime(&s.select_ms, R.t_sel0, R.t_sel1);
-    cudaEventElapsedTime(&s.raycast_ms, R.t_ray0, R.t_ray1);
+    if (cudaEventElapsedTime(&s.select_ms, R.t_sel0, R.t_sel1) != cudaSuccess ||
+        cudaEventElapsedTime(&s.raycast_ms, R.t_ray0, R.t_ray1) != cudaSuccess)
+    {
+        cudaGetLastError(); /* do not leave the error for the next launch check */
+        s.select_ms = s.raycast_ms = 0.f;
+    }
     *out = s;
     if (hc[FC_ERROR])
         return fail(ctx, LV_ENOMEM, "rendering set overflowed its buffer");

@@ -2,7 +2,8 @@
  * Livre hot-path oracle (CPU restatement). TEST INFRASTRUCTURE ONLY: the
  * product never links or calls it. Built with -ffp-contract=off so every
  * float expression below is a sequence of single IEEE round-to-nearest
- * operations in source order.
+ * operations in source order; where the kernel uses a fused multiply-add the
+ * oracle calls std::fmaf (correctly rounded) at the same point.
  *
  * Reference files restated (paths inside the BlueBrain/Livre project):
  *  - livre/data/NodeId.cpp:23-163, livre/data/types.h:80-93
@@ -349,6 +350,37 @@ struct RenderSet
             return double(reinterpret_cast<const uint16_t*>(bricks)
                               [brick * brickVoxels + i]);
         return double(bricks[brick * brickVoxels + i]);
+    }
+
+    /* Per-ray mode: s = FP32 slot coordinate (nearest: the local position;
+     * trilinear: local position - 0.5, texel centres on integers), computed
+     * with the same FMA chain as the kernel; taps clamp to the brick
+     * (GL_CLAMP_TO_EDGE) and the weights are evaluated in double. */
+    double sample_f(uint32_t brick, const float s[3], uint32_t filter) const
+    {
+        if (filter == 0)
+            return voxel(brick, int(std::floor(s[0])), int(std::floor(s[1])),
+                         int(std::floor(s[2])));
+        double f[3];
+        int i0[3];
+        for (int a = 0; a < 3; ++a)
+        {
+            const float fl = std::floor(s[a]);
+            i0[a] = int(fl);
+            f[a] = double(s[a] - fl);
+        }
+        double c[2][2][2];
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx)
+                    c[dz][dy][dx] = voxel(brick, i0[0] + dx, i0[1] + dy, i0[2] + dz);
+        double cy[2][2], cz[2];
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                cy[dz][dy] = c[dz][dy][0] + (c[dz][dy][1] - c[dz][dy][0]) * f[0];
+        for (int dz = 0; dz < 2; ++dz)
+            cz[dz] = cy[dz][0] + (cy[dz][1] - cy[dz][0]) * f[1];
+        return cz[0] + (cz[1] - cz[0]) * f[2];
     }
 
     /* sv: continuous voxel coordinate inside the slot (texel centres at +0.5) */
@@ -822,7 +854,7 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
     sh.ac = double(view->alpha_correction);
     sh.early = double(view->early_exit);
 
-    float gmin[3], gmax[3], gscale[3];
+    float gmin[3], gmax[3], gscale[3], goff[3];
     uint32_t bm = std::max(rs.dims[0], std::max(rs.dims[1], rs.dims[2]));
     for (int a = 0; a < 3; ++a)
     {
@@ -830,6 +862,7 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
         gmin[a] = -half;
         gmax[a] = half;
         gscale[a] = float(bm) / vol->world_size[a];
+        goff[a] = half * gscale[a];
     }
     const float step = 1.0f / float(view->n_samples);
     const uint32_t W = view->width, H = view->height;
@@ -885,9 +918,11 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
         int64_t k = 0;
         if (tlo > tg)
             k = int64_t(std::ceil((tlo - tg) / step));
+        const float half_texel = view->filter ? 0.5f : 0.0f;
         for (;; ++k)
         {
-            const float t = tg + float(k) * step;
+            /* single-rounding fused multiply-adds, as the kernel */
+            const float t = std::fmaf(float(k), step, tg);
             if (!(t < thi))
                 break;
             float f[3];
@@ -895,8 +930,8 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
             bool inside = true;
             for (int a = 0; a < 3; ++a)
             {
-                const float p = r.eye[a] + r.dir[a] * t;
-                f[a] = (p - gmin[a]) * gscale[a];
+                const float p = std::fmaf(r.dir[a], t, r.eye[a]);
+                f[a] = std::fmaf(p, gscale[a], goff[a]);
                 const float fl = std::floor(f[a]);
                 if (!(fl >= 0.0f) || !(fl < float(rs.dims[a])))
                     inside = false;
@@ -912,15 +947,15 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
             const uint32_t L = nid_level(id);
             const uint32_t shf = rs.Lf - L;
             const uint32_t P[3] = {nid_x(id), nid_y(id), nid_z(id)};
-            double sv[3];
+            float sc[3];
             for (int a = 0; a < 3; ++a)
             {
                 const float vs = float(rs.B[a]) / float(1u << shf);
-                const float v = f[a] * vs;
-                const float local = v - float(P[a] * rs.B[a]) + float(rs.O[a]);
-                sv[a] = double(local);
+                const float off =
+                    (float(rs.O[a]) - float(P[a] * rs.B[a])) - half_texel;
+                sc[a] = std::fmaf(f[a], vs, off);
             }
-            const double val = rs.sample(uint32_t(e), sv, view->filter);
+            const double val = rs.sample_f(uint32_t(e), sc, view->filter);
             const double dens = val * sh.mul + sh.add;
             double src[4];
             sh.tf_lookup(dens, src);
