@@ -55,6 +55,10 @@ def parse():
     p.add_argument("--cpu-rows", type=int, default=12)
     p.add_argument("--pool-gib", type=int, default=None,
                    help="brick pool size (default: the config's)")
+    p.add_argument("--modes", default="plain,batched,served",
+                   help="comma list: plain (headline), batched (64 uneven views in one "
+                        "persistent launch), served (Poisson request stream)")
+    p.add_argument("--serve-seconds", type=float, default=1.5)
     return p.parse_args()
 
 
@@ -177,6 +181,167 @@ def reference_arm(args, cfg):
             "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------- batched / served modes
+BATCH_VIEWPORTS = [(256, 256), (512, 512), (1024, 768), (1920, 1080), (2048, 2048)]
+
+
+def batched_mode(ctx, args, dev, seed=7):
+    """64 views of uneven viewports over 4 resident volumes: plain per-view
+    lv_render launches vs one lv_batch_render (persistent kernel, CUDA graph,
+    autotuned tiles)."""
+    import numpy as np
+    import torch
+    import livre_gb300 as lv
+    rng = np.random.default_rng(seed)
+    specs = [(512, lv.DT_UINT8, 64), (1024, lv.DT_UINT8, 160), (2048, lv.DT_UINT8, 512),
+             (1024, lv.DT_UINT16, 128)]
+    vols = []
+    for k, (n, dt, blobs) in enumerate(specs):
+        vi = lv.VolumeInformation(n, 64, 1, dtype=dt)
+        vols.append((ctx.blob_volume(vi, blobs, 100 + k, noise=4), vi))
+    tfs = [ctx.transfer_function(lv.gaussian_peaks_tf(256, seed=s_)) for s_ in range(4)]
+    items = []
+    for i in range(64):
+        v, vi = vols[i % 4]
+        W, H = BATCH_VIEWPORTS[int(rng.integers(0, len(BATCH_VIEWPORTS)))]
+        mv, proj = lv.orbit_camera(int(rng.integers(0, 64)), 64, vi.world_size, W, H,
+                                   radius_scale=float(rng.uniform(1.2, 2.5)))
+        desc = ctx.render_desc(mv, proj, W, H, sse=float(rng.uniform(0.5, 4.0)),
+                               early_exit=0.99, step_policy=lv.STEP_HALF_VOXEL)
+        out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+        items.append((v, tfs[i % 4], desc, out))
+    for v, t, d, o in items:  # residency: every brick of every view
+        ctx.render(v, t, d, o)
+    ctx.last_stats()
+    # plain: one lv_render per view
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * len(items))]
+    reps = max(2, args.steps // 16)
+    plain_ms = []
+    for r in range(reps + 1):
+        for i, (v, t, d, o) in enumerate(items):
+            ev[2 * i].record()
+            ctx.render(v, t, d, o)
+            ev[2 * i + 1].record()
+        torch.cuda.synchronize()
+        if r:
+            plain_ms.extend(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(len(items)))
+    plain_ms = np.array(plain_ms)
+    # batched: autotune, then graph replays
+    batch = lv.Batch(ctx)
+    t0 = time.time()
+    cfg = batch.autotune(items, reps=2)
+    tune_s = time.time() - t0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    batch_ms, ray_ms = [], []
+    for r in range(args.warmup + reps * 4):
+        e0.record()
+        batch.render(items)
+        e1.record()
+        stats, total, ray = batch.stats(len(items))
+        if r >= args.warmup:
+            batch_ms.append(e0.elapsed_time(e1))
+            ray_ms.append(ray)
+    batch_ms = np.array(batch_ms)
+    n = len(items)
+    samples = float(sum(st["n_samples"] for st in stats))
+    pixels = float(sum(d.width * d.height for _, _, d, _ in items))
+    out = {"views": n, "volumes": "512^3 u8, 1024^3 u8, 2048^3 u8, 1024^3 u16 (64^3 bricks)",
+           "plain": {"frames_per_s": 1000.0 * len(plain_ms) / plain_ms.sum(),
+                     "p50_ms": float(np.percentile(plain_ms, 50)),
+                     "p99_ms": float(np.percentile(plain_ms, 99))},
+           "batched": {"frames_per_s": 1000.0 * n / batch_ms.mean(),
+                       "batch_ms_p50": float(np.percentile(batch_ms, 50)),
+                       "batch_ms_p99": float(np.percentile(batch_ms, 99)),
+                       "raycast_ms_mean": float(np.mean(ray_ms)),
+                       "samples_per_batch": samples, "pixels_per_batch": pixels,
+                       "autotuned": cfg, "autotune_s": tune_s,
+                       "gpu_launches_per_batch": int(stats[0]["n_launches"])}}
+    out["speedup_frames_per_s"] = out["batched"]["frames_per_s"] / out["plain"]["frames_per_s"]
+    batch.close()
+    for v, _ in vols:
+        v.close()
+    for t in tfs:
+        t.close()
+    return out
+
+
+def served_mode(ctx, args, dev, seed=11):
+    """Poisson request streams over 8 resident volumes: continuous-batching
+    server vs the plain per-request server, p50/p99 latency and frames/s."""
+    import numpy as np
+    import torch
+    import livre_gb300 as lv
+    rng = np.random.default_rng(seed)
+    specs = [(256, lv.DT_UINT8), (512, lv.DT_UINT8), (512, lv.DT_UINT16), (1024, lv.DT_UINT8),
+             (1024, lv.DT_UINT16), (2048, lv.DT_UINT8), (2048, lv.DT_UINT16), (4096, lv.DT_UINT8)]
+    vols = []
+    for k, (n, dt) in enumerate(specs):
+        vi = lv.VolumeInformation(n, 64, 1, dtype=dt)
+        vols.append((ctx.blob_volume(vi, int(rng.integers(64, 513)), 300 + k, noise=4), vi))
+    tfs = [ctx.transfer_function(lv.gaussian_peaks_tf(256, seed=100 + k)) for k in range(16)]
+    viewports = [(512, 512), (1920, 1080), (3840, 2160)]
+
+    def make_request():
+        v, vi = vols[int(rng.integers(0, len(vols)))]
+        W, H = viewports[int(rng.integers(0, 3))]
+        mv, proj = lv.orbit_camera(int(rng.integers(0, 256)), 256, vi.world_size, W, H,
+                                   radius_scale=float(rng.uniform(1.2, 2.5)))
+        d = ctx.render_desc(mv, proj, W, H, sse=float(rng.uniform(0.5, 4.0)), early_exit=0.99)
+        return v, tfs[int(rng.integers(0, 16))], d
+
+    # Output frames: a ring of 8 buffers per viewport size (timing only; the
+    # images of requests sharing a buffer are not inspected here, the server
+    # tests check each result against lv_render).
+    rings, ring_pos = {}, {}
+
+    def take(W, H):
+        ring = rings.setdefault((W, H), [torch.empty((H, W, 4), dtype=torch.float32,
+                                                     device=dev) for _ in range(8)])
+        k = ring_pos.get((W, H), 0)
+        ring_pos[(W, H)] = (k + 1) % len(ring)
+        return ring[k]
+
+    def run(mode, rate, reqs):
+        srv = lv.Server(ctx, mode=mode, max_batch=64)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+        tickets, outs = [], []
+        t0 = time.perf_counter()
+        for (v, t, d), at in zip(reqs, arrivals):
+            now = time.perf_counter() - t0
+            if at > now:
+                time.sleep(at - now)
+            o = take(d.width, d.height)
+            tickets.append(srv.submit(v, t, d, o))
+            outs.append(o)
+        res = [srv.wait(tk, 600000) for tk in tickets]
+        wall = time.perf_counter() - t0
+        srv.close()
+        lat = np.array([r["latency_ms"] for r in res])
+        return {"rate_req_s": rate, "requests": len(reqs),
+                "frames_per_s": len(reqs) / wall, "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)),
+                "mean_batch": float(np.mean([r["batch_size"] for r in res])),
+                "failed": int(sum(r["status"] != 0 for r in res))}
+
+    # residency warm-up: one pass of requests through the plain path
+    warm = [make_request() for _ in range(64)]
+    for v, t, d in warm:
+        ctx.render(v, t, d, take(d.width, d.height))
+    ctx.last_stats()
+    out = {"volumes": "8 blob volumes 256^3..4096^3 u8/u16, 64^3 bricks",
+           "pool_gib": args.pool_gib or 96, "rates": []}
+    for rate in (200, 500, 1000, 2000):
+        reqs = [make_request() for _ in range(max(64, int(rate * args.serve_seconds)))]
+        served = run(0, rate, reqs)
+        plain = run(1, rate, reqs)
+        out["rates"].append({"served": served, "plain": plain})
+    for v, _ in vols:
+        v.close()
+    for t in tfs:
+        t.close()
+    return out
 
 
 # ------------------------------------------------------------ GPU arm
@@ -316,6 +481,15 @@ def gb300_arm(args, cfg):
         "visible_bricks_mean": float(np.mean([s["n_visible"] for s in stats])),
         "samples_per_ray": int(stats[-1]["samples_per_ray"]),
     }
+    modes = set(args.modes.split(","))
+    if "batched" in modes:
+        bctx = lv.Context(local, pool_bytes=32 << 30)
+        line["batched"] = batched_mode(bctx, args, dev)
+        bctx.close()
+    if "served" in modes:
+        sctx = lv.Context(local, pool_bytes=96 << 30)
+        line["served"] = served_mode(sctx, args, dev)
+        sctx.close()
     if world == 1 and not args.no_cpu_baseline:
         sec, t_lod, t_rows = cpu_frame_estimate(cfg, k=0, rows=args.cpu_rows)
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "frames/s", "cores": os.cpu_count(),

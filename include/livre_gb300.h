@@ -317,6 +317,65 @@ lv_status lv_batch_autotune(lv_batch* batch, const lv_batch_view* views,
                             uint32_t n, void* stream, uint32_t reps,
                             lv_batch_config* chosen);
 
+/* -------------------------------------------------------------- serving */
+
+typedef struct lv_server lv_server;
+
+enum
+{
+    LV_SERVE_BATCHED = 0, /* continuous batching through lv_batch_render */
+    LV_SERVE_PLAIN = 1    /* one lv_render per request, in arrival order */
+};
+
+typedef struct lv_server_config
+{
+    uint32_t mode;        /* LV_SERVE_BATCHED or LV_SERVE_PLAIN */
+    uint32_t max_batch;   /* requests per launch */
+    uint32_t max_queue;   /* submit returns LV_EAGAIN beyond this (0 = no limit) */
+    uint32_t use_graph;   /* replay batches as CUDA graphs */
+    uint32_t tile_w, tile_h, ctas_per_sm; /* 0 = batch defaults */
+} lv_server_config;
+
+/* One render request: the output buffer (width*height RGBA32F, device) must
+ * stay valid until lv_server_wait returns for it. */
+typedef struct lv_request
+{
+    lv_volume* volume;
+    lv_tf* tf;
+    lv_render_desc desc;
+    float* d_rgba;
+} lv_request;
+
+typedef struct lv_request_result
+{
+    uint32_t status;    /* lv_status of the request */
+    uint32_t batch_size;/* requests rendered in the same launch */
+    double latency_ms;  /* submit -> frame complete on the device */
+    double queue_ms;    /* submit -> admitted (bricks resident, pinned) */
+    lv_frame_stats stats;
+} lv_request_result;
+
+/* A render server on ctx with its own thread. Requests are admitted in
+ * arrival order while the brick pool can hold their missing bricks (free
+ * slots plus resident bricks that no admitted request uses), their visible
+ * bricks are pinned until they complete, and admitted requests are rendered
+ * together while the next ones are admitted (continuous batching). Create the
+ * volumes first. No reference counterpart (Livre renders one view per
+ * Equalizer channel). */
+lv_status lv_server_create(lv_ctx* ctx, const lv_server_config* cfg,
+                           lv_server** out);
+/* Queues a request (any thread); `ticket` identifies it for lv_server_wait. */
+lv_status lv_server_submit(lv_server* server, const lv_request* req,
+                           uint64_t* ticket);
+/* Waits up to timeout_ms for a request; LV_ETIMEDOUT if it is not done. On
+ * LV_OK the result is returned and the ticket is released. */
+lv_status lv_server_wait(lv_server* server, uint64_t ticket,
+                         uint32_t timeout_ms, lv_request_result* out);
+lv_status lv_server_counters(lv_server* server, uint64_t* completed,
+                             uint64_t* batches, uint64_t* queued);
+/* Finishes every queued request, then stops the server thread. */
+void lv_server_destroy(lv_server* server);
+
 /* RGBA32F -> RGBA8 (alpha forced to 255 like the framebuffer copy of
  * livre/eq/render/shaders/fragTexCopy.glsl:11-15 onto the RGB window of
  * livre/eq/Window.cpp:122-124), truncating x * 255 after clamping to [0,1]. */

@@ -14,9 +14,12 @@ include/livre_gb300.h (liblivre_gb300.so, built in-tree):
 Device buffers are torch CUDA tensors; torch is only the allocator and
 stream provider. Every computation runs in the native library.
 """
+import atexit
 import ctypes as C
 import dataclasses
 import math
+import sys
+import weakref
 
 import numpy as np
 
@@ -346,6 +349,8 @@ class Volume:
             self.ctx._children.discard(self)
 
     def __del__(self):
+        if sys.is_finalizing():
+            return  # CUDA may already be torn down; the OS reclaims everything
         try:
             self.close()
         except Exception:
@@ -369,8 +374,23 @@ class TransferFunction:
             self.ctx._children.discard(self)
 
     def __del__(self):
+        if sys.is_finalizing():
+            return  # CUDA may already be torn down; the OS reclaims everything
         try:
             self.close()
+        except Exception:
+            pass
+
+
+_live_contexts = weakref.WeakSet()
+
+
+@atexit.register
+def _close_live_contexts():
+    """Destroys contexts still open at exit while the CUDA runtime is alive."""
+    for ctx in list(_live_contexts):
+        try:
+            ctx.close()
         except Exception:
             pass
 
@@ -379,8 +399,8 @@ class Context:
     """One CUDA device; owns the brick pool (lv_ctx)."""
 
     def __init__(self, device=0, pool_bytes=None):
-        import weakref
         self._children = weakref.WeakSet()
+        _live_contexts.add(self)
         self.handle = None
         h = C.c_void_p()
         check(lib().lv_ctx_create(int(device), C.byref(h)))
@@ -399,6 +419,8 @@ class Context:
             self.handle = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return  # CUDA may already be torn down; the OS reclaims everything
         try:
             self.close()
         except Exception:
@@ -525,6 +547,8 @@ class Batch:
             self.ctx._children.discard(self)
 
     def __del__(self):
+        if sys.is_finalizing():
+            return  # CUDA may already be torn down; the OS reclaims everything
         try:
             self.close()
         except Exception:
@@ -569,3 +593,53 @@ class Batch:
         check(lib().lv_batch_autotune(self.handle, arr, len(items), _stream(stream), reps,
                                       C.byref(c)), self.ctx.handle)
         return c.as_dict()
+
+
+class Server:
+    """Render server (lv_server): continuous batching or plain per-request."""
+
+    def __init__(self, ctx, mode=_abi.SERVE_BATCHED, max_batch=32, max_queue=0, use_graph=1,
+                 tile=None, ctas_per_sm=0):
+        self.ctx = ctx
+        tw, th = tile if tile else (0, 0)
+        cfg = _abi.ServerConfig(mode, max_batch, max_queue, use_graph, tw, th, ctas_per_sm)
+        h = C.c_void_p()
+        check(lib().lv_server_create(ctx.handle, C.byref(cfg), C.byref(h)), ctx.handle)
+        self.handle = h
+        ctx._children.add(self)
+        self._outs = {}
+
+    def submit(self, volume, tf, desc, out):
+        r = _abi.Request(volume.handle.value, tf.handle.value, desc, out.data_ptr())
+        t = C.c_uint64()
+        check(lib().lv_server_submit(self.handle, C.byref(r), C.byref(t)), self.ctx.handle)
+        self._outs[t.value] = out
+        return t.value
+
+    def wait(self, ticket, timeout_ms=60000):
+        res = _abi.RequestResult()
+        st = lib().lv_server_wait(self.handle, ticket, timeout_ms, C.byref(res))
+        check(st, self.ctx.handle)
+        self._outs.pop(ticket, None)
+        return {"status": res.status, "batch_size": res.batch_size,
+                "latency_ms": res.latency_ms, "queue_ms": res.queue_ms,
+                "stats": res.stats.as_dict()}
+
+    def counters(self):
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(lib().lv_server_counters(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return {"completed": a.value, "batches": b.value, "queued": c.value}
+
+    def close(self):
+        if self.handle:
+            lib().lv_server_destroy(self.handle)
+            self.handle = None
+            self.ctx._children.discard(self)
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return  # CUDA may already be torn down; the OS reclaims everything
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -79,6 +79,24 @@ class BatchConfig(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("max_batch", C.c_uint32), ("max_queue", C.c_uint32),
+                ("use_graph", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
+                ("ctas_per_sm", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("volume", C.c_void_p), ("tf", C.c_void_p), ("desc", RenderDesc),
+                ("d_rgba", C.c_void_p)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_uint32), ("batch_size", C.c_uint32), ("latency_ms", C.c_double),
+                ("queue_ms", C.c_double), ("stats", FrameStats)]
+
+
+SERVE_BATCHED, SERVE_PLAIN = 0, 1
+
 GET_DATA_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_size_t)
 
 P = C.POINTER
@@ -116,6 +134,12 @@ _SIGNATURES = {
                                  P(C.c_float)]),
     "lv_batch_autotune": (C.c_int, [C.c_void_p, P(BatchView), C.c_uint32, C.c_void_p,
                                     C.c_uint32, P(BatchConfig)]),
+    "lv_server_create": (C.c_int, [C.c_void_p, P(ServerConfig), P(C.c_void_p)]),
+    "lv_server_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_uint64)]),
+    "lv_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, P(RequestResult)]),
+    "lv_server_counters": (C.c_int, [C.c_void_p, P(C.c_uint64), P(C.c_uint64),
+                                     P(C.c_uint64)]),
+    "lv_server_destroy": (None, [C.c_void_p]),
     "lv_frame_to_rgba8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                     C.c_void_p, C.c_void_p]),
 }

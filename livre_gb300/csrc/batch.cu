@@ -62,6 +62,7 @@ struct lv_batch
     uint32_t depth_max = 0;
     lv::DeviceBuffer params, zeroed, leafs, lists;
     lv::PinnedBuffer h_params, h_out;
+    lv::SelectScratch sel; /* own frontier queues: independent of lv_render */
     uint64_t params_bytes = 0;
     uint32_t generation = 0;
     std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t, uint32_t,
@@ -325,7 +326,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     LV_CUDA(ctx, cudaMemcpyAsync(d, b->h_params.ptr, PL.bytes, cudaMemcpyHostToDevice, s));
     LV_CUDA(ctx, cudaMemsetAsync(b->zeroed.ptr, 0, sizeof(uint32_t) * (kOutWords * n + 64), s));
     LV_CUDA(ctx, cudaMemsetAsync(b->leafs.ptr, 0xFF, sizeof(uint32_t) * b->cells_stride * n, s));
-    lv_status st = enqueue_selection(ctx, reinterpret_cast<LodView*>(d + PL.lod), n,
+    lv_status st = enqueue_selection(ctx, b->sel, reinterpret_cast<LodView*>(d + PL.lod), n,
                                      total_roots, b->depth_max, s);
     if (st != LV_OK)
         return st;
@@ -456,7 +457,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     uint64_t frontier = 0;
     for (uint32_t i = 0; i < n; ++i)
         frontier += max_frontier(views[i].volume->info);
-    st = reserve_frontier(ctx, frontier, b->stream);
+    st = reserve_frontier(ctx, b->sel, frontier, b->stream);
     if (st != LV_OK)
         return st;
     b->frame = ++ctx->renderer->frame;
@@ -479,7 +480,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     {
         const auto key = std::make_tuple(n, mask, b->cfg.tile_w, b->cfg.tile_h, b->cfg.ctas_per_sm,
                                          b->cfg.tf_shared ? tfn_max : 0u, b->depth_max,
-                                         b->generation, uintptr_t(ctx->sel.ids[0].ptr));
+                                         b->generation, uintptr_t(b->sel.ids[0].ptr));
         auto it = b->graphs.find(key);
         if (it == b->graphs.end())
         {

@@ -496,15 +496,14 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
     LV_CUDA(ctx, cudaMemcpyAsync(S.views.ptr, S.staging.ptr,
                                  sizeof(LodView) * n_views,
                                  cudaMemcpyHostToDevice, stream));
-    return enqueue_selection(ctx, S.views.as<LodView>(), n_views, total_roots,
+    return enqueue_selection(ctx, S, S.views.as<LodView>(), n_views, total_roots,
                              max_depth, stream);
 }
 
-lv_status enqueue_selection(lv_ctx* ctx, const LodView* dviews, uint32_t n_views,
-                            uint32_t total_roots, uint32_t max_depth,
+lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* dviews,
+                            uint32_t n_views, uint32_t total_roots, uint32_t max_depth,
                             cudaStream_t stream)
 {
-    SelectScratch& S = ctx->sel;
     const uint32_t cap = S.frontier_capacity;
     if (total_roots > cap)
         return fail(ctx, LV_ENOMEM, "root frontier exceeds scratch capacity");
@@ -532,10 +531,9 @@ lv_status enqueue_selection(lv_ctx* ctx, const LodView* dviews, uint32_t n_views
     return LV_OK;
 }
 
-lv_status reserve_frontier(lv_ctx* ctx, uint64_t nodes, cudaStream_t s)
+lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaStream_t s)
 {
     const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(nodes, 64), 1u << 24);
-    SelectScratch& S = ctx->sel;
     if (S.frontier_capacity >= cap)
         return LV_OK;
     LV_CUDA(ctx, cudaStreamSynchronize(s));
@@ -600,7 +598,7 @@ extern "C" lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
     V.out_ids = d_out_ids;
     V.capacity = capacity;
     V.result = d_result;
-    st = reserve_frontier(ctx, max_frontier(*vol), s);
+    st = reserve_frontier(ctx, ctx->sel, max_frontier(*vol), s);
     if (st != LV_OK)
         return st;
     st = run_selection(ctx, &V, 1, vol->depth, s);

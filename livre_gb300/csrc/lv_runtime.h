@@ -159,12 +159,12 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
 
 /* Enqueues the selection kernels for n views whose constants are already
  * on the device (capturable: no host synchronisation). */
-lv_status enqueue_selection(lv_ctx* ctx, const LodView* d_views, uint32_t n_views,
-                            uint32_t total_roots, uint32_t max_depth,
+lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* d_views,
+                            uint32_t n_views, uint32_t total_roots, uint32_t max_depth,
                             cudaStream_t stream);
-/* Grows the frontier queues to hold `nodes` per level (synchronises `s`
+/* Grows the frontier queues of S to hold `nodes` per level (synchronises `s`
  * when it reallocates). */
-lv_status reserve_frontier(lv_ctx* ctx, uint64_t nodes, cudaStream_t s);
+lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaStream_t s);
 
 /* Frontier size needed for a full traversal of a volume. */
 uint64_t max_frontier(const lv_volume_info& vol);
@@ -203,6 +203,8 @@ struct Pool
     std::map<uint32_t, std::vector<uint32_t>> free_by_units;
     std::list<Resident> lru; /* front = oldest load */
     uint64_t resident_bytes = 0;
+    /* per slot size: resident bricks and those pinned by server requests */
+    std::map<uint32_t, uint64_t> resident_count, pinned_count;
 };
 
 struct Renderer
@@ -272,6 +274,9 @@ struct lv_volume
     uint64_t n_nodes = 0;
     lv::DeviceBuffer node_table, node_stamp;
     std::vector<int32_t> host_table;
+    /* host pin counts per node: bricks of admitted, unfinished server
+     * requests are never evicted (empty until a server uses the volume) */
+    std::vector<uint16_t> pins;
     uint32_t time_step = 0;
     /* pinned staging ring for callback sources */
     std::vector<lv::PinnedBuffer*> staging;

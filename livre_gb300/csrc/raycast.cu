@@ -82,9 +82,11 @@ __device__ void resolve_body(const ResolveView& R, uint32_t first, uint32_t stri
             const int32_t ps = R.node_table[pidx];
             if (ps >= 0)
             {
-                R.node_stamp[pidx] = R.frame;
+                /* the exchange comes first: on the single-view path the view
+                 * stamps and the in-use stamps are the same array */
                 if (atomicExch(&R.view_stamp[pidx], R.view_frame) != R.view_frame)
                     emit_render(R, cur, uint32_t(ps));
+                R.node_stamp[pidx] = R.frame;
                 break;
             }
         }

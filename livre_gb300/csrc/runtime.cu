@@ -149,7 +149,7 @@ lv_status ensure_renderer(lv_ctx* ctx)
 lv_status reserve_selection(lv_ctx* ctx, const lv_volume_info& info,
                             cudaStream_t s)
 {
-    return reserve_frontier(ctx, max_frontier(info), s);
+    return reserve_frontier(ctx, ctx->sel, max_frontier(info), s);
 }
 
 /* Frees one slot of `units` for a new brick, evicting the oldest resident
@@ -179,6 +179,19 @@ bool pool_alloc(lv_ctx* ctx, uint32_t units, uint32_t protect_frame,
         if (it->units != units)
             continue;
         lv_volume* v = it->vol;
+        if (protect_frame == 0xFFFFFFFFu)
+        {
+            /* pins alone decide (server requests) */
+            if (!v->pins.empty() && v->pins[it->node_idx] != 0)
+                continue;
+            out_unit = it->unit;
+            v->host_table[it->node_idx] = -1;
+            updates.push_back({v, {it->node_idx, -1}});
+            P.resident_bytes -= uint64_t(units) * kSlotUnit;
+            --P.resident_count[units];
+            P.lru.erase(it);
+            return true;
+        }
         auto st = stamps.find(v);
         if (st == stamps.end())
         {
@@ -189,12 +202,14 @@ bool pool_alloc(lv_ctx* ctx, uint32_t units, uint32_t protect_frame,
             st = stamps.emplace(v, std::move(h)).first;
         }
         const uint32_t stamp = st->second[it->node_idx];
-        if (stamp != 0 && stamp >= protect_frame)
+        if ((stamp != 0 && stamp >= protect_frame) ||
+            (!v->pins.empty() && v->pins[it->node_idx] != 0))
             continue; /* in use: Cache.cpp:148 skips referenced objects */
         out_unit = it->unit;
         v->host_table[it->node_idx] = -1;
         updates.push_back({v, {it->node_idx, -1}});
         P.resident_bytes -= uint64_t(units) * kSlotUnit;
+        --P.resident_count[units];
         P.lru.erase(it);
         return true;
     }
@@ -315,6 +330,7 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
         updates.push_back({vol, {idx, int32_t(unit)}});
         P.lru.push_back(Resident{vol, idx, unit, vol->slot_units});
         P.resident_bytes += uint64_t(vol->slot_units) * kSlotUnit;
+        ++P.resident_count[vol->slot_units];
         ++n_loaded;
     }
     if (!gen_ids.empty())
@@ -400,6 +416,9 @@ void drop_volume_residency(lv_ctx* ctx, lv_volume* v)
         {
             P.free_by_units[it->units].push_back(it->unit);
             P.resident_bytes -= uint64_t(it->units) * kSlotUnit;
+            --P.resident_count[it->units];
+            if (!v->pins.empty() && v->pins[it->node_idx])
+                --P.pinned_count[it->units];
             it = P.lru.erase(it);
         }
         else
@@ -593,6 +612,10 @@ extern "C" lv_status lv_pool_purge(lv_ctx* ctx)
     P.free_by_units.clear();
     P.bump = 0;
     P.resident_bytes = 0;
+    P.resident_count.clear();
+    P.pinned_count.clear();
+    for (lv_volume* v : vols)
+        std::fill(v->pins.begin(), v->pins.end(), uint16_t(0));
     if (ctx->renderer)
         ctx->renderer->pending_vol = nullptr;
     return LV_OK;
