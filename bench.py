@@ -465,6 +465,8 @@ def gb300_arm(args, cfg):
                    "parallelism": "replicas" if world > 1 else "single"},
         "p50_ms": float(np.percentile(frame_ms, 50)), "p99_ms": float(np.percentile(frame_ms, 99)),
         "samples_per_s": float(n_samples.sum() / (total_ms / 1000.0)),
+        "raycast_ms_mean": float(ray_ms.mean()),
+        "select_ms_mean": float(np.mean([s["select_ms"] for s in stats])),
         "wall_s": wall, "volume_generation_s": gen_s,
         "gpu_launches": int(sum(s["n_launches"] for s in stats)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -174,6 +174,19 @@ void lv_volume_destroy(lv_volume* vol);
 /* The derived VolumeInformation of a volume. */
 lv_status lv_volume_get_info(const lv_volume* vol, lv_volume_info* out);
 
+/* A volume opened from a URI by the built-in data sources, like
+ * livre::DataSource(uri) (livre/data/DataSource.cpp:29-63):
+ *   mem://[#w,h,d,block][?datatype=T]   MemoryDataSource (constant bricks)
+ *   raw://f.raw#x,y,z[,T]                RawDataSource (one brick)
+ *   raw://f.nrrd[?output=T]              RawDataSource with an NRRD header
+ * Unknown schemes return LV_EINVAL ("no data source handles ..."). */
+lv_status lv_volume_open(lv_ctx* ctx, const char* uri, lv_volume** out);
+/* DataSource::getData (livre/data/DataSource.cpp:101-111): the brick of
+ * `node_id` into host memory `dst` (at least the brick's bytes); LV_ENOTFOUND
+ * for invalid ids or a source that has no data for the node. */
+lv_status lv_volume_get_data(lv_volume* vol, uint64_t node_id, void* dst,
+                             size_t bytes);
+
 /* Loads the bricks `ids` (host array) of `vol` into the pool now, evicting
  * the oldest resident bricks when it is full, like Cache::load<TextureObject>
  * (livre/core/cache/Cache.cpp:111-123) driven by DataUploadFilter::load
@@ -191,6 +204,18 @@ lv_status lv_volume_resident(const lv_volume* vol, uint64_t* ids,
 lv_status lv_blob_generate(lv_ctx* ctx, const lv_volume_info* info,
                            const lv_blob_desc* blob, const uint64_t* ids,
                            uint32_t n, void* d_out, void* stream);
+
+/* Value histograms of bricks `ids` (host array; loaded into the pool if
+ * missing), replacing HistogramObject (livre/lib/cache/HistogramObject.cpp:
+ * 30-224) and the accumulation of HistogramFilter::execute (livre/lib/
+ * pipeline/HistogramFilter.cpp:78-149) for a full viewport. Only each brick's
+ * own voxels count, weighted by (2^(depth-1-level))^3 finest voxels per voxel;
+ * value v falls in bin floor((v - lo) * (n_bins - 1) / (hi - lo)) clamped to
+ * the bins (bin = v for uint8, 256 bins over [0, 255]). per_brick (nullable):
+ * n * n_bins host words; accumulated: n_bins host words. Synchronous. */
+lv_status lv_histogram(lv_volume* vol, const uint64_t* ids, uint32_t n,
+                       uint32_t n_bins, float range_lo, float range_hi,
+                       uint64_t* per_brick, uint64_t* accumulated);
 
 /* ------------------------------------------------------ transfer function */
 
@@ -248,6 +273,9 @@ typedef struct lv_frame_stats
     uint32_t n_launches;      /* kernels this library launched for the frame */
     float select_ms;          /* device time of the LOD selection */
     float raycast_ms;         /* device time of the ray-cast kernel */
+    uint32_t error_flags;     /* 0, or the device's index-check code: 1 rendering
+                                 set overflow, 2 node outside the octree,
+                                 3 brick outside the pool (the access was skipped) */
 } lv_frame_stats;
 
 /* One frame of one view: LOD selection, brick residency (streaming misses

@@ -132,6 +132,7 @@ class VolumeInformation:
     max_block = property(lambda s: tuple(s.info.max_block))
     overlap = property(lambda s: tuple(s.info.overlap))
     dtype = property(lambda s: s.info.dtype)
+    comp_count = property(lambda s: s.info.comp_count)
 
     @property
     def block_size(self):
@@ -333,6 +334,27 @@ class Volume:
                                    len(ids), C.byref(n)), self.ctx.handle)
         return n.value
 
+    def get_data(self, node_id):
+        """DataSource::getData: the brick's bytes (numpy uint8) or None."""
+        out = np.zeros(self.info.brick_bytes, np.uint8)
+        st = lib().lv_volume_get_data(self.handle, C.c_uint64(int(node_id)),
+                                      out.ctypes.data, out.nbytes)
+        if st == _abi.LV_ENOTFOUND:
+            return None
+        check(st, self.ctx.handle)
+        return out
+
+    def histogram(self, node_ids, n_bins=256, data_range=(0.0, 255.0), per_brick=False):
+        """Accumulated (and optionally per-brick) value histograms of bricks."""
+        ids = np.ascontiguousarray([int(i) for i in node_ids], np.uint64)
+        acc = np.zeros(n_bins, np.uint64)
+        pb = np.zeros((len(ids), n_bins), np.uint64) if per_brick else None
+        check(lib().lv_histogram(self.handle, ids.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                 len(ids), n_bins, float(data_range[0]), float(data_range[1]),
+                                 pb.ctypes.data_as(C.POINTER(C.c_uint64)) if per_brick else None,
+                                 acc.ctypes.data_as(C.POINTER(C.c_uint64))), self.ctx.handle)
+        return (acc, pb) if per_brick else acc
+
     def resident(self):
         """Resident node ids, oldest load first."""
         n = C.c_uint32()
@@ -469,6 +491,16 @@ class Context:
         check(lib().lv_volume_create(self.handle, C.byref(vol_info.info), cfn, None,
                                      C.byref(h)), self.handle)
         return Volume(self, h, vol_info, keepalive=cfn)
+
+    def open_volume(self, uri):
+        """A volume from a data-source URI (mem://, raw://)."""
+        h = C.c_void_p()
+        check(lib().lv_volume_open(self.handle, uri.encode(), C.byref(h)), self.handle)
+        info = _abi.VolumeInfo()
+        check(lib().lv_volume_get_info(h, C.byref(info)))
+        vi = VolumeInformation.__new__(VolumeInformation)
+        vi.info = info
+        return Volume(self, h, vi)
 
     def blob_bricks(self, vol_info, node_ids, n_blobs, seed, noise=0, stream=None):
         """Generated bricks of `node_ids` as a device tensor (n, brick_bytes) uint8."""

@@ -60,7 +60,7 @@ class FrameStats(C.Structure):
                 ("samples_per_ray", C.c_uint32), ("n_uploaded", C.c_uint32),
                 ("n_samples", C.c_uint64), ("bytes_uploaded", C.c_uint64),
                 ("n_launches", C.c_uint32), ("select_ms", C.c_float),
-                ("raycast_ms", C.c_float)]
+                ("raycast_ms", C.c_float), ("error_flags", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -116,6 +116,10 @@ _SIGNATURES = {
                                         P(C.c_void_p)]),
     "lv_volume_destroy": (None, [C.c_void_p]),
     "lv_volume_get_info": (C.c_int, [C.c_void_p, P(VolumeInfo)]),
+    "lv_volume_open": (C.c_int, [C.c_void_p, C.c_char_p, P(C.c_void_p)]),
+    "lv_volume_get_data": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_size_t]),
+    "lv_histogram": (C.c_int, [C.c_void_p, P(C.c_uint64), C.c_uint32, C.c_uint32, C.c_float,
+                               C.c_float, P(C.c_uint64), P(C.c_uint64)]),
     "lv_volume_load": (C.c_int, [C.c_void_p, P(C.c_uint64), C.c_uint32, P(C.c_uint32)]),
     "lv_volume_resident": (C.c_int, [C.c_void_p, P(C.c_uint64), C.c_uint32, P(C.c_uint32)]),
     "lv_blob_generate": (C.c_int, [C.c_void_p, P(VolumeInfo), P(BlobDesc), P(C.c_uint64),

@@ -78,6 +78,7 @@ struct lv_batch
     uint32_t uploaded = 0;
     uint32_t launches = 0;
     uint32_t last_n = 0;
+    uint32_t sel_generation = 0; /* b->sel.generation the cached graphs use */
 
     ~lv_batch()
     {
@@ -118,8 +119,10 @@ ParamLayout param_layout(uint32_t n)
     L.resolve = al(L.lod + sizeof(LodView) * n);
     L.ray = al(L.resolve + sizeof(ResolveView) * n);
     L.tables = al(L.ray + sizeof(RayView) * n);
-    /* kGroups x (view ids n + tile starts n + 1) */
-    L.bytes = al(L.tables + sizeof(uint32_t) * kGroups * (2 * n + 1));
+    /* kGroups x (view ids n + tile starts n + 1), then kGroups view counts
+     * and the total root count: everything that changes between launches of
+     * one captured graph lives in this copied block */
+    L.bytes = al(L.tables + sizeof(uint32_t) * (kGroups * (2 * n + 1) + kGroups + 1));
     return L;
 }
 
@@ -287,6 +290,7 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n,
         R.counters = counters;
         R.leaf = dleaf + S.leaf / 4;
         R.Lf = Lf;
+        R.n_nodes = vol->n_nodes;
 
         RayView& V = rays[i];
         st = make_ray_view(ctx, vol, bv.tf, d, lod, bv.d_rgba, R.leaf, counters, V);
@@ -313,6 +317,10 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n,
         }
         starts[groups[g].views.size()] = acc;
     }
+    uint32_t* counts = tables + stride * kGroups;
+    for (int g = 0; g < kGroups; ++g)
+        counts[g] = uint32_t(groups[g].views.size());
+    counts[kGroups] = total_roots;
     return LV_OK;
 }
 
@@ -326,8 +334,12 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     LV_CUDA(ctx, cudaMemcpyAsync(d, b->h_params.ptr, PL.bytes, cudaMemcpyHostToDevice, s));
     LV_CUDA(ctx, cudaMemsetAsync(b->zeroed.ptr, 0, sizeof(uint32_t) * (kOutWords * n + 64), s));
     LV_CUDA(ctx, cudaMemsetAsync(b->leafs.ptr, 0xFF, sizeof(uint32_t) * b->cells_stride * n, s));
+    const uint32_t* tables = reinterpret_cast<const uint32_t*>(d + PL.tables);
+    const uint32_t stride = 2 * b->views_cap + 1;
+    const uint32_t* group_counts = tables + stride * kGroups;
+    /* the root frontier is sized for every view having all its roots */
     lv_status st = enqueue_selection(ctx, b->sel, reinterpret_cast<LodView*>(d + PL.lod), n,
-                                     total_roots, b->depth_max, s);
+                                     total_roots, b->depth_max, s, group_counts + kGroups);
     if (st != LV_OK)
         return st;
     st = launch_views_pipeline(ctx, reinterpret_cast<ResolveView*>(d + PL.resolve),
@@ -336,8 +348,6 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         return st;
     uint32_t* heads = b->zeroed.as<uint32_t>() + kOutWords * n; /* kGroups words */
     unsigned long long* clock = reinterpret_cast<unsigned long long*>(heads + kGroups);
-    const uint32_t* tables = reinterpret_cast<const uint32_t*>(d + PL.tables);
-    const uint32_t stride = 2 * b->views_cap + 1;
     for (int g = 0; g < kGroups; ++g)
     {
         if (groups[g].views.empty())
@@ -345,7 +355,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         TileQueue Q;
         Q.view_ids = tables + stride * g;
         Q.tile_start = Q.view_ids + b->views_cap;
-        Q.n_views = uint32_t(groups[g].views.size());
+        Q.n_views = group_counts + g;
         Q.tile_w = b->cfg.tile_w;
         Q.tile_h = b->cfg.tile_h;
         Q.head = heads + g;
@@ -460,6 +470,15 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     st = reserve_frontier(ctx, b->sel, frontier, b->stream);
     if (st != LV_OK)
         return st;
+    if (b->sel.generation != b->sel_generation)
+    {
+        /* every buffer a cached graph references must still be the same:
+         * the frontier queues moved, drop the graphs that used them */
+        for (auto& kv : b->graphs)
+            cudaGraphExecDestroy(kv.second);
+        b->graphs.clear();
+        b->sel_generation = b->sel.generation;
+    }
     b->frame = ++ctx->renderer->frame;
     ++b->launch_id;
     std::vector<Group> groups;
@@ -480,7 +499,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     {
         const auto key = std::make_tuple(n, mask, b->cfg.tile_w, b->cfg.tile_h, b->cfg.ctas_per_sm,
                                          b->cfg.tf_shared ? tfn_max : 0u, b->depth_max,
-                                         b->generation, uintptr_t(b->sel.ids[0].ptr));
+                                         b->generation, uintptr_t(b->sel.generation));
         auto it = b->graphs.find(key);
         if (it == b->graphs.end())
         {
@@ -549,6 +568,7 @@ extern "C" lv_status lv_batch_stats(lv_batch* b, lv_frame_stats* out, uint32_t n
         s.max_level = c[FC_MAX_LEVEL] ? c[FC_MAX_LEVEL] - 1u : 0u;
         s.samples_per_ray = c[FC_SAMPLES_PER_RAY];
         s.n_samples = uint64_t(c[FC_SAMPLES_LO]) | (uint64_t(c[FC_SAMPLES_HI]) << 32);
+        s.error_flags = c[FC_ERROR];
         if (i == 0)
         {
             s.n_uploaded = b->uploaded;

@@ -169,8 +169,13 @@ __global__ void lod_roots_kernel(const LodView* __restrict__ views,
                                  uint32_t* __restrict__ view_of,
                                  uint32_t* __restrict__ counts,
                                  uint32_t n_counts, uint32_t total_roots,
-                                 uint32_t capacity)
+                                 uint32_t capacity,
+                                 const uint32_t* __restrict__ d_total_roots)
 {
+    /* d_total_roots (nullable): the count in device memory, for launches
+     * replayed from a CUDA graph with different views */
+    if (d_total_roots)
+        total_roots = *d_total_roots;
     const uint32_t v = blockIdx.x;
     if (v == 0)
     {
@@ -502,7 +507,7 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
 
 lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* dviews,
                             uint32_t n_views, uint32_t total_roots, uint32_t max_depth,
-                            cudaStream_t stream)
+                            cudaStream_t stream, const uint32_t* d_total_roots)
 {
     const uint32_t cap = S.frontier_capacity;
     if (total_roots > cap)
@@ -512,7 +517,7 @@ lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* dviews
     uint32_t* overflow = counts + kMaxLevels + 1;
     lod_roots_kernel<<<n_views, 128, 0, stream>>>(
         dviews, n_views, S.ids[0].as<uint64_t>(), S.view[0].as<uint32_t>(),
-        counts, n_counts, total_roots, cap);
+        counts, n_counts, total_roots, cap, d_total_roots);
     LV_CUDA(ctx, cudaGetLastError());
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -544,6 +549,7 @@ lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaSt
     }
     LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 2)));
     S.frontier_capacity = uint32_t(cap);
+    ++S.generation; /* captured graphs referencing the old queues are stale */
     return LV_OK;
 }
 

@@ -86,6 +86,8 @@ struct RayView
     uint32_t depth;
     const uint32_t* leaf;
     const uint8_t* pool; /* brick = pool + slot * kSlotUnit */
+    uint32_t pool_units;  /* arena size in kSlotUnit units */
+    uint32_t brick_units; /* units one brick of this volume occupies */
     const float4* tf; /* tfn (value, next - value) pairs */
     uint32_t tfn;
     float4* out;
@@ -132,6 +134,7 @@ struct ResolveView
     uint32_t* leaf;           /* leaf grid */
     uint32_t dims[3];
     uint32_t Lf;
+    uint64_t n_nodes;         /* entries of node_table / stamps */
 };
 
 /* Work queue of the persistent ray-cast kernel: the views of one voxel
@@ -140,7 +143,7 @@ struct TileQueue
 {
     const uint32_t* view_ids;   /* n_views entries: index into the RayView array */
     const uint32_t* tile_start; /* n_views + 1 prefix sums */
-    uint32_t n_views;
+    const uint32_t* n_views;    /* device word: views of this group (per launch) */
     uint32_t tile_w, tile_h;
     uint32_t* head;             /* zeroed before the launch */
     unsigned long long* clock;  /* [first CTA start, last CTA end] in ns (%globaltimer) */

@@ -102,6 +102,7 @@ struct SelectScratch
     DeviceBuffer sort;    /* range-slice sort keys/ids */
     PinnedBuffer staging; /* host copy of the LodView array */
     uint32_t frontier_capacity = 0;
+    uint32_t generation = 0; /* bumped whenever the queues are reallocated */
 };
 
 struct Pool;
@@ -161,7 +162,7 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
  * on the device (capturable: no host synchronisation). */
 lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* d_views,
                             uint32_t n_views, uint32_t total_roots, uint32_t max_depth,
-                            cudaStream_t stream);
+                            cudaStream_t stream, const uint32_t* d_total_roots = nullptr);
 /* Grows the frontier queues of S to hold `nodes` per level (synchronises `s`
  * when it reallocates). */
 lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaStream_t s);
@@ -265,6 +266,7 @@ struct lv_volume
     int kind = lv::SRC_CALLBACK;
     lv_get_data_fn fn = nullptr;
     void* user = nullptr;
+    void (*user_free)(void*) = nullptr; /* built-in sources own `user` */
     lv_blob_desc blob{};
     lv::DeviceBuffer d_blobs;
     lv::PinnedBuffer host_store;

@@ -56,7 +56,19 @@ __device__ void resolve_body(const ResolveView& R, uint32_t first, uint32_t stri
     for (uint32_t i = first; i < n; i += stride)
     {
         const uint64_t id = R.visible[i];
+        const uint32_t L = nid_level(id);
+        if (L >= R.depth || nid_x(id) >= (R.root_blocks[0] << L) ||
+            nid_y(id) >= (R.root_blocks[1] << L) || nid_z(id) >= (R.root_blocks[2] << L))
+        {
+            atomicExch(&R.counters[FC_ERROR], 2u); /* id outside this octree */
+            continue;
+        }
         const uint64_t idx = node_index(R.level_offset, R.root_blocks, id);
+        if (idx >= R.n_nodes)
+        {
+            atomicExch(&R.counters[FC_ERROR], 2u);
+            continue;
+        }
         const int32_t slot = R.node_table[idx];
         if (slot >= 0)
         {
@@ -470,6 +482,12 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
         {
             cur = lin;
             entry = __ldg(V.leaf + lin);
+            if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
+                                        (entry >> kLeafSlotBits) > V.Lf))
+            {
+                atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
+                entry = kLeafEmpty;
+            }
             if (entry != kLeafEmpty)
             {
                 const uint32_t L = entry >> kLeafSlotBits;
@@ -545,7 +563,8 @@ __global__ void __launch_bounds__(256)
     __shared__ RayView sV;
     __shared__ uint32_t s_item, s_view;
     extern __shared__ float4 s_tf[];
-    const uint32_t total = Q.tile_start[Q.n_views];
+    const uint32_t n_views = *Q.n_views;
+    const uint32_t total = Q.tile_start[n_views];
     if (threadIdx.x == 0)
         atomicCAS(Q.clock, 0ull, globaltimer());
     uint32_t cached = 0xFFFFFFFFu;
@@ -555,7 +574,7 @@ __global__ void __launch_bounds__(256)
         if (threadIdx.x == 0)
         {
             const uint32_t item = atomicAdd(Q.head, 1u);
-            uint32_t lo = 0, hi = Q.n_views;
+            uint32_t lo = 0, hi = n_views;
             if (item < total)
                 while (hi - lo > 1)
                 {

@@ -481,6 +481,8 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     V.depth = info.depth;
     V.leaf = leaf;
     V.pool = ctx->pool->arena.as<uint8_t>();
+    V.pool_units = uint32_t(ctx->pool->capacity_units);
+    V.brick_units = vol->slot_units;
     V.tf = tf->rgba.as<float4>();
     V.tfn = tf->n;
     V.out = reinterpret_cast<float4*>(d_rgba);
@@ -768,6 +770,8 @@ extern "C" void lv_volume_destroy(lv_volume* v)
         if (ctx->renderer && ctx->renderer->pending_vol == v)
             ctx->renderer->pending_vol = nullptr;
     }
+    if (v->user_free)
+        v->user_free(v->user);
     delete v;
 }
 
@@ -1014,8 +1018,32 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     RV.counters = R.counters.as<uint32_t>();
     RV.leaf = R.leaf.as<uint32_t>();
     RV.Lf = Lf;
-    LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
-    st = launch_resolve(ctx, RV, s);
+    RV.n_nodes = vol->n_nodes;
+    RayView V;
+    st = make_ray_view(ctx, vol, tf, *desc, lod, d_rgba, R.leaf.as<uint32_t>(),
+                       R.counters.as<uint32_t>(), V);
+    if (st != LV_OK)
+        return st;
+    /* residency pass, leaf grid and ray cast, enqueued without a host round
+     * trip; the synchronous mode checks for misses once the frame is done
+     * and, only if some brick was missing, streams it and renders again */
+    auto frame_tail = [&]() -> lv_status {
+        LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
+        lv_status t = launch_resolve(ctx, RV, s);
+        if (t != LV_OK)
+            return t;
+        LV_CUDA(ctx, cudaMemsetAsync(R.leaf.ptr, 0xFF, cells * sizeof(uint32_t), s));
+        t = launch_leaf_fill(ctx, RV, s);
+        if (t != LV_OK)
+            return t;
+        LV_CUDA(ctx, cudaEventRecord(R.t_ray0, s));
+        t = launch_raycast(ctx, V, s);
+        if (t != LV_OK)
+            return t;
+        LV_CUDA(ctx, cudaEventRecord(R.t_ray1, s));
+        return LV_OK;
+    };
+    st = frame_tail();
     if (st != LV_OK)
         return st;
     if (desc->synchronous)
@@ -1039,33 +1067,14 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             R.stats.bytes_uploaded += bytes;
             if (st != LV_OK && st != LV_EAGAIN)
                 return st;
-            /* resolve again with the streamed bricks; what still misses
+            /* render again with the streamed bricks; what still misses
              * (pool too small) is not rendered */
-            LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
-            st = launch_resolve(ctx, RV, s);
+            st = frame_tail();
             if (st != LV_OK)
                 return st;
-            R.launches += 1u;
+            R.launches += 5u;
         }
     }
-
-    /* 3. leaf grid */
-    LV_CUDA(ctx, cudaMemsetAsync(R.leaf.ptr, 0xFF, cells * sizeof(uint32_t), s));
-    st = launch_leaf_fill(ctx, RV, s);
-    if (st != LV_OK)
-        return st;
-
-    /* 4. ray cast */
-    RayView V;
-    st = make_ray_view(ctx, vol, tf, *desc, lod, d_rgba, R.leaf.as<uint32_t>(),
-                       R.counters.as<uint32_t>(), V);
-    if (st != LV_OK)
-        return st;
-    LV_CUDA(ctx, cudaEventRecord(R.t_ray0, s));
-    st = launch_raycast(ctx, V, s);
-    if (st != LV_OK)
-        return st;
-    LV_CUDA(ctx, cudaEventRecord(R.t_ray1, s));
 
     /* 5. copy back counters (+ misses in async mode) */
     uint32_t* hc = R.h_counters.as<uint32_t>();
@@ -1111,6 +1120,7 @@ extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)
     s.samples_per_ray = hc[FC_SAMPLES_PER_RAY];
     s.n_samples = uint64_t(hc[FC_SAMPLES_LO]) | (uint64_t(hc[FC_SAMPLES_HI]) << 32);
     s.n_launches = R.launches;
+    s.error_flags = hc[FC_ERROR];
     if (cudaEventElapsedTime(&s.select_ms, R.t_sel0, R.t_sel1) != cudaSuccess ||
         cudaEventElapsedTime(&s.raycast_ms, R.t_ray0, R.t_ray1) != cudaSuccess)
     {
@@ -1119,6 +1129,8 @@ extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)
     }
     *out = s;
     if (hc[FC_ERROR])
-        return fail(ctx, LV_ENOMEM, "rendering set overflowed its buffer");
+        return fail(ctx, hc[FC_ERROR] == 1 ? LV_ENOMEM : LV_EDEVICE,
+                    hc[FC_ERROR] == 1 ? "rendering set overflowed its buffer"
+                                      : "a device index check failed (access skipped)");
     return LV_OK;
 }

@@ -129,6 +129,8 @@ void complete(lv_server* S, Inflight& f)
         Req* r = f.reqs[i];
         r->t_done = t;
         r->stats = st[i];
+        if (r->status == LV_OK && st[i].error_flags)
+            r->status = LV_EDEVICE;
         r->done = true;
         ++S->n_done;
     }

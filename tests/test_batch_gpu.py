@@ -129,3 +129,65 @@ def test_autotune_picks_valid_config(gpu_ctx):
         v.close()
     for t in tfs:
         t.close()
+
+
+def test_graph_replay_with_new_composition(gpu_ctx):
+    """The same batch object replays its captured graph for a new set of views
+    with the same count and kernel variants but a different split between
+    them and a different number of octree roots: every view still matches."""
+    import torch
+    import livre_gb300 as lv
+    a = lv.VolumeInformation(128, 32, 1)
+    b16 = lv.VolumeInformation(96, 16, 1, dtype=lv.DT_UINT16)
+    c = lv.VolumeInformation((128, 96, 64), 16, 1)  # several root blocks
+    va, vb, vc = (gpu_ctx.blob_volume(vi, 8, 40 + k) for k, vi in enumerate((a, b16, c)))
+    tf = gpu_ctx.transfer_function(lv.linear_ramp_tf())
+
+    def view(vol, vi, k, W=40, H=32):
+        mv, proj = lv.orbit_camera(k, 8, vi.world_size, W, H, radius_scale=1.3)
+        d = gpu_ctx.render_desc(mv, proj, W, H, sse=1.0)
+        gpu_ctx.render(vol, tf, d)  # bricks resident
+        return (vol, tf, d, torch.zeros((H, W, 4), dtype=torch.float32, device="cuda"))
+
+    batch = lv.Batch(gpu_ctx)
+    first = [view(va, a, 0), view(va, a, 1), view(vb, b16, 2)]
+    second = [view(vc, c, 3), view(vb, b16, 4), view(vb, b16, 5)]  # 1 u8 + 2 u16, more roots
+    for items in (first, second, first, second):
+        batch.render(items)
+        stats = batch.stats(len(items))[0]
+        assert all(s["error_flags"] == 0 for s in stats)
+        for v, t, d, o in items:
+            ref = gpu_ctx.render(v, t, d)
+            assert float((ref - o).abs().max()) <= 1e-6
+    batch.close()
+    for v in (va, vb, vc):
+        v.close()
+    tf.close()
+
+
+def test_graph_cache_after_frontier_growth(gpu_ctx):
+    """Batches of growing size reallocate the batch's frontier queues several
+    times; replaying a smaller batch afterwards must use the new queues (the
+    graph captured before the growth is dropped) and still match."""
+    import torch
+    import livre_gb300 as lv
+    vi = lv.VolumeInformation(256, 32, 1)
+    vol = gpu_ctx.blob_volume(vi, 10, 77)
+    tf = gpu_ctx.transfer_function(lv.linear_ramp_tf())
+    views = []
+    for k in range(12):
+        mv, proj = lv.orbit_camera(k, 12, vi.world_size, 24, 24, radius_scale=1.2)
+        d = gpu_ctx.render_desc(mv, proj, 24, 24, sse=1.0)
+        gpu_ctx.render(vol, tf, d)
+        views.append((vol, tf, d, torch.zeros((24, 24, 4), dtype=torch.float32, device="cuda")))
+    batch = lv.Batch(gpu_ctx)
+    for n in list(range(1, 13)) + [1, 3, 12, 2]:
+        items = views[:n]
+        batch.render(items)
+        stats = batch.stats(n)[0]
+        assert all(s["error_flags"] == 0 for s in stats)
+        for v, t, d, o in items:
+            assert float((gpu_ctx.render(v, t, d) - o).abs().max()) <= 1e-6, n
+    batch.close()
+    vol.close()
+    tf.close()
