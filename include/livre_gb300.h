@@ -127,6 +127,24 @@ lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
                             uint32_t capacity, uint32_t* d_result,
                             void* stream);
 
+/* LOD selection that allocates nothing, for callers that cannot allocate
+ * device memory (a host application whose own caching allocator owns the
+ * GPU's memory, or a per-frame path that must not risk the device-wide
+ * synchronisation of an allocation). No counterpart in the reference.
+ * Same inputs and outputs as lv_select_visible, no context: it runs on the
+ * current device, with its frontier queues in one fixed device array of the
+ * library (about 6.3 MB, held by every GPU that loads the library until the
+ * process exits). Limits: at most 262144 nodes per octree level (larger
+ * volumes return LV_ENOMEM) and range {0, 1} only (LV_EINVAL otherwise).
+ * The first call on a device looks up that array's address; make it before
+ * any stream capture on the device. All calls share the array: calls whose
+ * work overlaps on the GPU race and must be ordered by the caller. */
+lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
+                                    const lv_camera* camera,
+                                    const lv_lod_params* params,
+                                    uint64_t* d_out_ids, uint32_t capacity,
+                                    uint32_t* d_result, void* stream);
+
 /* ---------------------------------------------------------- brick pool */
 
 /* Device brick pool budget in bytes (VolumeRendererParameters

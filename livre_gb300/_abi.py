@@ -108,6 +108,8 @@ _SIGNATURES = {
     "lv_abi_version": (C.c_uint32, []),
     "lv_select_visible": (C.c_int, [C.c_void_p, P(VolumeInfo), P(Camera), P(LodParams),
                                     C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "lv_select_visible_noalloc": (C.c_int, [P(VolumeInfo), P(Camera), P(LodParams), C.c_void_p,
+                                            C.c_uint32, C.c_void_p, C.c_void_p]),
     "lv_pool_configure": (C.c_int, [C.c_void_p, C.c_size_t]),
     "lv_pool_purge": (C.c_int, [C.c_void_p]),
     "lv_volume_create": (C.c_int, [C.c_void_p, P(VolumeInfo), GET_DATA_FN, C.c_void_p,

@@ -615,3 +615,172 @@ extern "C" lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
         return range_slice(ctx, *vol, params->range, d_out_ids, d_result, s);
     return LV_OK;
 }
+
+/* ------------------------------------------------------------------------
+ * LOD selection without any allocation.
+ *
+ * Some callers cannot allocate device memory when they select bricks: a host
+ * application whose caching allocator already owns the GPU's memory (an extra
+ * cudaMalloc would fail or fragment it), or a per-frame path where the
+ * device-wide synchronisation an allocation may trigger is not acceptable.
+ * lv_select_visible_noalloc serves them: its frontier queues live in one
+ * fixed device array of this file, so it needs no context and allocates
+ * nothing. The caller still passes the output ids and result words.
+ *
+ * Limits and sharing:
+ *  - the array holds kNoAllocFrontier nodes per octree level; a volume whose
+ *    largest level has more nodes is rejected with LV_ENOMEM;
+ *  - only the full range {0, 1} is supported (the DFS-order range slice needs
+ *    sort space); other ranges return LV_EINVAL;
+ *  - every call on a device shares the one array, and the array keeps the
+ *    last call's contents: the kernels clear what must start at zero
+ *    (per-level counters, result words) on every call, but two calls whose
+ *    work overlaps on the GPU (different streams, or different host threads
+ *    without ordering) race on the array and give wrong results;
+ *  - the first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current) and caches it; make
+ *    that first call before any stream capture on the device.
+ * ---------------------------------------------------------------------- */
+namespace lv
+{
+namespace
+{
+constexpr uint32_t kNoAllocFrontier = 262144; /* nodes per octree level */
+constexpr uint32_t kNoAllocMaxDevices = 64;
+constexpr uint64_t kNoAllocIds = 0;                                   /* 2 x u64 queues */
+constexpr uint64_t kNoAllocViews = kNoAllocIds + 16ull * kNoAllocFrontier; /* 2 x u32 */
+constexpr uint64_t kNoAllocCounts = kNoAllocViews + 8ull * kNoAllocFrontier;
+constexpr uint64_t kNoAllocLod = kNoAllocCounts + 256;
+constexpr uint64_t kNoAllocBytes = kNoAllocLod + ((sizeof(LodView) + 255) & ~size_t(255));
+
+/* 24 B per frontier node + counters + one LodView: about 6.3 MB per device. */
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mutex;
+unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+/* Device address of g_noalloc_scratch on `dev` (the current device). */
+lv_status noalloc_scratch(int dev, unsigned char** out)
+{
+    if (dev < 0 || dev >= int(kNoAllocMaxDevices))
+        return LV_EDEVICE;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev])
+    {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+        {
+            cudaGetLastError();
+            return LV_EDEVICE;
+        }
+        g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return LV_OK;
+}
+
+/* The per-view constants of make_lod_view, with status codes only. */
+lv_status noalloc_lod_view(const lv_volume_info& vol, const lv_camera& cam,
+                           const lv_lod_params& p, LodView& V)
+{
+    if (vol.depth == 0 || vol.depth > kMaxLevels || p.window_height == 0 ||
+        p.n_clip_planes > 6)
+        return LV_EINVAL;
+    float inv_mv[16], inv_p[16], lim[6], planes[6][4], eye[3], dir[3];
+    bool ok = false;
+    frustum_setup(cam.modelview, cam.projection, inv_mv, inv_p, lim, planes, eye, dir, &ok);
+    if (!ok)
+        return LV_EINVAL;
+    std::memset(&V, 0, sizeof(V));
+    std::memcpy(V.planes, planes, sizeof(planes));
+    V.nearp = lim[4];
+    for (int i = 0; i < 3; ++i)
+        V.eye_near[i] = eye[i] - dir[i] * V.nearp;
+    V.wspp = (lim[3] - lim[2]) / float(p.window_height);
+    V.sse = p.screen_space_error;
+    for (int i = 0; i < 3; ++i)
+    {
+        if (vol.max_block[i] <= 2u * vol.overlap[i])
+            return LV_EINVAL;
+        V.world_size[i] = vol.world_size[i];
+        V.half[i] = vol.world_size[i] * 0.5f;
+        V.root_blocks[i] = vol.root_blocks[i];
+        V.block[i] = vol.max_block[i] - 2u * vol.overlap[i];
+    }
+    V.n_clip = p.n_clip_planes;
+    std::memcpy(V.clip, p.clip_planes, sizeof(V.clip));
+    V.min_lod = p.min_lod;
+    V.max_lod = p.max_lod;
+    V.depth = vol.depth;
+    V.time_step = p.time_step;
+    return LV_OK;
+}
+} // namespace
+} // namespace lv
+
+extern "C" lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
+                                               const lv_camera* camera,
+                                               const lv_lod_params* params,
+                                               uint64_t* d_out_ids, uint32_t capacity,
+                                               uint32_t* d_result, void* stream)
+{
+    using namespace lv;
+    if (!vol || !camera || !params || !d_result || (!d_out_ids && capacity))
+        return LV_EINVAL;
+    if (!(params->range[0] == 0.0f && params->range[1] == 1.0f))
+        return LV_EINVAL;
+    if (vol->depth == 0 || vol->depth > kMaxLevels)
+        return LV_EINVAL;
+    if (max_frontier(*vol) > kNoAllocFrontier)
+        return LV_ENOMEM; /* the octree needs more than the fixed scratch holds */
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return LV_EDEVICE;
+    }
+    unsigned char* base = nullptr;
+    lv_status st = noalloc_scratch(dev, &base);
+    if (st != LV_OK)
+        return st;
+    LodView V;
+    st = noalloc_lod_view(*vol, *camera, *params, V);
+    if (st != LV_OK)
+        return st;
+    V.out_ids = d_out_ids;
+    V.capacity = capacity;
+    V.result = d_result;
+    V.root_offset = 0;
+    const uint32_t roots = vol->root_blocks[0] * vol->root_blocks[1] * vol->root_blocks[2];
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    LodView* dview = reinterpret_cast<LodView*>(base + kNoAllocLod);
+    uint64_t* ids[2] = {reinterpret_cast<uint64_t*>(base + kNoAllocIds),
+                        reinterpret_cast<uint64_t*>(base + kNoAllocIds) + kNoAllocFrontier};
+    uint32_t* views[2] = {reinterpret_cast<uint32_t*>(base + kNoAllocViews),
+                          reinterpret_cast<uint32_t*>(base + kNoAllocViews) + kNoAllocFrontier};
+    uint32_t* counts = reinterpret_cast<uint32_t*>(base + kNoAllocCounts);
+    uint32_t* overflow = counts + kMaxLevels + 1;
+    /* V lives on the host stack: a copy from pageable memory has consumed it
+     * by the time cudaMemcpyAsync returns */
+    if (cudaMemcpyAsync(dview, &V, sizeof(V), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return LV_EDEVICE;
+    }
+    lod_roots_kernel<<<1, 128, 0, s>>>(dview, 1, ids[0], views[0], counts, kMaxLevels + 2,
+                                       roots, kNoAllocFrontier, nullptr);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    for (uint32_t l = 0; l < vol->depth; ++l)
+    {
+        const int in = l & 1, out = in ^ 1;
+        lod_level_kernel<<<2 * sms, 256, 0, s>>>(dview, ids[in], views[in], counts + l,
+                                                 ids[out], views[out], counts + l + 1,
+                                                 kNoAllocFrontier, overflow);
+    }
+    lod_finish_kernel<<<1, 128, 0, s>>>(dview, 1, overflow);
+    if (cudaGetLastError() != cudaSuccess)
+        return LV_EDEVICE;
+    return LV_OK;
+}
