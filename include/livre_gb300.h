@@ -306,6 +306,22 @@ typedef struct lv_frame_stats
 lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                     const lv_render_desc* desc, float* d_rgba, void* stream);
 
+/* Launch shape of lv_render's ray cast. tile_w x tile_h pixel tiles (32 to
+ * 1024 pixels) go to the warps of a persistent grid through a device queue,
+ * and a lane whose ray has finished takes the tile's next pixel after
+ * samples_per_check samples (1..64). tile_w = 0 launches one thread per
+ * pixel instead (8 x 16 blocks), the default: on short rays (tens of
+ * samples) the per-ray set-up a refill repeats costs more than the idle
+ * lanes it saves. The image is the same either way. No reference counterpart (the reference rasterises one brick
+ * at a time, RayCastRenderer.cpp:503-571). */
+typedef struct lv_render_launch
+{
+    uint32_t tile_w, tile_h;
+    uint32_t samples_per_check;
+} lv_render_launch;
+lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* cfg);
+lv_status lv_get_render_launch(lv_ctx* ctx, lv_render_launch* cfg);
+
 /* Statistics of the last lv_render / lv_render_batch call (synchronises with
  * its stream). */
 lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out);
@@ -327,14 +343,29 @@ typedef struct lv_batch_view
     float* d_rgba; /* width*height RGBA32F on the device */
 } lv_batch_view;
 
+/* Work queues of the persistent ray-cast kernels. */
+enum
+{
+    LV_QUEUE_CTA_TILES = 0,  /* a CTA per work item: tile_w x tile_h threads,
+                                one ray each */
+    LV_QUEUE_WARP_REFILL = 1 /* a warp per work item: the tile's pixels are
+                                handed to lanes as their rays finish */
+};
+
 /* Launch shape of the persistent ray-cast kernel. */
 typedef struct lv_batch_config
 {
-    uint32_t tile_w, tile_h; /* pixels per work item = threads per CTA
-                                (a multiple of 32, at most 256) */
-    uint32_t ctas_per_sm;    /* persistent grid = SMs * ctas_per_sm */
-    uint32_t tf_shared;      /* 1: transfer function staged in shared memory */
+    uint32_t tile_w, tile_h; /* pixels per work item; CTA tiles: = threads per
+                                CTA (a multiple of 32, at most 256); warp
+                                refill: 32 to 1024 pixels */
+    uint32_t ctas_per_sm;    /* persistent grid = SMs * ctas_per_sm; 0 = as
+                                many CTAs as are resident at once */
+    uint32_t tf_shared;      /* 1: transfer function staged in shared memory
+                                (CTA tiles only) */
     uint32_t use_graph;      /* 1: replay the batch as one CUDA graph */
+    uint32_t queue;          /* LV_QUEUE_* */
+    uint32_t samples_per_check; /* warp refill: samples a lane takes between
+                                   refills (1..64) */
 } lv_batch_config;
 
 /* A batch renderer on ctx (its own stream, graphs and per-view buffers).
@@ -355,10 +386,18 @@ lv_status lv_batch_render(lv_batch* batch, const lv_batch_view* views,
  * (device global timer, first CTA start to last CTA end). */
 lv_status lv_batch_stats(lv_batch* batch, lv_frame_stats* out, uint32_t n,
                          float* batch_ms, float* raycast_ms);
-/* Times the persistent kernel on this batch for every tile shape in
- * {8x8, 16x8, 8x16, 16x16, 32x4, 32x8}, CTAs per SM in {2, 4, 8} and
- * transfer-function staging on/off (reps timed launches each), keeps the
- * fastest configuration and returns it in `chosen`. */
+/* CUDA-graph cache of a batch: graphs captured and launches replayed so
+ * far, and the graphs held now. A batch of n views runs as a launch for the
+ * next power of two (padded with empty views), so batch sizes 1..64 share 7
+ * graphs per set of kernel variants. */
+lv_status lv_batch_graph_stats(lv_batch* batch, uint64_t* captures,
+                               uint64_t* replays, uint32_t* cached);
+/* Times the persistent ray cast on this batch (reps timed launches each)
+ * for CTA tiles of {8x8, 16x8, 8x16, 16x16, 32x4, 32x8} pixels with and
+ * without transfer-function staging, and for warp-refill tiles of {8x4, 8x8,
+ * 16x8, 16x16} pixels with refills every {2, 8, 32} samples, all on a
+ * resident grid; keeps the fastest configuration and returns it in
+ * `chosen`. */
 lv_status lv_batch_autotune(lv_batch* batch, const lv_batch_view* views,
                             uint32_t n, void* stream, uint32_t reps,
                             lv_batch_config* chosen);
@@ -380,6 +419,8 @@ typedef struct lv_server_config
     uint32_t max_queue;   /* submit returns LV_EAGAIN beyond this (0 = no limit) */
     uint32_t use_graph;   /* replay batches as CUDA graphs */
     uint32_t tile_w, tile_h, ctas_per_sm; /* 0 = batch defaults */
+    uint64_t max_pixels;  /* pixels per launch, 0 = no limit (a request larger
+                             than the budget still runs, alone) */
 } lv_server_config;
 
 /* One render request: the output buffer (width*height RGBA32F, device) must
@@ -419,6 +460,20 @@ lv_status lv_server_wait(lv_server* server, uint64_t ticket,
                          uint32_t timeout_ms, lv_request_result* out);
 lv_status lv_server_counters(lv_server* server, uint64_t* completed,
                              uint64_t* batches, uint64_t* queued);
+/* Where the server thread's time went, summed since creation (batched
+ * mode; the plain mode reports its lv_render calls as launch_ms and their
+ * device time as device_ms). */
+typedef struct lv_server_profile
+{
+    uint64_t batches, requests, graph_captures;
+    double select_ms;  /* admission selections: host wall time */
+    double stream_ms;  /* streaming admitted misses: host wall time */
+    double launch_ms;  /* enqueuing batches (graph capture included) */
+    double wait_ms;    /* blocked on in-flight batches */
+    double device_ms;  /* device time of the batches (events around each) */
+    double raycast_ms; /* of which the ray-cast launches */
+} lv_server_profile;
+lv_status lv_server_get_profile(lv_server* server, lv_server_profile* out);
 /* Finishes every queued request, then stops the server thread. */
 void lv_server_destroy(lv_server* server);
 

@@ -25,7 +25,8 @@ import numpy as np
 
 from . import _abi
 from ._abi import (BLOB_DEVICE, BLOB_HOST, DT_UINT8, DT_UINT16, FILTER_NEAREST,
-                   FILTER_TRILINEAR, STEP_HALF_VOXEL, STEP_REFERENCE, LivreError, check, lib)
+                   FILTER_TRILINEAR, QUEUE_CTA_TILES, QUEUE_WARP_REFILL, STEP_HALF_VOXEL,
+                   STEP_REFERENCE, LivreError, check, lib)
 
 __all__ = ["NodeId", "VolumeInformation", "VolumeRendererParameters", "TransferFunction1D",
            "Context", "perspective", "look_at", "orbit_camera", "LivreError"]
@@ -545,6 +546,17 @@ class Context:
                               _stream(stream)), self.handle)
         return out
 
+    def render_launch(self):
+        """lv_render's ray-cast launch shape (lv_get_render_launch)."""
+        c = _abi.RenderLaunch()
+        check(lib().lv_get_render_launch(self.handle, C.byref(c)), self.handle)
+        return {k: getattr(c, k) for k, _ in c._fields_}
+
+    def set_render_launch(self, tile_w=8, tile_h=8, samples_per_check=8):
+        """tile_w = 0: one thread per pixel; else warp tiles with lane refill."""
+        c = _abi.RenderLaunch(tile_w, tile_h, samples_per_check)
+        check(lib().lv_set_render_launch(self.handle, C.byref(c)), self.handle)
+
     def last_stats(self):
         s = _abi.FrameStats()
         check(lib().lv_last_stats(self.handle, C.byref(s)), self.handle)
@@ -591,8 +603,12 @@ class Batch:
         check(lib().lv_batch_get_config(self.handle, C.byref(c)), self.ctx.handle)
         return c.as_dict()
 
-    def set_config(self, tile_w=16, tile_h=8, ctas_per_sm=4, tf_shared=0, use_graph=1):
-        c = _abi.BatchConfig(tile_w, tile_h, ctas_per_sm, tf_shared, use_graph)
+    def set_config(self, tile_w=8, tile_h=8, ctas_per_sm=0, tf_shared=0, use_graph=1,
+                   queue=None, samples_per_check=8):
+        if queue is None:
+            queue = _abi.QUEUE_CTA_TILES if tf_shared else _abi.QUEUE_WARP_REFILL
+        c = _abi.BatchConfig(tile_w, tile_h, ctas_per_sm, tf_shared, use_graph, queue,
+                             samples_per_check)
         check(lib().lv_batch_set_config(self.handle, C.byref(c)), self.ctx.handle)
 
     @staticmethod
@@ -611,6 +627,12 @@ class Batch:
         self._views = (arr, items)  # keep tensors alive until the next call
         check(lib().lv_batch_render(self.handle, arr, len(items), _stream(stream)),
               self.ctx.handle)
+
+    def graph_stats(self):
+        """(captures, replays, cached graphs) of this batch's graph cache."""
+        a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint32()
+        check(lib().lv_batch_graph_stats(self.handle, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def stats(self, n):
         out = (_abi.FrameStats * max(n, 1))()
@@ -631,10 +653,11 @@ class Server:
     """Render server (lv_server): continuous batching or plain per-request."""
 
     def __init__(self, ctx, mode=_abi.SERVE_BATCHED, max_batch=32, max_queue=0, use_graph=1,
-                 tile=None, ctas_per_sm=0):
+                 tile=None, ctas_per_sm=0, max_pixels=0):
         self.ctx = ctx
         tw, th = tile if tile else (0, 0)
-        cfg = _abi.ServerConfig(mode, max_batch, max_queue, use_graph, tw, th, ctas_per_sm)
+        cfg = _abi.ServerConfig(mode, max_batch, max_queue, use_graph, tw, th, ctas_per_sm,
+                                max_pixels)
         h = C.c_void_p()
         check(lib().lv_server_create(ctx.handle, C.byref(cfg), C.byref(h)), ctx.handle)
         self.handle = h
@@ -661,6 +684,12 @@ class Server:
         a, b, c = C.c_uint64(), C.c_uint64(), C.c_uint64()
         check(lib().lv_server_counters(self.handle, C.byref(a), C.byref(b), C.byref(c)))
         return {"completed": a.value, "batches": b.value, "queued": c.value}
+
+    def profile(self):
+        """Where the server thread's time went (lv_server_get_profile)."""
+        p = _abi.ServerProfile()
+        check(lib().lv_server_get_profile(self.handle, C.byref(p)))
+        return {k: getattr(p, k) for k, _ in _abi.ServerProfile._fields_}
 
     def close(self):
         if self.handle:

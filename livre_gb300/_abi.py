@@ -71,18 +71,36 @@ class BatchView(C.Structure):
                 ("d_rgba", C.c_void_p)]
 
 
+QUEUE_CTA_TILES = 0
+QUEUE_WARP_REFILL = 1
+
+
 class BatchConfig(C.Structure):
     _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("ctas_per_sm", C.c_uint32),
-                ("tf_shared", C.c_uint32), ("use_graph", C.c_uint32)]
+                ("tf_shared", C.c_uint32), ("use_graph", C.c_uint32), ("queue", C.c_uint32),
+                ("samples_per_check", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class RenderLaunch(C.Structure):
+    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
+                ("samples_per_check", C.c_uint32)]
+
+
+class ServerProfile(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("requests", C.c_uint64),
+                ("graph_captures", C.c_uint64), ("select_ms", C.c_double),
+                ("stream_ms", C.c_double), ("launch_ms", C.c_double),
+                ("wait_ms", C.c_double), ("device_ms", C.c_double),
+                ("raycast_ms", C.c_double)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("mode", C.c_uint32), ("max_batch", C.c_uint32), ("max_queue", C.c_uint32),
                 ("use_graph", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
-                ("ctas_per_sm", C.c_uint32)]
+                ("ctas_per_sm", C.c_uint32), ("max_pixels", C.c_uint64)]
 
 
 class Request(C.Structure):
@@ -143,6 +161,11 @@ _SIGNATURES = {
     "lv_server_create": (C.c_int, [C.c_void_p, P(ServerConfig), P(C.c_void_p)]),
     "lv_server_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_uint64)]),
     "lv_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, P(RequestResult)]),
+    "lv_set_render_launch": (C.c_int, [C.c_void_p, P(RenderLaunch)]),
+    "lv_get_render_launch": (C.c_int, [C.c_void_p, P(RenderLaunch)]),
+    "lv_server_get_profile": (C.c_int, [C.c_void_p, P(ServerProfile)]),
+    "lv_batch_graph_stats": (C.c_int, [C.c_void_p, P(C.c_uint64), P(C.c_uint64),
+                                       P(C.c_uint32)]),
     "lv_server_counters": (C.c_int, [C.c_void_p, P(C.c_uint64), P(C.c_uint64),
                                      P(C.c_uint64)]),
     "lv_server_destroy": (None, [C.c_void_p]),

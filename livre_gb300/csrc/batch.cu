@@ -55,7 +55,7 @@ struct lv_batch
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr, user_ready = nullptr;
     cudaEvent_t t_sel0 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
-    lv_batch_config cfg{16, 8, 4, 0, 1};
+    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_CTA_TILES, 8};
     /* per-view region strides (grow-only) */
     uint64_t nodes_stride = 0, cells_stride = 0, missing_stride = 0;
     uint32_t views_cap = 0;
@@ -79,6 +79,7 @@ struct lv_batch
     uint32_t launches = 0;
     uint32_t last_n = 0;
     uint32_t sel_generation = 0; /* b->sel.generation the cached graphs use */
+    uint64_t captures = 0, replays = 0;
 
     ~lv_batch()
     {
@@ -127,7 +128,7 @@ ParamLayout param_layout(uint32_t n)
 }
 
 lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
-                         cudaStream_t user)
+                         cudaStream_t user, uint32_t n_run)
 {
     lv_ctx* ctx = b->ctx;
     uint64_t nodes = b->nodes_stride, cells = b->cells_stride;
@@ -142,7 +143,7 @@ lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
         cells = std::max(cells, c);
         depth = std::max(depth, vi.depth);
     }
-    const uint32_t vcap = std::max(b->views_cap, n);
+    const uint32_t vcap = std::max(b->views_cap, n_run);
     const bool grow = nodes > b->nodes_stride || cells > b->cells_stride ||
                       vcap > b->views_cap;
     b->depth_max = depth;
@@ -220,7 +221,7 @@ lv_status process_misses(lv_batch* b)
     return LV_OK;
 }
 
-lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n,
+lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n, uint32_t n_run,
                       std::vector<Group>& groups, uint32_t& total_roots,
                       uint32_t& tfn_max)
 {
@@ -299,6 +300,28 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n,
         tfn_max = std::max(tfn_max, bv.tf->n);
         groups[kernel_variant(V.dtype, V.filter, V.edge)].views.push_back(i);
     }
+    /* views [n, n_run) pad the launch to a power of two so a few captured
+     * graphs serve every batch size: no roots, no visible nodes, no tiles */
+    for (uint32_t i = n; i < n_run; ++i)
+    {
+        const ViewSlots S = view_slots(b, i);
+        uint32_t* counters = dz + kOutWords * i;
+        uint32_t* selres = counters + FC_WORDS;
+        std::memset(&lods[i], 0, sizeof(LodView));
+        lods[i].out_ids = reinterpret_cast<uint64_t*>(dlists + S.visible);
+        lods[i].result = selres;
+        lods[i].depth = 1;
+        lods[i].root_offset = total_roots;
+        std::memset(&res[i], 0, sizeof(ResolveView));
+        res[i].n_visible_ptr = selres + LV_SEL_WRITTEN;
+        res[i].counters = counters;
+        res[i].leaf = dleaf + S.leaf / 4;
+        res[i].depth = 1;
+        std::memset(&rays[i], 0, sizeof(RayView));
+        rays[i].counters = counters;
+        rays[i].depth = 1;
+        rays[i].samples_fixed = 1;
+    }
     /* queue tables */
     uint32_t* tables = reinterpret_cast<uint32_t*>(h + PL.tables);
     const uint32_t stride = 2 * b->views_cap + 1;
@@ -360,8 +383,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         Q.tile_h = b->cfg.tile_h;
         Q.head = heads + g;
         Q.clock = clock;
-        st = launch_persistent(ctx, g, b->cfg.tf_shared,
-                               reinterpret_cast<RayView*>(d + PL.ray), Q, b->cfg.ctas_per_sm,
+        st = launch_persistent(ctx, g, b->cfg, reinterpret_cast<RayView*>(d + PL.ray), Q,
                                tfn_max, s);
         if (st != LV_OK)
             return st;
@@ -421,11 +443,25 @@ extern "C" lv_status lv_batch_set_config(lv_batch* b, const lv_batch_config* cfg
 {
     if (!b || !cfg)
         return LV_EINVAL;
-    const uint32_t threads = cfg->tile_w * cfg->tile_h;
-    if (threads == 0 || threads > 256 || threads % 32 != 0 || cfg->ctas_per_sm == 0 ||
-        cfg->ctas_per_sm > 16)
-        return fail(b->ctx, LV_EINVAL, "tile_w * tile_h must be a multiple of 32 up to 256; "
-                                       "ctas_per_sm in 1..16");
+    const uint32_t pixels = cfg->tile_w * cfg->tile_h;
+    if (cfg->ctas_per_sm > 16)
+        return fail(b->ctx, LV_EINVAL, "ctas_per_sm in 0..16");
+    if (cfg->queue == LV_QUEUE_CTA_TILES)
+    {
+        if (pixels == 0 || pixels > 256 || pixels % 32 != 0)
+            return fail(b->ctx, LV_EINVAL,
+                        "CTA tiles: tile_w * tile_h must be a multiple of 32 up to 256");
+    }
+    else if (cfg->queue == LV_QUEUE_WARP_REFILL)
+    {
+        if (pixels < 32 || pixels > 1024 || cfg->samples_per_check == 0 ||
+            cfg->samples_per_check > 64 || cfg->tf_shared)
+            return fail(b->ctx, LV_EINVAL,
+                        "warp refill: 32..1024 pixels per tile, samples_per_check in 1..64, "
+                        "no shared transfer function");
+    }
+    else
+        return fail(b->ctx, LV_EINVAL, "unknown queue kind");
     std::lock_guard<std::mutex> lock(b->ctx->mutex);
     b->cfg = *cfg;
     return LV_OK;
@@ -461,7 +497,11 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
         return LV_OK;
     /* the host staging is read by the previous launch until it completes */
     LV_CUDA(ctx, cudaEventSynchronize(b->done));
-    st = ensure_regions(b, views, n, user);
+    uint32_t n_run = n;
+    if (b->cfg.use_graph)
+        while (n_run & (n_run - 1))
+            n_run += n_run & (~n_run + 1); /* round up to a power of two */
+    st = ensure_regions(b, views, n, user, n_run);
     if (st != LV_OK)
         return st;
     uint64_t frontier = 0;
@@ -483,7 +523,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     ++b->launch_id;
     std::vector<Group> groups;
     uint32_t total_roots = 0, tfn_max = 0;
-    st = fill_params(b, views, n, groups, total_roots, tfn_max);
+    st = fill_params(b, views, n, n_run, groups, total_roots, tfn_max);
     if (st != LV_OK)
         return st;
     if (b->cfg.tf_shared && tfn_max > 2048)
@@ -497,20 +537,22 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     LV_CUDA(ctx, cudaEventRecord(b->t_sel0, b->stream));
     if (b->cfg.use_graph)
     {
-        const auto key = std::make_tuple(n, mask, b->cfg.tile_w, b->cfg.tile_h, b->cfg.ctas_per_sm,
-                                         b->cfg.tf_shared ? tfn_max : 0u, b->depth_max,
-                                         b->generation, uintptr_t(b->sel.generation));
+        const auto key = std::make_tuple(
+            n_run, mask, b->cfg.tile_w, b->cfg.tile_h,
+            b->cfg.ctas_per_sm | (b->cfg.queue << 8) | (b->cfg.samples_per_check << 16),
+            b->cfg.tf_shared ? tfn_max : 0u, b->depth_max, b->generation,
+            uintptr_t(b->sel.generation));
         auto it = b->graphs.find(key);
         if (it == b->graphs.end())
         {
-            if (b->graphs.size() >= 16)
+            if (b->graphs.size() >= 32)
             {
                 cudaGraphExecDestroy(b->graphs.begin()->second);
                 b->graphs.erase(b->graphs.begin());
             }
             cudaGraph_t g = nullptr;
             LV_CUDA(ctx, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            st = enqueue_batch(b, n, groups, total_roots, tfn_max);
+            st = enqueue_batch(b, n_run, groups, total_roots, tfn_max);
             const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
             if (st != LV_OK)
             {
@@ -524,7 +566,10 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
             cudaGraphDestroy(g);
             LV_CUDA(ctx, ie);
             it = b->graphs.emplace(key, exec).first;
+            ++b->captures;
         }
+        else
+            ++b->replays;
         LV_CUDA(ctx, cudaGraphLaunch(it->second, b->stream));
     }
     else
@@ -536,7 +581,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     LV_CUDA(ctx, cudaEventRecord(b->t_ray1, b->stream));
     LV_CUDA(ctx, cudaEventRecord(b->done, b->stream));
     LV_CUDA(ctx, cudaStreamWaitEvent(user, b->done, 0));
-    b->last_n = n;
+    b->last_n = n_run;
     b->last.assign(views, views + n);
     b->pending = true;
     /* selection: roots + levels + finish; resolve, prune, leaf, step;
@@ -594,48 +639,84 @@ extern "C" lv_status lv_batch_stats(lv_batch* b, lv_frame_stats* out, uint32_t n
     return LV_OK;
 }
 
+extern "C" lv_status lv_batch_graph_stats(lv_batch* b, uint64_t* captures, uint64_t* replays,
+                                          uint32_t* cached)
+{
+    if (!b)
+        return LV_EINVAL;
+    std::lock_guard<std::mutex> lock(b->ctx->mutex);
+    if (captures)
+        *captures = b->captures;
+    if (replays)
+        *replays = b->replays;
+    if (cached)
+        *cached = uint32_t(b->graphs.size());
+    return LV_OK;
+}
+
 extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, uint32_t n,
                                        void* stream, uint32_t reps, lv_batch_config* chosen)
 {
     if (!b || !views || n == 0)
         return LV_EINVAL;
-    static const uint32_t shapes[][2] = {{8, 8}, {16, 8}, {8, 16}, {16, 16}, {32, 4}, {32, 8}};
-    static const uint32_t ctas[] = {2, 4, 8};
+    /* CTA tiles: 6 tile shapes x TF staging, resident grid; warp refill:
+     * 4 tile sizes x 3 refill intervals */
+    static const uint32_t cta_shapes[][2] = {{8, 8}, {16, 8}, {8, 16}, {16, 16}, {32, 4}, {32, 8}};
+    static const uint32_t warp_shapes[][2] = {{8, 4}, {8, 8}, {16, 8}, {16, 16}};
+    static const uint32_t checks[] = {2, 8, 32};
+    std::vector<lv_batch_config> cands;
     const lv_batch_config start = b->cfg;
+    for (const auto& sh : cta_shapes)
+        for (uint32_t tfs = 0; tfs < 2; ++tfs)
+        {
+            lv_batch_config c = start;
+            c.queue = LV_QUEUE_CTA_TILES;
+            c.tile_w = sh[0];
+            c.tile_h = sh[1];
+            c.ctas_per_sm = 0;
+            c.tf_shared = tfs;
+            c.samples_per_check = 8;
+            cands.push_back(c);
+        }
+    for (const auto& sh : warp_shapes)
+        for (uint32_t k : checks)
+        {
+            lv_batch_config c = start;
+            c.queue = LV_QUEUE_WARP_REFILL;
+            c.tile_w = sh[0];
+            c.tile_h = sh[1];
+            c.ctas_per_sm = 0;
+            c.tf_shared = 0;
+            c.samples_per_check = k;
+            cands.push_back(c);
+        }
     lv_batch_config best = start;
     float best_ms = 1e30f;
     reps = reps ? reps : 3;
-    for (const auto& sh : shapes)
-        for (uint32_t c : ctas)
-            for (uint32_t tfs = 0; tfs < 2; ++tfs)
+    for (const lv_batch_config& cfg : cands)
+    {
+        if (lv_batch_set_config(b, &cfg) != LV_OK)
+            continue;
+        float total = 0.f;
+        bool ok = true;
+        for (uint32_t r = 0; r <= reps && ok; ++r)
+        {
+            if (lv_batch_render(b, views, n, stream) != LV_OK)
             {
-                lv_batch_config cfg = start;
-                cfg.tile_w = sh[0];
-                cfg.tile_h = sh[1];
-                cfg.ctas_per_sm = c;
-                cfg.tf_shared = tfs;
-                if (lv_batch_set_config(b, &cfg) != LV_OK)
-                    continue;
-                float total = 0.f;
-                bool ok = true;
-                for (uint32_t r = 0; r <= reps && ok; ++r)
-                {
-                    if (lv_batch_render(b, views, n, stream) != LV_OK)
-                    {
-                        ok = false;
-                        break;
-                    }
-                    float all = 0.f, ray = 0.f;
-                    lv_batch_stats(b, nullptr, 0, &all, &ray);
-                    if (r > 0)
-                        total += ray;
-                }
-                if (ok && total / reps < best_ms)
-                {
-                    best_ms = total / reps;
-                    best = cfg;
-                }
+                ok = false;
+                break;
             }
+            float all = 0.f, ray = 0.f;
+            lv_batch_stats(b, nullptr, 0, &all, &ray);
+            if (r > 0)
+                total += ray;
+        }
+        if (ok && total / reps < best_ms)
+        {
+            best_ms = total / reps;
+            best = cfg;
+        }
+    }
     lv_batch_set_config(b, &best);
     if (chosen)
         *chosen = best;

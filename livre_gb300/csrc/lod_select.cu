@@ -538,7 +538,11 @@ lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* dviews
 
 lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaStream_t s)
 {
-    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(nodes, 64), 1u << 24);
+    /* grow to powers of two: few reallocations (each one drops the graphs
+     * captured on the old queues) */
+    uint64_t cap = 64;
+    while (cap < nodes && cap < (1u << 24))
+        cap <<= 1;
     if (S.frontier_capacity >= cap)
         return LV_OK;
     LV_CUDA(ctx, cudaStreamSynchronize(s));

@@ -108,6 +108,7 @@ enum FrameCounter
     FC_ERROR = 8,         /* nonzero: an index check failed in a kernel */
     FC_KEPT = 9,          /* rendering-set entries left after dropping the
                              ones with an ancestor in the set */
+    FC_QUEUE = 10,        /* tile queue head of the single-view ray cast */
     FC_WORDS = 16
 };
 

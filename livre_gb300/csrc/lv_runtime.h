@@ -119,6 +119,7 @@ struct lv_ctx
     lv::Pool* pool = nullptr;
     lv::Renderer* renderer = nullptr;
     size_t pool_bytes = size_t(3072) << 20;
+    lv_render_launch launch{0, 0, 0}; /* lv_render's ray-cast launch shape */
     std::mutex mutex;
 };
 
@@ -245,8 +246,8 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
                         uint32_t* leaf, uint32_t* counters, RayView& V);
 /* Index of the ray-cast kernel instantiation for a view. */
 int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge);
-lv_status launch_persistent(lv_ctx* ctx, int variant, int tf_shared, const RayView* d_rays,
-                            const TileQueue& Q, uint32_t ctas, uint32_t tfn_max,
+lv_status launch_persistent(lv_ctx* ctx, int variant, const lv_batch_config& cfg,
+                            const RayView* d_rays, const TileQueue& Q, uint32_t tfn_max,
                             cudaStream_t s);
 lv_status launch_resolve_views(lv_ctx* ctx, const ResolveView* d_views,
                                uint32_t n_views, cudaStream_t s);

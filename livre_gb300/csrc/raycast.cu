@@ -24,6 +24,8 @@
  * intrinsics in a fixed order, so every sample reads the same voxels as the
  * CPU oracle; shading runs in FP32 with fused multiply-adds.
  */
+#include <algorithm>
+
 #include "lv_runtime.h"
 
 namespace lv
@@ -438,94 +440,134 @@ __device__ __forceinline__ RayGeom ray_setup(const RayView& V, uint32_t px,
     return g;
 }
 
+/* State of one ray between two samples, so that a lane can take a number of
+ * samples, stop, and go on later (the refill kernels below). */
+struct RayState
+{
+    float dir[3];
+    float tg, thi;
+    float kf;            /* index of the next sample (exact in FP32 below 2^24) */
+    float4 dst;
+    uint32_t cur, entry; /* leaf cell of the last sample and its entry */
+    const uint8_t* brick;
+    float vs[3], off[3];
+};
+
+/* First sample on the global grid at or after tlo; false: no sample. */
+__device__ __forceinline__ bool ray_begin(const RayGeom& g, float step, RayState& r)
+{
+    r.dst = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!g.hit || !(g.tlo <= g.thi))
+        return false;
+    int k = 0;
+    if (g.tlo > g.tg)
+        k = int(ceilf(__fdiv_rn(__fsub_rn(g.tlo, g.tg), step)));
+    r.kf = __int2float_rn(k);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        r.dir[a] = g.dir[a];
+        r.vs[a] = 0.f;
+        r.off[a] = 0.f;
+    }
+    r.tg = g.tg;
+    r.thi = g.thi;
+    r.cur = 0xFFFFFFFFu;
+    r.entry = kLeafEmpty;
+    r.brick = nullptr;
+    return true;
+}
+
+/* One sample of the ray: returns false once the ray has left its segment or
+ * reached the early-termination opacity. */
+template <int DT, int FILTER, int TFS, int EDGE>
+__device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float step, float ac,
+                                         const float dimf[3], uint32_t& nsamp)
+{
+    /* sample position, cell and slot coordinate: single-rounding FMAs in a
+     * fixed order (the CPU oracle evaluates the same fmaf chain) */
+    const float t = fmaf(r.kf, step, r.tg);
+    if (!(t < r.thi))
+        return false;
+    r.kf += 1.0f;
+    float f[3];
+    int c[3];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        const float p = fmaf(r.dir[a], t, V.eye[a]);
+        f[a] = fmaf(p, V.gscale[a], V.goff[a]);
+        const float fl = floorf(f[a]);
+        inside = inside && (fl >= 0.0f) && (fl < dimf[a]);
+        c[a] = int(fl);
+    }
+    if (!inside)
+        return true;
+    const uint32_t lin =
+        (uint32_t(c[2]) * V.dims[1] + uint32_t(c[1])) * V.dims[0] + uint32_t(c[0]);
+    if (lin != r.cur)
+    {
+        r.cur = lin;
+        uint32_t entry = __ldg(V.leaf + lin);
+        if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
+                                    (entry >> kLeafSlotBits) > V.Lf))
+        {
+            atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
+            entry = kLeafEmpty;
+        }
+        r.entry = entry;
+        if (entry != kLeafEmpty)
+        {
+            const float half_texel = FILTER == LV_FILTER_TRILINEAR ? 0.5f : 0.0f;
+            const uint32_t L = entry >> kLeafSlotBits;
+            const uint32_t slot = entry & kLeafSlotMask;
+            const uint32_t sh = V.Lf - L;
+            r.brick = V.pool + uint64_t(slot) * kSlotUnit;
+            const float inv_side = __int_as_float(int(127u - sh) << 23); /* 2^-sh */
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                r.vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
+                r.off[a] = (__uint2float_rn(V.O[a]) -
+                            __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a])) -
+                           half_texel; /* exact */
+            }
+        }
+    }
+    if (r.entry == kLeafEmpty)
+        return true;
+    float sc[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        sc[a] = fmaf(f[a], r.vs[a], r.off[a]);
+    const float value = sample_brick<DT, FILTER, EDGE>(V, r.brick, sc);
+    const float dens = fmaf(value, V.dmul, V.dadd);
+    const float4 src = tf_lookup<TFS>(V, dens);
+    const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
+    const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
+    const float w = alpha * (1.0f - r.dst.w);
+    r.dst.x = fmaf(src.x, w, r.dst.x);
+    r.dst.y = fmaf(src.y, w, r.dst.y);
+    r.dst.z = fmaf(src.z, w, r.dst.z);
+    r.dst.w = fmaf(alpha, 1.0f - r.dst.w, r.dst.w);
+    ++nsamp;
+    return !(r.dst.w > V.early);
+}
+
 template <int DT, int FILTER, int TFS, int EDGE>
 __device__ float4 march(const RayView& V, const RayGeom& g, float step,
                         float ac, uint32_t& nsamp)
 {
-    float4 dst = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!g.hit || !(g.tlo <= g.thi))
-        return dst;
-    int k = 0;
-    if (g.tlo > g.tg)
-        k = int(ceilf(__fdiv_rn(__fsub_rn(g.tlo, g.tg), step)));
+    RayState r;
+    if (!ray_begin(g, step, r))
+        return r.dst;
     const float dimf[3] = {__uint2float_rn(V.dims[0]), __uint2float_rn(V.dims[1]),
                            __uint2float_rn(V.dims[2])};
-    uint32_t cur = 0xFFFFFFFFu, entry = kLeafEmpty;
-    const uint8_t* brick = nullptr;
-    float vs[3] = {0.f, 0.f, 0.f}, off[3] = {0.f, 0.f, 0.f};
-    const float early = V.early;
-    const float half_texel = FILTER == LV_FILTER_TRILINEAR ? 0.5f : 0.0f;
-    for (;; ++k)
+    while (ray_step<DT, FILTER, TFS, EDGE>(V, r, step, ac, dimf, nsamp))
     {
-        /* sample position, cell and slot coordinate: single-rounding FMAs in
-         * a fixed order (the CPU oracle evaluates the same fmaf chain) */
-        const float t = fmaf(__int2float_rn(k), step, g.tg);
-        if (!(t < g.thi))
-            break;
-        float f[3];
-        int c[3];
-        bool inside = true;
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-        {
-            const float p = fmaf(g.dir[a], t, V.eye[a]);
-            f[a] = fmaf(p, V.gscale[a], V.goff[a]);
-            const float fl = floorf(f[a]);
-            inside = inside && (fl >= 0.0f) && (fl < dimf[a]);
-            c[a] = int(fl);
-        }
-        if (!inside)
-            continue;
-        const uint32_t lin =
-            (uint32_t(c[2]) * V.dims[1] + uint32_t(c[1])) * V.dims[0] + uint32_t(c[0]);
-        if (lin != cur)
-        {
-            cur = lin;
-            entry = __ldg(V.leaf + lin);
-            if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
-                                        (entry >> kLeafSlotBits) > V.Lf))
-            {
-                atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
-                entry = kLeafEmpty;
-            }
-            if (entry != kLeafEmpty)
-            {
-                const uint32_t L = entry >> kLeafSlotBits;
-                const uint32_t slot = entry & kLeafSlotMask;
-                const uint32_t sh = V.Lf - L;
-                brick = V.pool + uint64_t(slot) * kSlotUnit;
-                const float inv_side = __int_as_float(int(127u - sh) << 23); /* 2^-sh */
-#pragma unroll
-                for (int a = 0; a < 3; ++a)
-                {
-                    vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
-                    off[a] = (__uint2float_rn(V.O[a]) -
-                              __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a])) -
-                             half_texel; /* exact */
-                }
-            }
-        }
-        if (entry == kLeafEmpty)
-            continue;
-        float sc[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-            sc[a] = fmaf(f[a], vs[a], off[a]);
-        const float value = sample_brick<DT, FILTER, EDGE>(V, brick, sc);
-        const float dens = fmaf(value, V.dmul, V.dadd);
-        const float4 src = tf_lookup<TFS>(V, dens);
-        const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
-        const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
-        const float w = alpha * (1.0f - dst.w);
-        dst.x = fmaf(src.x, w, dst.x);
-        dst.y = fmaf(src.y, w, dst.y);
-        dst.z = fmaf(src.z, w, dst.z);
-        dst.w = fmaf(alpha, 1.0f - dst.w, dst.w);
-        ++nsamp;
-        if (dst.w > early)
-            break;
     }
-    return dst;
+    return r.dst;
 }
 
 template <int DT, int FILTER, int EDGE>
@@ -637,6 +679,208 @@ __global__ void __launch_bounds__(256)
         atomicMax(Q.clock + 1, globaltimer());
 }
 
+/* ---------------------------------------------------------------- refill
+ * Persistent ray cast with lane refill. Every warp takes tile_w x tile_h
+ * pixel tiles from a device queue (one atomic per tile) and hands the tile's
+ * pixels to its lanes in order; a lane whose ray has finished takes the next
+ * pixel at the next check (every `checks` samples), so lanes do not idle
+ * while the longest ray of their warp finishes. When a tile runs out, the
+ * warp takes the next one of the same view without waiting for its lanes;
+ * a tile of another view (batched launch) is started once the warp has
+ * drained. Each ray takes exactly the samples of march() in the same
+ * order, so the image is identical to the one-thread-per-pixel kernel's. */
+constexpr uint32_t kRefillThreads = 128;
+constexpr uint32_t kRefillMinCtas = 8; /* 32 warps per SM: at most 64 registers */
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+constexpr uint32_t kNoItem = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t warp_pop(uint32_t* head)
+{
+    uint32_t v = 0;
+    if ((threadIdx.x & 31u) == 0)
+        v = atomicAdd(head, 1u);
+    return __shfl_sync(kFull, v, 0);
+}
+
+/* group view of a work item: tile_start is ascending, tile_start[0] = 0 */
+__device__ __forceinline__ uint32_t find_view(const TileQueue& Q, uint32_t n_views,
+                                              uint32_t item)
+{
+    uint32_t lo = 0, hi = n_views;
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (Q.tile_start[mid] <= item)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void load_view(RayView* dst, const RayView* src)
+{
+    __syncwarp();
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (uint32_t w = threadIdx.x & 31u; w < sizeof(RayView) / 4; w += 32)
+        d[w] = s[w];
+    __syncwarp();
+}
+
+__device__ __forceinline__ void flush_samples(const RayView& V, uint32_t nsamp)
+{
+    unsigned long long s = nsamp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        s += __shfl_down_sync(kFull, s, o);
+    if ((threadIdx.x & 31u) == 0 && s)
+        atomicAdd(reinterpret_cast<unsigned long long*>(V.counters + FC_SAMPLES_LO), s);
+}
+
+struct ViewConsts
+{
+    float step, ac, dimf[3];
+    uint32_t tiles_x;
+};
+
+__device__ __forceinline__ ViewConsts view_consts(const RayView& V, uint32_t tile_w)
+{
+    ViewConsts k;
+    const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
+    k.step = __fdiv_rn(1.0f, __uint2float_rn(n));
+    k.ac = __fdiv_rn(32.0f, __uint2float_rn(n));
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        k.dimf[a] = __uint2float_rn(V.dims[a]);
+    k.tiles_x = (V.W + tile_w - 1) / tile_w;
+    return k;
+}
+
+/* MULTI: V is this warp's shared copy `sv` of the current view, reloaded
+ * from `views` on a view change; else V is the launch's single view. */
+template <int DT, int FILTER, int EDGE, bool MULTI>
+__device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
+                                            const RayView* __restrict__ views,
+                                            const TileQueue& Q, uint32_t* head,
+                                            uint32_t n_views, uint32_t total, uint32_t checks)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t below = (1u << lane) - 1u;
+    const uint32_t tw = Q.tile_w, th = Q.tile_h, npix = tw * th;
+    uint32_t item = warp_pop(head);
+    if (item >= total)
+        return;
+    uint32_t gv = 0;
+    if (MULTI)
+    {
+        gv = find_view(Q, n_views, item);
+        load_view(sv, views + Q.view_ids[gv]);
+    }
+    ViewConsts K = view_consts(V, tw);
+    uint32_t tile = item - (MULTI ? Q.tile_start[gv] : 0u);
+    uint32_t next = 0, pending = kNoItem;
+    bool exhausted = false, active = false;
+    uint32_t px = 0, py = 0, nsamp = 0;
+    RayState r;
+    for (;;)
+    {
+        /* hand the tile's next pixels to idle lanes, in lane order */
+        for (;;)
+        {
+            const uint32_t idle = __ballot_sync(kFull, !active);
+            if (!idle)
+                break;
+            if (next >= npix)
+            {
+                if (exhausted || pending != kNoItem)
+                    break;
+                const uint32_t nitem = warp_pop(head);
+                if (nitem >= total)
+                {
+                    exhausted = true;
+                    break;
+                }
+                if (MULTI && find_view(Q, n_views, nitem) != gv)
+                {
+                    pending = nitem; /* another view: drain first */
+                    break;
+                }
+                tile = nitem - (MULTI ? Q.tile_start[gv] : 0u);
+                next = 0;
+            }
+            const uint32_t mine = next + __popc(idle & below);
+            next = min(next + uint32_t(__popc(idle)), npix);
+            if (!active && mine < npix)
+            {
+                px = (tile % K.tiles_x) * tw + mine % tw;
+                py = (tile / K.tiles_x) * th + mine / tw;
+                if (px < V.W && py < V.H)
+                {
+                    const RayGeom g = ray_setup(V, px, py);
+                    active = ray_begin(g, K.step, r);
+                    if (!active)
+                        V.out[uint64_t(py) * V.W + px] = r.dst;
+                }
+            }
+        }
+        if (!__any_sync(kFull, active))
+        {
+            if (MULTI && pending != kNoItem)
+            {
+                flush_samples(V, nsamp);
+                nsamp = 0;
+                gv = find_view(Q, n_views, pending);
+                load_view(sv, views + Q.view_ids[gv]);
+                K = view_consts(V, tw);
+                tile = pending - Q.tile_start[gv];
+                pending = kNoItem;
+                next = 0;
+                continue;
+            }
+            break; /* queue exhausted and every lane done */
+        }
+        if (active)
+            for (uint32_t k = 0; k < checks; ++k)
+                if (!ray_step<DT, FILTER, 0, EDGE>(V, r, K.step, K.ac, K.dimf, nsamp))
+                {
+                    active = false;
+                    V.out[uint64_t(py) * V.W + px] = r.dst;
+                    break;
+                }
+    }
+    flush_samples(V, nsamp);
+}
+
+/* Single view (lv_render): the queue head is the view's FC_QUEUE counter. */
+template <int DT, int FILTER, int EDGE>
+__global__ void __launch_bounds__(kRefillThreads, kRefillMinCtas)
+    raycast_refill_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h, uint32_t checks)
+{
+    TileQueue Q{};
+    Q.tile_w = tile_w;
+    Q.tile_h = tile_h;
+    const uint32_t tiles = ((V.W + tile_w - 1) / tile_w) * ((V.H + tile_h - 1) / tile_h);
+    refill_body<DT, FILTER, EDGE, false>(V, nullptr, nullptr, Q, V.counters + FC_QUEUE, 1u,
+                                         tiles, checks);
+}
+
+/* Batched: tiles of many views of one kernel variant. */
+template <int DT, int FILTER, int EDGE>
+__global__ void __launch_bounds__(kRefillThreads, kRefillMinCtas)
+    raycast_refill_views_kernel(const RayView* __restrict__ views, TileQueue Q, uint32_t checks)
+{
+    __shared__ RayView sV[kRefillThreads / 32];
+    if (threadIdx.x == 0)
+        atomicCAS(Q.clock, 0ull, globaltimer());
+    const uint32_t n_views = *Q.n_views;
+    RayView* sv = sV + (threadIdx.x >> 5);
+    refill_body<DT, FILTER, EDGE, true>(*sv, sv, views, Q, Q.head, n_views,
+                                        Q.tile_start[n_views], checks);
+    if ((threadIdx.x & 31u) == 0)
+        atomicMax(Q.clock + 1, globaltimer());
+}
+
 __global__ void to_rgba8_kernel(const float4* __restrict__ in,
                                 uchar4* __restrict__ out, uint64_t n)
 {
@@ -675,16 +919,72 @@ lv_status launch_leaf_fill(lv_ctx* ctx, const ResolveView& R, cudaStream_t s)
 
 namespace
 {
-/* One instantiation per (voxel type, filter, TF staging, edge clamping). */
+/* CTAs of `kernel` resident on the whole GPU at once (occupancy API). */
+template <typename K>
+uint32_t resident_ctas(lv_ctx* ctx, K kernel, int threads, size_t smem)
+{
+    int per_sm = 0, sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
+            cudaSuccess ||
+        per_sm < 1)
+    {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return uint32_t(per_sm) * uint32_t(sms);
+}
+
+/* One instantiation per (voxel type, filter, TF staging, edge clamping);
+ * ctas = 0: as many CTAs as are resident at once. */
 template <int DT, int F, int TFS, int EDGE>
 lv_status persistent_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
-                              uint32_t grid, size_t smem, cudaStream_t s)
+                              uint32_t ctas, size_t smem, cudaStream_t s)
 {
     auto k = raycast_persistent_kernel<DT, F, TFS, EDGE>;
     if (smem > 48 * 1024)
         LV_CUDA(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           int(smem)));
-    k<<<grid, Q.tile_w * Q.tile_h, smem, s>>>(d_rays, Q);
+    const int threads = int(Q.tile_w * Q.tile_h);
+    uint32_t grid = resident_ctas(ctx, k, threads, smem);
+    if (ctas)
+    {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        grid = uint32_t(sms) * ctas;
+    }
+    k<<<grid, threads, smem, s>>>(d_rays, Q);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+template <int DT, int F, int EDGE>
+lv_status refill_views_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
+                                uint32_t ctas, uint32_t checks, cudaStream_t s)
+{
+    auto k = raycast_refill_views_kernel<DT, F, EDGE>;
+    uint32_t grid = resident_ctas(ctx, k, kRefillThreads, 0);
+    if (ctas)
+    {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        grid = uint32_t(sms) * ctas;
+    }
+    k<<<grid, kRefillThreads, 0, s>>>(d_rays, Q, checks);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+template <int DT, int F, int EDGE>
+lv_status refill_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                          cudaStream_t s)
+{
+    auto k = raycast_refill_kernel<DT, F, EDGE>;
+    const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
+    const uint32_t warps = kRefillThreads / 32;
+    const uint32_t grid = std::max(1u, std::min(resident_ctas(ctx, k, kRefillThreads, 0),
+                                                (tiles + warps - 1) / warps));
+    k<<<grid, kRefillThreads, 0, s>>>(V, L.tile_w, L.tile_h, L.samples_per_check);
     LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;
 }
@@ -700,18 +1000,34 @@ lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, dim3 grid, dim3 block, c
 /* combination index: dtype (u8 0 / u16 1), filter, edge */
 template <int TFS>
 lv_status persistent_by_index(int idx, lv_ctx* ctx, const RayView* d, const TileQueue& Q,
-                              uint32_t grid, size_t smem, cudaStream_t s)
+                              uint32_t ctas, size_t smem, cudaStream_t s)
 {
     switch (idx)
     {
-    case 0: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 0>(ctx, d, Q, grid, smem, s);
-    case 1: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 1>(ctx, d, Q, grid, smem, s);
-    case 2: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 0>(ctx, d, Q, grid, smem, s);
-    case 3: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 1>(ctx, d, Q, grid, smem, s);
-    case 4: return persistent_dispatch<LV_DT_UINT16, 0, TFS, 0>(ctx, d, Q, grid, smem, s);
-    case 5: return persistent_dispatch<LV_DT_UINT16, 0, TFS, 1>(ctx, d, Q, grid, smem, s);
-    case 6: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 0>(ctx, d, Q, grid, smem, s);
-    default: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 1>(ctx, d, Q, grid, smem, s);
+    case 0: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 0>(ctx, d, Q, ctas, smem, s);
+    case 1: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 1>(ctx, d, Q, ctas, smem, s);
+    case 2: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 0>(ctx, d, Q, ctas, smem, s);
+    case 3: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 1>(ctx, d, Q, ctas, smem, s);
+    case 4: return persistent_dispatch<LV_DT_UINT16, 0, TFS, 0>(ctx, d, Q, ctas, smem, s);
+    case 5: return persistent_dispatch<LV_DT_UINT16, 0, TFS, 1>(ctx, d, Q, ctas, smem, s);
+    case 6: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 0>(ctx, d, Q, ctas, smem, s);
+    default: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 1>(ctx, d, Q, ctas, smem, s);
+    }
+}
+
+lv_status refill_views_by_index(int idx, lv_ctx* ctx, const RayView* d, const TileQueue& Q,
+                                uint32_t ctas, uint32_t checks, cudaStream_t s)
+{
+    switch (idx)
+    {
+    case 0: return refill_views_dispatch<LV_DT_UINT8, 0, 0>(ctx, d, Q, ctas, checks, s);
+    case 1: return refill_views_dispatch<LV_DT_UINT8, 0, 1>(ctx, d, Q, ctas, checks, s);
+    case 2: return refill_views_dispatch<LV_DT_UINT8, 1, 0>(ctx, d, Q, ctas, checks, s);
+    case 3: return refill_views_dispatch<LV_DT_UINT8, 1, 1>(ctx, d, Q, ctas, checks, s);
+    case 4: return refill_views_dispatch<LV_DT_UINT16, 0, 0>(ctx, d, Q, ctas, checks, s);
+    case 5: return refill_views_dispatch<LV_DT_UINT16, 0, 1>(ctx, d, Q, ctas, checks, s);
+    case 6: return refill_views_dispatch<LV_DT_UINT16, 1, 0>(ctx, d, Q, ctas, checks, s);
+    default: return refill_views_dispatch<LV_DT_UINT16, 1, 1>(ctx, d, Q, ctas, checks, s);
     }
 }
 } // namespace
@@ -729,9 +1045,23 @@ lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
     step_kernel<<<1, 1, 0, s>>>(V.counters, V.samples_fixed, V.step_policy,
                                 V.max_voxel_dim, V.depth);
     LV_CUDA(ctx, cudaGetLastError());
+    const lv_render_launch L = ctx->launch;
+    const int variant = kernel_variant(V.dtype, V.filter, V.edge);
+    if (L.tile_w)
+        switch (variant)
+        {
+        case 0: return refill_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, L, s);
+        case 1: return refill_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, L, s);
+        case 2: return refill_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, L, s);
+        case 3: return refill_dispatch<LV_DT_UINT8, 1, 1>(ctx, V, L, s);
+        case 4: return refill_dispatch<LV_DT_UINT16, 0, 0>(ctx, V, L, s);
+        case 5: return refill_dispatch<LV_DT_UINT16, 0, 1>(ctx, V, L, s);
+        case 6: return refill_dispatch<LV_DT_UINT16, 1, 0>(ctx, V, L, s);
+        default: return refill_dispatch<LV_DT_UINT16, 1, 1>(ctx, V, L, s);
+        }
     const dim3 block(8, 16);
     const dim3 grid((V.W + block.x - 1) / block.x, (V.H + block.y - 1) / block.y);
-    switch (kernel_variant(V.dtype, V.filter, V.edge))
+    switch (variant)
     {
     case 0: return plain_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, grid, block, s);
     case 1: return plain_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, grid, block, s);
@@ -755,17 +1085,17 @@ lv_status launch_views_pipeline(lv_ctx* ctx, const ResolveView* d_resolve,
     return LV_OK;
 }
 
-lv_status launch_persistent(lv_ctx* ctx, int variant, int tf_shared, const RayView* d_rays,
-                            const TileQueue& Q, uint32_t ctas, uint32_t tfn_max,
+lv_status launch_persistent(lv_ctx* ctx, int variant, const lv_batch_config& cfg,
+                            const RayView* d_rays, const TileQueue& Q, uint32_t tfn_max,
                             cudaStream_t s)
 {
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const uint32_t grid = uint32_t(sms) * ctas;
-    const size_t smem = tf_shared ? size_t(tfn_max) * 2 * sizeof(float4) : 0;
-    if (tf_shared)
-        return persistent_by_index<1>(variant, ctx, d_rays, Q, grid, smem, s);
-    return persistent_by_index<0>(variant, ctx, d_rays, Q, grid, smem, s);
+    if (cfg.queue == LV_QUEUE_WARP_REFILL)
+        return refill_views_by_index(variant, ctx, d_rays, Q, cfg.ctas_per_sm,
+                                     cfg.samples_per_check, s);
+    const size_t smem = cfg.tf_shared ? size_t(tfn_max) * 2 * sizeof(float4) : 0;
+    if (cfg.tf_shared)
+        return persistent_by_index<1>(variant, ctx, d_rays, Q, cfg.ctas_per_sm, smem, s);
+    return persistent_by_index<0>(variant, ctx, d_rays, Q, cfg.ctas_per_sm, smem, s);
 }
 
 } // namespace lv

@@ -901,6 +901,29 @@ lv_status process_pending(lv_ctx* ctx, cudaStream_t s)
 } // namespace
 } // namespace lv
 
+extern "C" lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* cfg)
+{
+    if (!ctx || !cfg)
+        return LV_EINVAL;
+    const uint32_t pixels = cfg->tile_w * cfg->tile_h;
+    if (cfg->tile_w && (pixels < 32 || pixels > 1024 || cfg->samples_per_check == 0 ||
+                        cfg->samples_per_check > 64))
+        return fail(ctx, LV_EINVAL,
+                    "render launch: 32..1024 pixels per tile, samples_per_check in 1..64");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    ctx->launch = *cfg;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_get_render_launch(lv_ctx* ctx, lv_render_launch* cfg)
+{
+    if (!ctx || !cfg)
+        return LV_EINVAL;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    *cfg = ctx->launch;
+    return LV_OK;
+}
+
 extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                                const lv_render_desc* desc, float* d_rgba,
                                void* stream)

@@ -100,6 +100,7 @@ struct lv_server
     uint64_t vis_stride = 0;
     /* counters */
     uint64_t n_done = 0, n_batches = 0;
+    lv_server_profile prof{};
 };
 
 namespace
@@ -110,8 +111,9 @@ void complete(lv_server* S, Inflight& f)
     if (f.clock && f.clock->t.load() > 0.0)
         t = f.clock->t.load();
     std::vector<lv_frame_stats> st(f.reqs.size());
+    float batch_ms = 0.f, ray_ms = 0.f;
     if (f.batch && !f.reqs.empty())
-        lv_batch_stats(f.batch, st.data(), uint32_t(st.size()), nullptr, nullptr);
+        lv_batch_stats(f.batch, st.data(), uint32_t(st.size()), &batch_ms, &ray_ms);
     {
         std::lock_guard<std::mutex> lk(S->ctx->mutex);
         for (Req* r : f.reqs)
@@ -124,6 +126,9 @@ void complete(lv_server* S, Inflight& f)
         }
     }
     std::lock_guard<std::mutex> lk(S->m);
+    S->prof.device_ms += batch_ms;
+    S->prof.raycast_ms += ray_ms;
+    S->prof.requests += f.reqs.size();
     for (size_t i = 0; i < f.reqs.size(); ++i)
     {
         Req* r = f.reqs[i];
@@ -137,6 +142,20 @@ void complete(lv_server* S, Inflight& f)
     if (f.ev)
         S->free_events.push_back(f.ev);
     S->cv_done.notify_all();
+}
+
+void add_time(lv_server* S, double lv_server_profile::*field, double ms)
+{
+    std::lock_guard<std::mutex> lk(S->m);
+    S->prof.*field += ms;
+}
+
+/* Blocks until an in-flight batch finishes (server thread). */
+void wait_batch(lv_server* S, cudaEvent_t ev)
+{
+    const double t0 = now_ms();
+    cudaEventSynchronize(ev);
+    add_time(S, &lv_server_profile::wait_ms, now_ms() - t0);
 }
 
 void fail_request(lv_server* S, Req* r, lv_status st)
@@ -237,7 +256,9 @@ void admit(lv_server* S, std::vector<Req*>& cand, std::vector<Req*>& admitted,
            std::vector<Req*>& rejected)
 {
     std::vector<std::vector<uint64_t>> vis;
+    const double t0 = now_ms();
     lv_status st = dry_run(S, cand, vis);
+    add_time(S, &lv_server_profile::select_ms, now_ms() - t0);
     if (st != LV_OK)
     {
         rejected = cand;
@@ -286,8 +307,10 @@ void admit(lv_server* S, std::vector<Req*>& cand, std::vector<Req*>& admitted,
         }
         uint32_t loaded = 0;
         uint64_t bytes = 0;
+        const double t1 = now_ms();
         st = stream_bricks(ctx, v, missing.data(), uint32_t(missing.size()), 0xFFFFFFFFu,
                            S->sel_stream, loaded, bytes);
+        add_time(S, &lv_server_profile::stream_ms, now_ms() - t1);
         /* bricks that became resident while pinned now count as pinned */
         for (uint64_t idx : missing_idx)
             if (v->host_table[idx] >= 0 && v->pins[idx] > 0)
@@ -330,7 +353,7 @@ void loop_batched(lv_server* S)
                     Inflight f = S->inflight.front();
                     S->inflight.pop_front();
                     lk.unlock();
-                    cudaEventSynchronize(f.ev);
+                    wait_batch(S, f.ev);
                     complete(S, f);
                     continue;
                 }
@@ -344,12 +367,20 @@ void loop_batched(lv_server* S)
                 Inflight f = S->inflight.front();
                 S->inflight.pop_front();
                 lk.unlock();
-                cudaEventSynchronize(f.ev);
+                wait_batch(S, f.ev);
                 complete(S, f);
                 continue;
             }
+            uint64_t pixels = 0;
             for (size_t i = 0; i < S->queue.size() && cand.size() < S->cfg.max_batch; ++i)
+            {
+                const lv_render_desc& d = S->queue[i]->r.desc;
+                const uint64_t p = uint64_t(d.width) * d.height;
+                if (!cand.empty() && S->cfg.max_pixels && pixels + p > S->cfg.max_pixels)
+                    break;
+                pixels += p;
                 cand.push_back(S->queue[i]);
+            }
         }
         std::vector<Req*> admitted, rejected;
         {
@@ -376,7 +407,7 @@ void loop_batched(lv_server* S)
                 Inflight f = S->inflight.front();
                 S->inflight.pop_front();
                 lk.unlock();
-                cudaEventSynchronize(f.ev);
+                wait_batch(S, f.ev);
                 complete(S, f);
             }
             else if (!rejected.size())
@@ -402,7 +433,9 @@ void loop_batched(lv_server* S)
         lv_batch* b = S->batches[S->cur];
         S->cur ^= 1;
         cudaStreamWaitEvent(S->launch_stream, S->uploads_done, 0);
+        const double t_launch = now_ms();
         const lv_status st = lv_batch_render(b, bv.data(), uint32_t(bv.size()), S->launch_stream);
+        add_time(S, &lv_server_profile::launch_ms, now_ms() - t_launch);
         Inflight f;
         f.batch = b;
         {
@@ -449,10 +482,15 @@ void loop_plain(lv_server* S)
         r->batch_size = 1;
         lv_render_desc d = r->r.desc;
         d.synchronous = 1;
+        const double t0 = now_ms();
         lv_status st = lv_render(S->ctx, r->r.volume, r->r.tf, &d, r->r.d_rgba, S->launch_stream);
         if (st == LV_OK)
             st = lv_last_stats(S->ctx, &r->stats); /* synchronises */
         std::lock_guard<std::mutex> lk(S->m);
+        S->prof.launch_ms += now_ms() - t0;
+        S->prof.device_ms += r->stats.select_ms + r->stats.raycast_ms;
+        S->prof.raycast_ms += r->stats.raycast_ms;
+        ++S->prof.requests;
         r->status = st;
         r->t_done = now_ms();
         r->done = true;
@@ -479,7 +517,11 @@ extern "C" lv_status lv_server_create(lv_ctx* ctx, const lv_server_config* cfg, 
     lv_server* S = new lv_server();
     S->ctx = ctx;
     S->cfg = *cfg;
-    if (cudaStreamCreateWithFlags(&S->sel_stream, cudaStreamNonBlocking) != cudaSuccess ||
+    /* admission selections take the next free SM slots ahead of batch work */
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    if (cudaStreamCreateWithPriority(&S->sel_stream, cudaStreamNonBlocking, hi_prio) !=
+            cudaSuccess ||
         cudaStreamCreateWithFlags(&S->launch_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&S->uploads_done, cudaEventDisableTiming) != cudaSuccess)
     {
@@ -557,6 +599,24 @@ extern "C" lv_status lv_server_wait(lv_server* S, uint64_t ticket, uint32_t time
     out->stats = r->stats;
     S->reqs.erase(it);
     delete r;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_server_get_profile(lv_server* S, lv_server_profile* out)
+{
+    if (!S || !out)
+        return LV_EINVAL;
+    uint64_t captures = 0;
+    for (lv_batch* b : S->batches)
+    {
+        uint64_t c = 0;
+        if (b && lv_batch_graph_stats(b, &c, nullptr, nullptr) == LV_OK)
+            captures += c;
+    }
+    std::lock_guard<std::mutex> lk(S->m);
+    *out = S->prof;
+    out->batches = S->n_batches;
+    out->graph_captures = captures;
     return LV_OK;
 }
 
