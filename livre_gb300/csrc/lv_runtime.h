@@ -119,7 +119,8 @@ struct lv_ctx
     lv::Pool* pool = nullptr;
     lv::Renderer* renderer = nullptr;
     size_t pool_bytes = size_t(3072) << 20;
-    lv_render_launch launch{0, 0, 0}; /* lv_render's ray-cast launch shape */
+    /* lv_render's ray cast */
+    lv_render_launch launch{LV_LAUNCH_TILE_QUEUE, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 0};
     std::mutex mutex;
 };
 
@@ -213,6 +214,7 @@ struct Renderer
 {
     DeviceBuffer visible, sel_result, render_ids, render_slots, missing,
         counters, leaf, pairs;
+    DeviceBuffer tiles; /* longest-first tile order: bucket counts, keys, order */
     PinnedBuffer h_counters, h_missing, h_pairs;
     uint64_t visible_capacity = 0;
     uint32_t frame = 0;

@@ -25,6 +25,7 @@
  * CPU oracle; shading runs in FP32 with fused multiply-adds.
  */
 #include <algorithm>
+#include <cmath>
 
 #include "lv_runtime.h"
 
@@ -265,16 +266,24 @@ __device__ __forceinline__ float ldv(const uint8_t* p)
     return float(__ldg(p));
 }
 
-/* Voxel value at slot coordinate s (nearest: s = local position; trilinear:
+/* The voxels a sample reads and its interpolation weights; loaded one
+ * sample ahead of the compositing (march) so that the loads of the next
+ * sample are in flight while the current one is composited. */
+template <int FILTER>
+struct Taps
+{
+    static constexpr int N = FILTER == LV_FILTER_TRILINEAR ? 8 : 1;
+    float c[N];
+    float fx, fy, fz;
+};
+
+/* Voxels around slot coordinate s (nearest: s = local position; trilinear:
  * s = local position - 0.5, texel centres on integers). EDGE = 1 clamps every
  * tap to the brick (GL_CLAMP_TO_EDGE, needed without overlap); EDGE = 0 uses
- * one base address and immediate offsets, valid when every overlap >= 1
- * keeps both taps inside the brick (the base is still clamped so no access
- * can leave the slot). */
+ * one base address and immediate offsets, valid when every overlap >= 1. */
 template <int DT, int FILTER, int EDGE>
-__device__ __forceinline__ float sample_brick(const RayView& V,
-                                              const uint8_t* brick,
-                                              const float s[3])
+__device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick,
+                                          const float s[3], Taps<FILTER>& T)
 {
     constexpr int bpv = DT == LV_DT_UINT16 ? 2 : 1;
     const int n0 = int(V.N[0]), n1 = int(V.N[1]), n2 = int(V.N[2]);
@@ -283,12 +292,14 @@ __device__ __forceinline__ float sample_brick(const RayView& V,
         const int x = min(max(int(floorf(s[0])), 0), n0 - 1);
         const int y = min(max(int(floorf(s[1])), 0), n1 - 1);
         const int z = min(max(int(floorf(s[2])), 0), n2 - 1);
-        return ldv<DT>(brick + ((z * n1 + y) * n0 + x) * bpv);
+        T.c[0] = ldv<DT>(brick + ((z * n1 + y) * n0 + x) * bpv);
+        return;
     }
     const float fx0 = floorf(s[0]), fy0 = floorf(s[1]), fz0 = floorf(s[2]);
-    const float fx = s[0] - fx0, fy = s[1] - fy0, fz = s[2] - fz0;
-    int ix = int(fx0), iy = int(fy0), iz = int(fz0);
-    float c000, c001, c010, c011, c100, c101, c110, c111;
+    T.fx = s[0] - fx0;
+    T.fy = s[1] - fy0;
+    T.fz = s[2] - fz0;
+    const int ix = int(fx0), iy = int(fy0), iz = int(fz0);
     if (EDGE)
     {
         const int x0 = min(max(ix, 0), n0 - 1), x1 = min(max(ix + 1, 0), n0 - 1);
@@ -296,51 +307,64 @@ __device__ __forceinline__ float sample_brick(const RayView& V,
         const int z0 = min(max(iz, 0), n2 - 1), z1 = min(max(iz + 1, 0), n2 - 1);
         const int r00 = (z0 * n1 + y0) * n0, r01 = (z0 * n1 + y1) * n0;
         const int r10 = (z1 * n1 + y0) * n0, r11 = (z1 * n1 + y1) * n0;
-        c000 = ldv<DT>(brick + (r00 + x0) * bpv);
-        c001 = ldv<DT>(brick + (r00 + x1) * bpv);
-        c010 = ldv<DT>(brick + (r01 + x0) * bpv);
-        c011 = ldv<DT>(brick + (r01 + x1) * bpv);
-        c100 = ldv<DT>(brick + (r10 + x0) * bpv);
-        c101 = ldv<DT>(brick + (r10 + x1) * bpv);
-        c110 = ldv<DT>(brick + (r11 + x0) * bpv);
-        c111 = ldv<DT>(brick + (r11 + x1) * bpv);
+        T.c[0] = ldv<DT>(brick + (r00 + x0) * bpv);
+        T.c[1] = ldv<DT>(brick + (r00 + x1) * bpv);
+        T.c[2] = ldv<DT>(brick + (r01 + x0) * bpv);
+        T.c[3] = ldv<DT>(brick + (r01 + x1) * bpv);
+        T.c[4] = ldv<DT>(brick + (r10 + x0) * bpv);
+        T.c[5] = ldv<DT>(brick + (r10 + x1) * bpv);
+        T.c[6] = ldv<DT>(brick + (r11 + x0) * bpv);
+        T.c[7] = ldv<DT>(brick + (r11 + x1) * bpv);
     }
     else
     {
-        ix = min(max(ix, 0), n0 - 2);
-        iy = min(max(iy, 0), n1 - 2);
-        iz = min(max(iz, 0), n2 - 2);
+        /* every overlap >= 1: for a sample in cell c the slot coordinate is in
+         * [O - 1/2, O + B - 1/2], so the base voxel is in [0, N - 2] on each
+         * axis and all eight taps are in the slot. One unsigned clamp of the
+         * linear base keeps any tap inside the slot whatever the inputs. */
+        const uint32_t base = min(uint32_t((iz * n1 + iy) * n0 + ix), V.max_base);
         const int dy = n0 * bpv, dz = n0 * n1 * bpv;
-        const uint8_t* p00 = brick + ((iz * n1 + iy) * n0 + ix) * bpv;
+        const uint8_t* p00 = brick + base * bpv;
         const uint8_t* p01 = p00 + dy;
         const uint8_t* p10 = p00 + dz;
         const uint8_t* p11 = p10 + dy;
-        c000 = ldv<DT>(p00);
-        c001 = ldv<DT>(p00 + bpv);
-        c010 = ldv<DT>(p01);
-        c011 = ldv<DT>(p01 + bpv);
-        c100 = ldv<DT>(p10);
-        c101 = ldv<DT>(p10 + bpv);
-        c110 = ldv<DT>(p11);
-        c111 = ldv<DT>(p11 + bpv);
+        T.c[0] = ldv<DT>(p00);
+        T.c[1] = ldv<DT>(p00 + bpv);
+        T.c[2] = ldv<DT>(p01);
+        T.c[3] = ldv<DT>(p01 + bpv);
+        T.c[4] = ldv<DT>(p10);
+        T.c[5] = ldv<DT>(p10 + bpv);
+        T.c[6] = ldv<DT>(p11);
+        T.c[7] = ldv<DT>(p11 + bpv);
     }
-    const float a0 = fmaf(c001 - c000, fx, c000);
-    const float a1 = fmaf(c011 - c010, fx, c010);
-    const float a2 = fmaf(c101 - c100, fx, c100);
-    const float a3 = fmaf(c111 - c110, fx, c110);
-    const float b0 = fmaf(a1 - a0, fy, a0);
-    const float b1 = fmaf(a3 - a2, fy, a2);
-    return fmaf(b1 - b0, fz, b0);
 }
 
-/* Linear, clamp-to-edge lookup of the transfer function, stored as
- * interleaved (value_i, value_{i+1} - value_i) pairs (last difference 0). */
-template <int TFS>
-__device__ __forceinline__ float4 tf_lookup(const RayView& V, float d)
+/* Trilinear weights applied x, then y, then z (the oracle's order). */
+template <int FILTER>
+__device__ __forceinline__ float interp(const Taps<FILTER>& T)
 {
-    const float s = fmaf(d, float(V.tfn), -0.5f);
-    const int i0 = min(max(int(floorf(s)), 0), int(V.tfn) - 1);
-    const float f = fmaxf(s - float(i0), 0.0f);
+    if (FILTER == LV_FILTER_NEAREST)
+        return T.c[0];
+    const float a0 = fmaf(T.c[1] - T.c[0], T.fx, T.c[0]);
+    const float a1 = fmaf(T.c[3] - T.c[2], T.fx, T.c[2]);
+    const float a2 = fmaf(T.c[5] - T.c[4], T.fx, T.c[4]);
+    const float a3 = fmaf(T.c[7] - T.c[6], T.fx, T.c[6]);
+    const float b0 = fmaf(a1 - a0, T.fy, a0);
+    const float b1 = fmaf(a3 - a2, T.fy, a2);
+    return fmaf(b1 - b0, T.fz, b0);
+}
+
+/* Linear, clamp-to-edge lookup of the transfer function at voxel value v
+ * (texel coordinate v * tf_mul + tf_add = density * tfn - 1/2), stored as
+ * interleaved (value_i, value_{i+1} - value_i) pairs (last difference 0).
+ * Clamping the coordinate to [0, tfn - 1] before splitting it gives the
+ * same texel pair and weight as clamping the texel index after. */
+template <int TFS>
+__device__ __forceinline__ float4 tf_lookup(const RayView& V, float v)
+{
+    const float s = fminf(fmaxf(fmaf(v, V.tf_mul, V.tf_add), 0.0f), V.tf_last);
+    const int i0 = int(s);
+    const float f = s - float(i0);
     /* TFS: the table is in shared memory (generic loads), else read-only global */
     const float4* e = V.tf + 2 * i0;
     const float4 a = TFS ? e[0] : __ldg(e);
@@ -478,14 +502,102 @@ __device__ __forceinline__ bool ray_begin(const RayGeom& g, float step, RayState
     return true;
 }
 
-/* One sample of the ray: returns false once the ray has left its segment or
- * reached the early-termination opacity. */
+/* Advances the ray to its next sample. Returns 0 once the ray has left its
+ * segment, 1 for a sample without data (outside the octree or no brick
+ * rendered there), 2 with the sample's voxels in T. Position, cell and slot
+ * coordinate are single-rounding FMAs in a fixed order (the CPU oracle
+ * evaluates the same fmaf chain); the cell is floor(f) in one conversion and
+ * 0 <= c < dims one unsigned compare (f is finite: a ray with a non-finite
+ * direction or bounds has no samples). */
+template <int DT, int FILTER, int EDGE>
+__device__ __forceinline__ int fetch_sample(const RayView& V, RayState& r, float step,
+                                            Taps<FILTER>& T)
+{
+    const float t = fmaf(r.kf, step, r.tg);
+    if (!(t < r.thi))
+        return 0;
+    r.kf += 1.0f;
+    float f[3];
+    int c[3];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        const float p = fmaf(r.dir[a], t, V.eye[a]);
+        f[a] = fmaf(p, V.gscale[a], V.goff[a]);
+        c[a] = __float2int_rd(f[a]);
+        inside = inside && uint32_t(c[a]) < V.dims[a];
+    }
+    if (!inside)
+        return 1;
+    const uint32_t lin =
+        (uint32_t(c[2]) * V.dims[1] + uint32_t(c[1])) * V.dims[0] + uint32_t(c[0]);
+    if (lin != r.cur)
+    {
+        r.cur = lin;
+        uint32_t entry = __ldg(V.leaf + lin);
+        if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
+                                    (entry >> kLeafSlotBits) > V.Lf))
+        {
+            atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
+            entry = kLeafEmpty;
+        }
+        r.entry = entry;
+        if (entry != kLeafEmpty)
+        {
+            const float half_texel = FILTER == LV_FILTER_TRILINEAR ? 0.5f : 0.0f;
+            const uint32_t L = entry >> kLeafSlotBits;
+            const uint32_t slot = entry & kLeafSlotMask;
+            const uint32_t sh = V.Lf - L;
+            r.brick = V.pool + uint64_t(slot) * kSlotUnit;
+            const float inv_side = __int_as_float(int(127u - sh) << 23); /* 2^-sh */
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+            {
+                r.vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
+                r.off[a] = (__uint2float_rn(V.O[a]) -
+                            __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a])) -
+                           half_texel; /* exact */
+            }
+        }
+    }
+    if (r.entry == kLeafEmpty)
+        return 1;
+    float sc[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        sc[a] = fmaf(f[a], r.vs[a], r.off[a]);
+    load_taps<DT, FILTER, EDGE>(V, r.brick, sc, T);
+    return 2;
+}
+
+/* Transfer function, opacity correction and front-to-back blending of one
+ * sample (fragRayCast.glsl:103-111); false once the early-termination
+ * opacity is reached. */
+template <int FILTER, int TFS>
+__device__ __forceinline__ bool composite_sample(const RayView& V, RayState& r, float ac,
+                                                 const Taps<FILTER>& T, uint32_t& nsamp)
+{
+    const float4 src = tf_lookup<TFS>(V, interp<FILTER>(T));
+    const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
+    const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
+    const float w = alpha * (1.0f - r.dst.w);
+    r.dst.x = fmaf(src.x, w, r.dst.x);
+    r.dst.y = fmaf(src.y, w, r.dst.y);
+    r.dst.z = fmaf(src.z, w, r.dst.z);
+    r.dst.w = fmaf(alpha, 1.0f - r.dst.w, r.dst.w);
+    ++nsamp;
+    return !(r.dst.w > V.early);
+}
+
+/* One sample of the ray: false once the ray has ended or reached the
+ * early-termination opacity. The steps of fetch_sample and composite_sample
+ * in one straight body (fewer registers live across the loop than the two
+ * calls). */
 template <int DT, int FILTER, int TFS, int EDGE>
 __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float step, float ac,
-                                         const float dimf[3], uint32_t& nsamp)
+                                         uint32_t& nsamp)
 {
-    /* sample position, cell and slot coordinate: single-rounding FMAs in a
-     * fixed order (the CPU oracle evaluates the same fmaf chain) */
     const float t = fmaf(r.kf, step, r.tg);
     if (!(t < r.thi))
         return false;
@@ -498,9 +610,8 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     {
         const float p = fmaf(r.dir[a], t, V.eye[a]);
         f[a] = fmaf(p, V.gscale[a], V.goff[a]);
-        const float fl = floorf(f[a]);
-        inside = inside && (fl >= 0.0f) && (fl < dimf[a]);
-        c[a] = int(fl);
+        c[a] = __float2int_rd(f[a]);
+        inside = inside && uint32_t(c[a]) < V.dims[a];
     }
     if (!inside)
         return true;
@@ -541,9 +652,9 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         sc[a] = fmaf(f[a], r.vs[a], r.off[a]);
-    const float value = sample_brick<DT, FILTER, EDGE>(V, r.brick, sc);
-    const float dens = fmaf(value, V.dmul, V.dadd);
-    const float4 src = tf_lookup<TFS>(V, dens);
+    Taps<FILTER> T;
+    load_taps<DT, FILTER, EDGE>(V, r.brick, sc, T);
+    const float4 src = tf_lookup<TFS>(V, interp<FILTER>(T));
     const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
     const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
     const float w = alpha * (1.0f - r.dst.w);
@@ -555,23 +666,42 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     return !(r.dst.w > V.early);
 }
 
-template <int DT, int FILTER, int TFS, int EDGE>
+/* The whole ray. LOOKAHEAD = 1 loads the voxels of sample k + 1 before
+ * sample k is composited, so the two latency chains overlap (a lone long
+ * ray runs faster; more registers per thread). Samples, values and the
+ * compositing order are those of ray_step either way; after an early
+ * termination the loads of one extra sample are dropped. */
+template <int DT, int FILTER, int TFS, int EDGE, int LOOKAHEAD = 0>
 __device__ float4 march(const RayView& V, const RayGeom& g, float step,
                         float ac, uint32_t& nsamp)
 {
     RayState r;
     if (!ray_begin(g, step, r))
         return r.dst;
-    const float dimf[3] = {__uint2float_rn(V.dims[0]), __uint2float_rn(V.dims[1]),
-                           __uint2float_rn(V.dims[2])};
-    while (ray_step<DT, FILTER, TFS, EDGE>(V, r, step, ac, dimf, nsamp))
+    if (!LOOKAHEAD)
     {
+        while (ray_step<DT, FILTER, TFS, EDGE>(V, r, step, ac, nsamp))
+        {
+        }
+        return r.dst;
+    }
+    Taps<FILTER> T0;
+    int s0 = fetch_sample<DT, FILTER, EDGE>(V, r, step, T0);
+    while (s0)
+    {
+        Taps<FILTER> T1;
+        const int s1 = fetch_sample<DT, FILTER, EDGE>(V, r, step, T1);
+        if (s0 == 2 && !composite_sample<FILTER, TFS>(V, r, ac, T0, nsamp))
+            break;
+        s0 = s1;
+        T0 = T1;
     }
     return r.dst;
 }
 
-template <int DT, int FILTER, int EDGE>
-__global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
+/* LA: one-sample look-ahead */
+template <int DT, int FILTER, int EDGE, int LA>
+__global__ void __launch_bounds__(256) raycast_kernel(const RayView V)
 {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t py = blockIdx.y * blockDim.y + threadIdx.y;
@@ -582,7 +712,7 @@ __global__ void __launch_bounds__(128) raycast_kernel(const RayView V)
     if (px < V.W && py < V.H)
     {
         const RayGeom g = ray_setup(V, px, py);
-        const float4 r = march<DT, FILTER, 0, EDGE>(V, g, step, ac, nsamp);
+        const float4 r = march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp);
         V.out[uint64_t(py) * V.W + px] = r;
     }
     /* warp-aggregated 64-bit sample count */
@@ -679,6 +809,109 @@ __global__ void __launch_bounds__(256)
         atomicMax(Q.clock + 1, globaltimer());
 }
 
+/* Longest-first tile order of one view. A tile's cost is estimated by the
+ * length of its centre ray inside the volume (near and clip planes
+ * applied), quantised to kTileBuckets classes; a counting sort lists the
+ * longest class first (the order within a class does not matter: every
+ * pixel is computed independently). hist[0, kTileBuckets) are the class
+ * counts and hist[kTileBuckets, 2 kTileBuckets) the scatter cursors, both
+ * zeroed before the key pass. */
+constexpr uint32_t kTileBuckets = 64;
+
+__global__ void __launch_bounds__(256)
+    tile_key_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h, uint32_t tiles_x,
+                    uint32_t total, float buckets_per_length, uint8_t* __restrict__ keys,
+                    uint32_t* __restrict__ hist)
+{
+    __shared__ uint32_t h[kTileBuckets];
+    for (uint32_t i = threadIdx.x; i < kTileBuckets; i += blockDim.x)
+        h[i] = 0;
+    __syncthreads();
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < total)
+    {
+        const uint32_t px = min((t % tiles_x) * tile_w + tile_w / 2, V.W - 1);
+        const uint32_t py = min((t / tiles_x) * tile_h + tile_h / 2, V.H - 1);
+        const RayGeom g = ray_setup(V, px, py);
+        const float len = g.hit && g.tlo <= g.thi ? g.thi - g.tlo : 0.0f;
+        const uint32_t q = uint32_t(fminf(len * buckets_per_length, float(kTileBuckets - 1)));
+        const uint32_t key = kTileBuckets - 1u - q;
+        keys[t] = uint8_t(key);
+        atomicAdd(&h[key], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kTileBuckets; i += blockDim.x)
+        if (h[i])
+            atomicAdd(&hist[i], h[i]);
+}
+
+__global__ void __launch_bounds__(256)
+    tile_order_kernel(const uint8_t* __restrict__ keys, uint32_t* __restrict__ hist,
+                      uint32_t* __restrict__ order, uint32_t total)
+{
+    __shared__ uint32_t base[kTileBuckets];
+    if (threadIdx.x == 0)
+    {
+        uint32_t acc = 0;
+        for (uint32_t k = 0; k < kTileBuckets; ++k)
+        {
+            base[k] = acc;
+            acc += hist[k];
+        }
+    }
+    __syncthreads();
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < total)
+    {
+        const uint32_t key = keys[t];
+        const uint32_t pos = base[key] + atomicAdd(&hist[kTileBuckets + key], 1u);
+        if (pos < total)
+            order[pos] = t;
+    }
+}
+
+/* Single view on a resident grid: CTAs take tile_w x tile_h pixel tiles
+ * (one ray per thread) from a device queue, the view's FC_QUEUE counter. */
+template <int DT, int FILTER, int EDGE, int LA>
+__global__ void __launch_bounds__(256)
+    raycast_queue_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h,
+                         const uint32_t* __restrict__ order)
+{
+    __shared__ uint32_t s_item;
+    const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
+    const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
+    const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
+    const uint32_t tiles_x = (V.W + tile_w - 1) / tile_w;
+    const uint32_t total = tiles_x * ((V.H + tile_h - 1) / tile_h);
+    const uint32_t tx = threadIdx.x % tile_w, ty = threadIdx.x / tile_w;
+    uint32_t nsamp = 0;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(V.counters + FC_QUEUE, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        __syncthreads();
+        if (item >= total)
+            break;
+        const uint32_t tile = order ? order[item] : item;
+        const uint32_t px = (tile % tiles_x) * tile_w + tx;
+        const uint32_t py = (tile / tiles_x) * tile_h + ty;
+        if (px < V.W && py < V.H)
+        {
+            const RayGeom g = ray_setup(V, px, py);
+            V.out[uint64_t(py) * V.W + px] =
+                march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp);
+        }
+    }
+    unsigned long long sum = nsamp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+    if ((threadIdx.x & 31u) == 0 && sum)
+        atomicAdd(reinterpret_cast<unsigned long long*>(V.counters + FC_SAMPLES_LO), sum);
+}
+
 /* ---------------------------------------------------------------- refill
  * Persistent ray cast with lane refill. Every warp takes tile_w x tile_h
  * pixel tiles from a device queue (one atomic per tile) and hands the tile's
@@ -740,7 +973,7 @@ __device__ __forceinline__ void flush_samples(const RayView& V, uint32_t nsamp)
 
 struct ViewConsts
 {
-    float step, ac, dimf[3];
+    float step, ac;
     uint32_t tiles_x;
 };
 
@@ -750,9 +983,6 @@ __device__ __forceinline__ ViewConsts view_consts(const RayView& V, uint32_t til
     const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
     k.step = __fdiv_rn(1.0f, __uint2float_rn(n));
     k.ac = __fdiv_rn(32.0f, __uint2float_rn(n));
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        k.dimf[a] = __uint2float_rn(V.dims[a]);
     k.tiles_x = (V.W + tile_w - 1) / tile_w;
     return k;
 }
@@ -763,7 +993,8 @@ template <int DT, int FILTER, int EDGE, bool MULTI>
 __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
                                             const RayView* __restrict__ views,
                                             const TileQueue& Q, uint32_t* head,
-                                            uint32_t n_views, uint32_t total, uint32_t checks)
+                                            uint32_t n_views, uint32_t total, uint32_t checks,
+                                            const uint32_t* __restrict__ order)
 {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t below = (1u << lane) - 1u;
@@ -778,7 +1009,7 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
         load_view(sv, views + Q.view_ids[gv]);
     }
     ViewConsts K = view_consts(V, tw);
-    uint32_t tile = item - (MULTI ? Q.tile_start[gv] : 0u);
+    uint32_t tile = MULTI ? item - Q.tile_start[gv] : (order ? order[item] : item);
     uint32_t next = 0, pending = kNoItem;
     bool exhausted = false, active = false;
     uint32_t px = 0, py = 0, nsamp = 0;
@@ -806,7 +1037,7 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
                     pending = nitem; /* another view: drain first */
                     break;
                 }
-                tile = nitem - (MULTI ? Q.tile_start[gv] : 0u);
+                tile = MULTI ? nitem - Q.tile_start[gv] : (order ? order[nitem] : nitem);
                 next = 0;
             }
             const uint32_t mine = next + __popc(idle & below);
@@ -842,7 +1073,7 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
         }
         if (active)
             for (uint32_t k = 0; k < checks; ++k)
-                if (!ray_step<DT, FILTER, 0, EDGE>(V, r, K.step, K.ac, K.dimf, nsamp))
+                if (!ray_step<DT, FILTER, 0, EDGE>(V, r, K.step, K.ac, nsamp))
                 {
                     active = false;
                     V.out[uint64_t(py) * V.W + px] = r.dst;
@@ -855,14 +1086,15 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
 /* Single view (lv_render): the queue head is the view's FC_QUEUE counter. */
 template <int DT, int FILTER, int EDGE>
 __global__ void __launch_bounds__(kRefillThreads, kRefillMinCtas)
-    raycast_refill_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h, uint32_t checks)
+    raycast_refill_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h, uint32_t checks,
+                          const uint32_t* __restrict__ order)
 {
     TileQueue Q{};
     Q.tile_w = tile_w;
     Q.tile_h = tile_h;
     const uint32_t tiles = ((V.W + tile_w - 1) / tile_w) * ((V.H + tile_h - 1) / tile_h);
     refill_body<DT, FILTER, EDGE, false>(V, nullptr, nullptr, Q, V.counters + FC_QUEUE, 1u,
-                                         tiles, checks);
+                                         tiles, checks, order);
 }
 
 /* Batched: tiles of many views of one kernel variant. */
@@ -876,7 +1108,7 @@ __global__ void __launch_bounds__(kRefillThreads, kRefillMinCtas)
     const uint32_t n_views = *Q.n_views;
     RayView* sv = sV + (threadIdx.x >> 5);
     refill_body<DT, FILTER, EDGE, true>(*sv, sv, views, Q, Q.head, n_views,
-                                        Q.tile_start[n_views], checks);
+                                        Q.tile_start[n_views], checks, nullptr);
     if ((threadIdx.x & 31u) == 0)
         atomicMax(Q.clock + 1, globaltimer());
 }
@@ -975,26 +1207,101 @@ lv_status refill_views_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQu
     return LV_OK;
 }
 
+/* Longest-first order of the tiles of V (two small launches); nullptr for
+ * raster order. */
+const uint32_t* tile_order(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                           cudaStream_t s, lv_status& st)
+{
+    st = LV_OK;
+    if (L.order != LV_ORDER_LONGEST_FIRST)
+        return nullptr;
+    const uint32_t tiles_x = (V.W + L.tile_w - 1) / L.tile_w;
+    const uint32_t total = tiles_x * ((V.H + L.tile_h - 1) / L.tile_h);
+    const size_t hist_bytes = 2 * kTileBuckets * sizeof(uint32_t);
+    const size_t key_bytes = (size_t(total) + 15) & ~size_t(15);
+    DeviceBuffer& buf = ctx->renderer->tiles;
+    cudaError_t e = buf.reserve(hist_bytes + key_bytes + sizeof(uint32_t) * total);
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(buf.ptr, 0, hist_bytes, s);
+    if (e != cudaSuccess)
+    {
+        st = cuda_fail(ctx, e, "tile order");
+        return nullptr;
+    }
+    uint32_t* hist = buf.as<uint32_t>();
+    uint8_t* keys = buf.as<uint8_t>() + hist_bytes;
+    uint32_t* order = reinterpret_cast<uint32_t*>(keys + key_bytes);
+    float diag = 0.f;
+    for (int a = 0; a < 3; ++a)
+        diag += (V.gmax[a] - V.gmin[a]) * (V.gmax[a] - V.gmin[a]);
+    const float per_length = float(kTileBuckets) / std::sqrt(diag);
+    const uint32_t blocks = (total + 255) / 256;
+    tile_key_kernel<<<blocks, 256, 0, s>>>(V, L.tile_w, L.tile_h, tiles_x, total, per_length,
+                                           keys, hist);
+    tile_order_kernel<<<blocks, 256, 0, s>>>(keys, hist, order, total);
+    e = cudaGetLastError();
+    if (e != cudaSuccess)
+    {
+        st = cuda_fail(ctx, e, "tile order");
+        return nullptr;
+    }
+    return order;
+}
+
 template <int DT, int F, int EDGE>
 lv_status refill_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                           cudaStream_t s)
 {
+    lv_status st = LV_OK;
+    const uint32_t* order = tile_order(ctx, V, L, s, st);
+    if (st != LV_OK)
+        return st;
     auto k = raycast_refill_kernel<DT, F, EDGE>;
     const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
     const uint32_t warps = kRefillThreads / 32;
     const uint32_t grid = std::max(1u, std::min(resident_ctas(ctx, k, kRefillThreads, 0),
                                                 (tiles + warps - 1) / warps));
-    k<<<grid, kRefillThreads, 0, s>>>(V, L.tile_w, L.tile_h, L.samples_per_check);
+    k<<<grid, kRefillThreads, 0, s>>>(V, L.tile_w, L.tile_h, L.samples_per_check, order);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+template <int DT, int F, int EDGE, int LA>
+lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                            cudaStream_t s)
+{
+    if (L.kind == LV_LAUNCH_TILE_QUEUE)
+    {
+        lv_status st = LV_OK;
+        const uint32_t* order = tile_order(ctx, V, L, s, st);
+        if (st != LV_OK)
+            return st;
+        auto k = raycast_queue_kernel<DT, F, EDGE, LA>;
+        const uint32_t threads = L.tile_w * L.tile_h;
+        const uint32_t tiles =
+            ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
+        const uint32_t grid =
+            std::max(1u, std::min(resident_ctas(ctx, k, int(threads), 0), tiles));
+        k<<<grid, threads, 0, s>>>(V, L.tile_w, L.tile_h, order);
+        LV_CUDA(ctx, cudaGetLastError());
+        return LV_OK;
+    }
+    const dim3 block(L.tile_w, L.tile_h);
+    const dim3 grid((V.W + block.x - 1) / block.x, (V.H + block.y - 1) / block.y);
+    raycast_kernel<DT, F, EDGE, LA><<<grid, block, 0, s>>>(V);
     LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;
 }
 
 template <int DT, int F, int EDGE>
-lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, dim3 grid, dim3 block, cudaStream_t s)
+lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                         cudaStream_t s)
 {
-    raycast_kernel<DT, F, EDGE><<<grid, block, 0, s>>>(V);
-    LV_CUDA(ctx, cudaGetLastError());
-    return LV_OK;
+    if (L.kind == LV_LAUNCH_WARP_REFILL)
+        return refill_dispatch<DT, F, EDGE>(ctx, V, L, s);
+    if (L.lookahead)
+        return plain_dispatch_la<DT, F, EDGE, 1>(ctx, V, L, s);
+    return plain_dispatch_la<DT, F, EDGE, 0>(ctx, V, L, s);
 }
 
 /* combination index: dtype (u8 0 / u16 1), filter, edge */
@@ -1046,31 +1353,16 @@ lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
                                 V.max_voxel_dim, V.depth);
     LV_CUDA(ctx, cudaGetLastError());
     const lv_render_launch L = ctx->launch;
-    const int variant = kernel_variant(V.dtype, V.filter, V.edge);
-    if (L.tile_w)
-        switch (variant)
-        {
-        case 0: return refill_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, L, s);
-        case 1: return refill_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, L, s);
-        case 2: return refill_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, L, s);
-        case 3: return refill_dispatch<LV_DT_UINT8, 1, 1>(ctx, V, L, s);
-        case 4: return refill_dispatch<LV_DT_UINT16, 0, 0>(ctx, V, L, s);
-        case 5: return refill_dispatch<LV_DT_UINT16, 0, 1>(ctx, V, L, s);
-        case 6: return refill_dispatch<LV_DT_UINT16, 1, 0>(ctx, V, L, s);
-        default: return refill_dispatch<LV_DT_UINT16, 1, 1>(ctx, V, L, s);
-        }
-    const dim3 block(8, 16);
-    const dim3 grid((V.W + block.x - 1) / block.x, (V.H + block.y - 1) / block.y);
-    switch (variant)
+    switch (kernel_variant(V.dtype, V.filter, V.edge))
     {
-    case 0: return plain_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, grid, block, s);
-    case 1: return plain_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, grid, block, s);
-    case 2: return plain_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, grid, block, s);
-    case 3: return plain_dispatch<LV_DT_UINT8, 1, 1>(ctx, V, grid, block, s);
-    case 4: return plain_dispatch<LV_DT_UINT16, 0, 0>(ctx, V, grid, block, s);
-    case 5: return plain_dispatch<LV_DT_UINT16, 0, 1>(ctx, V, grid, block, s);
-    case 6: return plain_dispatch<LV_DT_UINT16, 1, 0>(ctx, V, grid, block, s);
-    default: return plain_dispatch<LV_DT_UINT16, 1, 1>(ctx, V, grid, block, s);
+    case 0: return plain_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, L, s);
+    case 1: return plain_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, L, s);
+    case 2: return plain_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, L, s);
+    case 3: return plain_dispatch<LV_DT_UINT8, 1, 1>(ctx, V, L, s);
+    case 4: return plain_dispatch<LV_DT_UINT16, 0, 0>(ctx, V, L, s);
+    case 5: return plain_dispatch<LV_DT_UINT16, 0, 1>(ctx, V, L, s);
+    case 6: return plain_dispatch<LV_DT_UINT16, 1, 0>(ctx, V, L, s);
+    default: return plain_dispatch<LV_DT_UINT16, 1, 1>(ctx, V, L, s);
     }
 }
 

@@ -485,6 +485,11 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     V.brick_units = vol->slot_units;
     V.tf = tf->rgba.as<float4>();
     V.tfn = tf->n;
+    V.tf_mul = V.dmul * float(tf->n);
+    V.tf_add = V.dadd * float(tf->n) - 0.5f;
+    V.tf_last = float(tf->n - 1u);
+    V.max_base = V.edge ? 0u
+                        : (V.N[2] - 2u) * V.N[1] * V.N[0] + (V.N[1] - 2u) * V.N[0] + V.N[0] - 2u;
     V.out = reinterpret_cast<float4*>(d_rgba);
     V.counters = counters;
     return LV_OK;
@@ -906,10 +911,21 @@ extern "C" lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* c
     if (!ctx || !cfg)
         return LV_EINVAL;
     const uint32_t pixels = cfg->tile_w * cfg->tile_h;
-    if (cfg->tile_w && (pixels < 32 || pixels > 1024 || cfg->samples_per_check == 0 ||
-                        cfg->samples_per_check > 64))
+    const bool ok = cfg->kind == LV_LAUNCH_WARP_REFILL
+                        ? pixels >= 32 && pixels <= 1024 && cfg->samples_per_check >= 1 &&
+                              cfg->samples_per_check <= 64
+                        : (cfg->kind == LV_LAUNCH_GRID || cfg->kind == LV_LAUNCH_TILE_QUEUE) &&
+                              pixels >= 32 && pixels <= 256 && pixels % 32 == 0;
+    const bool order_ok = (cfg->order == LV_ORDER_RASTER ||
+                           (cfg->order == LV_ORDER_LONGEST_FIRST && cfg->kind != LV_LAUNCH_GRID)) &&
+                          (cfg->lookahead == 0 ||
+                           (cfg->lookahead == 1 && cfg->kind != LV_LAUNCH_WARP_REFILL));
+    if (!ok || !order_ok)
         return fail(ctx, LV_EINVAL,
-                    "render launch: 32..1024 pixels per tile, samples_per_check in 1..64");
+                    "render launch: grid and tile-queue tiles of 32..256 threads (a multiple "
+                    "of 32); warp-refill tiles of 32..1024 pixels, samples_per_check 1..64; "
+                    "longest-first order only for the queue kinds; lookahead 0 or 1, not for "
+                    "warp refill");
     std::lock_guard<std::mutex> lock(ctx->mutex);
     ctx->launch = *cfg;
     return LV_OK;
@@ -999,9 +1015,13 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     LV.out_ids = R.visible.as<uint64_t>();
     LV.capacity = uint32_t(std::min<uint64_t>(R.visible_capacity, 0xFFFFFFFFu));
     LV.result = R.sel_result.as<uint32_t>();
-    /* kernels: roots + one per level + finish, resolve (x2 on a sync miss),
-     * prune, leaf fill, step, ray cast */
-    R.launches = info.depth + 2u + 5u;
+    /* kernels: roots + one per level + finish, resolve, prune, leaf fill,
+     * step, ray cast (+ tile keys and order when longest first); the last
+     * five to seven again on a synchronous miss */
+    const lv_render_launch& RL = ctx->launch;
+    const uint32_t tail_launches =
+        5u + (RL.kind != LV_LAUNCH_GRID && RL.order == LV_ORDER_LONGEST_FIRST ? 2u : 0u);
+    R.launches = info.depth + 2u + tail_launches;
     LV_CUDA(ctx, cudaEventRecord(R.t_sel0, s));
     st = run_selection(ctx, &LV, 1, info.depth, s);
     if (st != LV_OK)
@@ -1095,7 +1115,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             st = frame_tail();
             if (st != LV_OK)
                 return st;
-            R.launches += 5u;
+            R.launches += tail_launches;
         }
     }
 

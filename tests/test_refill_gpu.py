@@ -1,12 +1,16 @@
-"""Ray-cast launch shapes: the persistent warp-refill kernels take exactly the
-samples of the one-thread-per-pixel kernel, in the same order, so every
-launch shape must give a bit-identical image and the same sample count."""
+"""Ray-cast launch shapes: the tile-queue and warp-refill kernels take exactly
+the samples of the one-thread-per-pixel kernel, in the same order, so every
+launch kind and shape must give a bit-identical image and the same sample
+count."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-LAUNCHES = [(8, 8, 8), (8, 4, 1), (16, 8, 2), (16, 16, 32), (32, 32, 64), (32, 1, 5)]
+LAUNCHES = [(0, 8, 4, 0, 0, 0), (0, 16, 16, 0, 0, 1), (0, 32, 2, 0, 0, 0),
+            (1, 8, 16, 0, 0, 1), (1, 16, 16, 0, 1, 0), (1, 8, 8, 0, 1, 1), (1, 32, 1, 0, 0, 0),
+            (2, 8, 8, 8, 0, 0), (2, 8, 4, 1, 1, 0), (2, 16, 8, 2, 0, 0), (2, 16, 16, 32, 1, 0),
+            (2, 32, 32, 64, 0, 0), (2, 32, 1, 5, 0, 0)]
 
 
 def scenes(ctx, lv):
@@ -32,16 +36,17 @@ def test_refill_launches_bit_identical(gpu_ctx):
     items = scenes(gpu_ctx, lv)
     default = gpu_ctx.render_launch()
     try:
-        gpu_ctx.set_render_launch(0, 0, 0)  # one thread per pixel
+        gpu_ctx.set_render_launch(lv.LAUNCH_GRID, 8, 16)  # one thread per pixel
         refs = []
         for vol, desc in items:
             refs.append((gpu_ctx.render(vol, tf, desc).clone(), gpu_ctx.last_stats()))
-        for tw, th, chk in LAUNCHES:
-            gpu_ctx.set_render_launch(tw, th, chk)
+        for kind, tw, th, chk, order, la in LAUNCHES:
+            gpu_ctx.set_render_launch(kind, tw, th, chk, order, la)
             for (vol, desc), (ref, rst) in zip(items, refs):
                 img = gpu_ctx.render(vol, tf, desc)
                 st = gpu_ctx.last_stats()
-                assert torch.equal(img, ref), (tw, th, chk, desc.width, desc.height)
+                assert torch.equal(img, ref), (kind, tw, th, chk, order, la, desc.width,
+                                               desc.height)
                 assert st["n_samples"] == rst["n_samples"]
                 assert st["error_flags"] == 0
     finally:
@@ -53,10 +58,13 @@ def test_refill_launches_bit_identical(gpu_ctx):
 
 def test_render_launch_validation(gpu_ctx):
     import livre_gb300 as lv
-    for bad in [(4, 4, 8), (64, 32, 8), (8, 8, 0), (8, 8, 65)]:
+    for bad in [(2, 4, 4, 8), (2, 64, 32, 8), (2, 8, 8, 0), (2, 8, 8, 65), (0, 8, 3, 0),
+                (0, 32, 16, 0), (1, 4, 4, 0), (3, 8, 8, 8), (0, 8, 16, 0, 1),
+                (1, 8, 16, 0, 2), (1, 8, 16, 0, 0, 2), (2, 8, 8, 8, 0, 1)]:
         with pytest.raises(lv.LivreError):
             gpu_ctx.set_render_launch(*bad)
-    assert gpu_ctx.render_launch() == {"tile_w": 0, "tile_h": 0, "samples_per_check": 0}
+    assert gpu_ctx.render_launch() == {"kind": 1, "tile_w": 8, "tile_h": 16,
+                                       "samples_per_check": 0, "order": 1, "lookahead": 0}
 
 
 @pytest.mark.parametrize("cfg", [
