@@ -392,6 +392,9 @@ typedef struct lv_batch_config
     uint32_t queue;          /* LV_QUEUE_* */
     uint32_t samples_per_check; /* warp refill: samples a lane takes between
                                    refills (1..64) */
+    uint32_t order;          /* LV_ORDER_* (CTA tiles): longest first ranks the
+                                (view, tile) items of all views by the
+                                estimated samples of their centre ray */
 } lv_batch_config;
 
 /* A batch renderer on ctx (its own stream, graphs and per-view buffers).
@@ -420,7 +423,8 @@ lv_status lv_batch_graph_stats(lv_batch* batch, uint64_t* captures,
                                uint64_t* replays, uint32_t* cached);
 /* Times the persistent ray cast on this batch (reps timed launches each)
  * for CTA tiles of {8x8, 16x8, 8x16, 16x16, 32x4, 32x8} pixels with and
- * without transfer-function staging, and for warp-refill tiles of {8x4, 8x8,
+ * without transfer-function staging in raster and longest-first order, and
+ * for warp-refill tiles of {8x4, 8x8,
  * 16x8, 16x16} pixels with refills every {2, 8, 32} samples, all on a
  * resident grid; keeps the fastest configuration and returns it in
  * `chosen`. */

@@ -610,12 +610,15 @@ class Batch:
         check(lib().lv_batch_get_config(self.handle, C.byref(c)), self.ctx.handle)
         return c.as_dict()
 
-    def set_config(self, tile_w=8, tile_h=8, ctas_per_sm=0, tf_shared=0, use_graph=1,
-                   queue=None, samples_per_check=8):
-        if queue is None:
-            queue = _abi.QUEUE_CTA_TILES if tf_shared else _abi.QUEUE_WARP_REFILL
+    def set_config(self, tile_w=8, tile_h=16, ctas_per_sm=0, tf_shared=0, use_graph=1,
+                   queue=_abi.QUEUE_CTA_TILES, samples_per_check=8, order=None):
+        """order: ORDER_LONGEST_FIRST (default for CTA tiles) or ORDER_RASTER
+        (the only order of warp refill)."""
+        if order is None:
+            order = (_abi.ORDER_LONGEST_FIRST if queue == _abi.QUEUE_CTA_TILES
+                     else _abi.ORDER_RASTER)
         c = _abi.BatchConfig(tile_w, tile_h, ctas_per_sm, tf_shared, use_graph, queue,
-                             samples_per_check)
+                             samples_per_check, order)
         check(lib().lv_batch_set_config(self.handle, C.byref(c)), self.ctx.handle)
 
     @staticmethod

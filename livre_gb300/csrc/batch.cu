@@ -39,6 +39,7 @@ namespace
 struct Group
 {
     std::vector<uint32_t> views;
+    uint32_t items = 0; /* work items (tiles) of the group's views */
 };
 constexpr int kGroups = 8;
 
@@ -55,7 +56,15 @@ struct lv_batch
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr, user_ready = nullptr;
     cudaEvent_t t_sel0 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
-    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_CTA_TILES, 8};
+    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_CTA_TILES, 8, LV_ORDER_LONGEST_FIRST};
+    /* per-group longest-first order: hist (128 words) | keys | order, each
+     * group at a fixed offset sized for order_cap items (grow-only) */
+    lv::DeviceBuffer order_buf;
+    uint32_t order_cap = 0;
+    /* one stream per non-first group: the groups' persistent launches run
+     * side by side, so one group's last tiles overlap the next group */
+    cudaStream_t aux[8] = {};
+    cudaEvent_t fork = nullptr, join[8] = {};
     /* per-view region strides (grow-only) */
     uint64_t nodes_stride = 0, cells_stride = 0, missing_stride = 0;
     uint32_t views_cap = 0;
@@ -95,6 +104,15 @@ struct lv_batch
             cudaEventDestroy(t_ray0);
         if (t_ray1)
             cudaEventDestroy(t_ray1);
+        if (fork)
+            cudaEventDestroy(fork);
+        for (int g = 0; g < 8; ++g)
+        {
+            if (join[g])
+                cudaEventDestroy(join[g]);
+            if (aux[g])
+                cudaStreamDestroy(aux[g]);
+        }
         if (stream)
             cudaStreamDestroy(stream);
     }
@@ -125,6 +143,34 @@ ParamLayout param_layout(uint32_t n)
      * one captured graph lives in this copied block */
     L.bytes = al(L.tables + sizeof(uint32_t) * (kGroups * (2 * n + 1) + kGroups + 1));
     return L;
+}
+
+constexpr uint64_t kOrderHistBytes = 2 * 64 * sizeof(uint32_t);
+uint64_t order_keys_bytes(uint32_t cap) { return (uint64_t(cap) + 255) & ~uint64_t(255); }
+uint64_t order_region_bytes(uint32_t cap)
+{
+    return kOrderHistBytes + order_keys_bytes(cap) + sizeof(uint32_t) * uint64_t(cap);
+}
+
+/* Longest-first order buffers for groups of up to `items` work items; a
+ * reallocation drops the captured graphs (they hold the old addresses). */
+lv_status ensure_order(lv_batch* b, uint32_t items)
+{
+    if (b->cfg.order != LV_ORDER_LONGEST_FIRST || items <= b->order_cap)
+        return LV_OK;
+    lv_ctx* ctx = b->ctx;
+    LV_CUDA(ctx, cudaStreamSynchronize(b->stream));
+    uint32_t cap = std::max<uint32_t>(b->order_cap, 4096);
+    while (cap < items)
+        cap += cap / 2;
+    b->order_buf.release();
+    LV_CUDA(ctx, b->order_buf.reserve(order_region_bytes(cap) * kGroups));
+    b->order_cap = cap;
+    for (auto& kv : b->graphs)
+        cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+    ++b->generation;
+    return LV_OK;
 }
 
 lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
@@ -339,6 +385,7 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n, uint3
             acc += ((rays[v].W + tw - 1) / tw) * ((rays[v].H + th - 1) / th);
         }
         starts[groups[g].views.size()] = acc;
+        groups[g].items = acc;
     }
     uint32_t* counts = tables + stride * kGroups;
     for (int g = 0; g < kGroups; ++g)
@@ -371,6 +418,10 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         return st;
     uint32_t* heads = b->zeroed.as<uint32_t>() + kOutWords * n; /* kGroups words */
     unsigned long long* clock = reinterpret_cast<unsigned long long*>(heads + kGroups);
+    const RayView* d_rays = reinterpret_cast<RayView*>(d + PL.ray);
+    const bool ordered = b->cfg.order == LV_ORDER_LONGEST_FIRST;
+    bool first = true;
+    LV_CUDA(ctx, cudaEventRecord(b->fork, s));
     for (int g = 0; g < kGroups; ++g)
     {
         if (groups[g].views.empty())
@@ -383,10 +434,32 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         Q.tile_h = b->cfg.tile_h;
         Q.head = heads + g;
         Q.clock = clock;
-        st = launch_persistent(ctx, g, b->cfg, reinterpret_cast<RayView*>(d + PL.ray), Q,
-                               tfn_max, s);
+        Q.order = nullptr;
+        /* the first group on the batch stream, the others each on its own */
+        cudaStream_t gs = first ? s : b->aux[g];
+        if (!first)
+            LV_CUDA(ctx, cudaStreamWaitEvent(gs, b->fork, 0));
+        if (ordered)
+        {
+            const uint64_t region = order_region_bytes(b->order_cap);
+            uint8_t* base = b->order_buf.as<uint8_t>() + region * g;
+            uint32_t* hist = reinterpret_cast<uint32_t*>(base);
+            uint8_t* keys = base + kOrderHistBytes;
+            uint32_t* order = reinterpret_cast<uint32_t*>(keys + order_keys_bytes(b->order_cap));
+            st = launch_batch_order(ctx, d_rays, Q, b->order_cap, keys, hist, order, gs);
+            if (st != LV_OK)
+                return st;
+            Q.order = order;
+        }
+        st = launch_persistent(ctx, g, b->cfg, d_rays, Q, tfn_max, gs);
         if (st != LV_OK)
             return st;
+        if (!first)
+        {
+            LV_CUDA(ctx, cudaEventRecord(b->join[g], gs));
+            LV_CUDA(ctx, cudaStreamWaitEvent(s, b->join[g], 0));
+        }
+        first = false;
     }
     LV_CUDA(ctx, cudaMemcpyAsync(b->h_out.ptr, b->zeroed.ptr,
                                  sizeof(uint32_t) * (kOutWords * n + kGroups + 4),
@@ -418,11 +491,19 @@ extern "C" lv_status lv_batch_create(lv_ctx* ctx, lv_batch** out)
         cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->user_ready, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&b->t_sel0) != cudaSuccess || cudaEventCreate(&b->t_ray0) != cudaSuccess ||
-        cudaEventCreate(&b->t_ray1) != cudaSuccess)
+        cudaEventCreate(&b->t_ray1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
     {
         delete b;
         return fail(ctx, LV_EDEVICE, "batch stream/events");
     }
+    for (int g = 0; g < kGroups; ++g)
+        if (cudaStreamCreateWithFlags(&b->aux[g], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming) != cudaSuccess)
+        {
+            delete b;
+            return fail(ctx, LV_EDEVICE, "batch stream/events");
+        }
     *out = b;
     return LV_OK;
 }
@@ -455,13 +536,15 @@ extern "C" lv_status lv_batch_set_config(lv_batch* b, const lv_batch_config* cfg
     else if (cfg->queue == LV_QUEUE_WARP_REFILL)
     {
         if (pixels < 32 || pixels > 1024 || cfg->samples_per_check == 0 ||
-            cfg->samples_per_check > 64 || cfg->tf_shared)
+            cfg->samples_per_check > 64 || cfg->tf_shared || cfg->order != LV_ORDER_RASTER)
             return fail(b->ctx, LV_EINVAL,
                         "warp refill: 32..1024 pixels per tile, samples_per_check in 1..64, "
-                        "no shared transfer function");
+                        "no shared transfer function, raster order");
     }
     else
         return fail(b->ctx, LV_EINVAL, "unknown queue kind");
+    if (cfg->order != LV_ORDER_RASTER && cfg->order != LV_ORDER_LONGEST_FIRST)
+        return fail(b->ctx, LV_EINVAL, "unknown tile order");
     std::lock_guard<std::mutex> lock(b->ctx->mutex);
     b->cfg = *cfg;
     return LV_OK;
@@ -526,6 +609,12 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     st = fill_params(b, views, n, n_run, groups, total_roots, tfn_max);
     if (st != LV_OK)
         return st;
+    uint32_t max_items = 0;
+    for (const Group& g : groups)
+        max_items = std::max(max_items, g.items);
+    st = ensure_order(b, max_items);
+    if (st != LV_OK)
+        return st;
     if (b->cfg.tf_shared && tfn_max > 2048)
         return fail(ctx, LV_EINVAL, "shared-memory transfer functions hold at most 2048 entries");
     uint32_t mask = 0;
@@ -539,7 +628,8 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     {
         const auto key = std::make_tuple(
             n_run, mask, b->cfg.tile_w, b->cfg.tile_h,
-            b->cfg.ctas_per_sm | (b->cfg.queue << 8) | (b->cfg.samples_per_check << 16),
+            b->cfg.ctas_per_sm | (b->cfg.queue << 8) | (b->cfg.samples_per_check << 16) |
+                (b->cfg.order << 24),
             b->cfg.tf_shared ? tfn_max : 0u, b->depth_max, b->generation,
             uintptr_t(b->sel.generation));
         auto it = b->graphs.find(key);
@@ -584,9 +674,11 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     b->last_n = n_run;
     b->last.assign(views, views + n);
     b->pending = true;
-    /* selection: roots + levels + finish; resolve, prune, leaf, step;
-     * one persistent launch per non-empty group */
-    b->launches = b->depth_max + 2u + 4u + uint32_t(__builtin_popcount(mask));
+    /* selection: roots + levels + finish; resolve, prune, leaf, step; per
+     * non-empty group one persistent launch (+ key and order passes) */
+    b->launches = b->depth_max + 2u + 4u +
+                  uint32_t(__builtin_popcount(mask)) *
+                      (b->cfg.order == LV_ORDER_LONGEST_FIRST ? 3u : 1u);
     return LV_OK;
 }
 
@@ -668,16 +760,18 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
     const lv_batch_config start = b->cfg;
     for (const auto& sh : cta_shapes)
         for (uint32_t tfs = 0; tfs < 2; ++tfs)
-        {
-            lv_batch_config c = start;
-            c.queue = LV_QUEUE_CTA_TILES;
-            c.tile_w = sh[0];
-            c.tile_h = sh[1];
-            c.ctas_per_sm = 0;
-            c.tf_shared = tfs;
-            c.samples_per_check = 8;
-            cands.push_back(c);
-        }
+            for (uint32_t ord = 0; ord < 2; ++ord)
+            {
+                lv_batch_config c = start;
+                c.queue = LV_QUEUE_CTA_TILES;
+                c.tile_w = sh[0];
+                c.tile_h = sh[1];
+                c.ctas_per_sm = 0;
+                c.tf_shared = tfs;
+                c.samples_per_check = 8;
+                c.order = ord;
+                cands.push_back(c);
+            }
     for (const auto& sh : warp_shapes)
         for (uint32_t k : checks)
         {
@@ -688,6 +782,7 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
             c.ctas_per_sm = 0;
             c.tf_shared = 0;
             c.samples_per_check = k;
+            c.order = LV_ORDER_RASTER;
             cands.push_back(c);
         }
     lv_batch_config best = start;

@@ -152,6 +152,8 @@ struct TileQueue
     const uint32_t* n_views;    /* device word: views of this group (per launch) */
     uint32_t tile_w, tile_h;
     uint32_t* head;             /* zeroed before the launch */
+    const uint32_t* order;      /* nullable: item k of the queue is work item
+                                   order[k] (longest first) */
     unsigned long long* clock;  /* [first CTA start, last CTA end] in ns (%globaltimer) */
 };
 

@@ -248,6 +248,12 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
                         uint32_t* leaf, uint32_t* counters, RayView& V);
 /* Index of the ray-cast kernel instantiation for a view. */
 int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge);
+/* Longest-first order of a batched group's work items (memset + 2 kernels);
+ * hist: 128 words, keys and order: max_items entries (an upper bound of the
+ * group's items at every replay of a captured launch). */
+lv_status launch_batch_order(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
+                             uint32_t max_items, uint8_t* keys, uint32_t* hist,
+                             uint32_t* order, cudaStream_t s);
 lv_status launch_persistent(lv_ctx* ctx, int variant, const lv_batch_config& cfg,
                             const RayView* d_rays, const TileQueue& Q, uint32_t tfn_max,
                             cudaStream_t s);

@@ -745,7 +745,9 @@ __global__ void __launch_bounds__(256)
     {
         if (threadIdx.x == 0)
         {
-            const uint32_t item = atomicAdd(Q.head, 1u);
+            uint32_t item = atomicAdd(Q.head, 1u);
+            if (Q.order && item < total)
+                item = Q.order[item];
             uint32_t lo = 0, hi = n_views;
             if (item < total)
                 while (hi - lo > 1)
@@ -959,6 +961,71 @@ __device__ __forceinline__ void load_view(RayView* dst, const RayView* src)
     for (uint32_t w = threadIdx.x & 31u; w < sizeof(RayView) / 4; w += 32)
         d[w] = s[w];
     __syncwarp();
+}
+
+/* Longest-first order of the work items of one batched group. The cost of
+ * a (view, tile) item is estimated as the samples of the tile's centre ray,
+ * its length inside the volume times the view's samples per unit length,
+ * in classes of a quarter octave; a counting sort lists the costliest
+ * class first. hist holds the class counts then the scatter cursors, both
+ * zeroed before the key pass. */
+__global__ void __launch_bounds__(256)
+    batch_key_kernel(const RayView* __restrict__ views, TileQueue Q, uint8_t* __restrict__ keys,
+                     uint32_t* __restrict__ hist)
+{
+    __shared__ uint32_t h[kTileBuckets];
+    for (uint32_t i = threadIdx.x; i < kTileBuckets; i += blockDim.x)
+        h[i] = 0;
+    __syncthreads();
+    const uint32_t n_views = *Q.n_views;
+    const uint32_t total = Q.tile_start[n_views];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += gridDim.x * blockDim.x)
+    {
+        const uint32_t gv = find_view(Q, n_views, i);
+        const RayView& V = views[Q.view_ids[gv]];
+        const uint32_t tile = i - Q.tile_start[gv];
+        const uint32_t tiles_x = (V.W + Q.tile_w - 1) / Q.tile_w;
+        const uint32_t px = min((tile % tiles_x) * Q.tile_w + Q.tile_w / 2, V.W - 1);
+        const uint32_t py = min((tile / tiles_x) * Q.tile_h + Q.tile_h / 2, V.H - 1);
+        const RayGeom g = ray_setup(V, px, py);
+        const float len = g.hit && g.tlo <= g.thi ? g.thi - g.tlo : 0.0f;
+        const float est = len * __uint2float_rn(V.counters[FC_SAMPLES_PER_RAY]);
+        const uint32_t q = uint32_t(fminf(log2f(est + 1.0f) * 4.0f, float(kTileBuckets - 1)));
+        const uint32_t key = kTileBuckets - 1u - q;
+        keys[i] = uint8_t(key);
+        atomicAdd(&h[key], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < kTileBuckets; i += blockDim.x)
+        if (h[i])
+            atomicAdd(&hist[i], h[i]);
+}
+
+__global__ void __launch_bounds__(256)
+    batch_order_kernel(TileQueue Q, const uint8_t* __restrict__ keys,
+                       uint32_t* __restrict__ hist, uint32_t* __restrict__ order)
+{
+    __shared__ uint32_t base[kTileBuckets];
+    if (threadIdx.x == 0)
+    {
+        uint32_t acc = 0;
+        for (uint32_t k = 0; k < kTileBuckets; ++k)
+        {
+            base[k] = acc;
+            acc += hist[k];
+        }
+    }
+    __syncthreads();
+    const uint32_t total = Q.tile_start[*Q.n_views];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += gridDim.x * blockDim.x)
+    {
+        const uint32_t key = keys[i];
+        const uint32_t pos = base[key] + atomicAdd(&hist[kTileBuckets + key], 1u);
+        if (pos < total)
+            order[pos] = i;
+    }
 }
 
 __device__ __forceinline__ void flush_samples(const RayView& V, uint32_t nsamp)
@@ -1373,6 +1440,21 @@ lv_status launch_views_pipeline(lv_ctx* ctx, const ResolveView* d_resolve,
     prune_views_kernel<<<dim3(8, n), 256, 0, s>>>(d_resolve);
     leaf_fill_views_kernel<<<dim3(16, n), 256, 0, s>>>(d_resolve);
     step_views_kernel<<<(n + 127) / 128, 128, 0, s>>>(d_rays, n);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+lv_status launch_batch_order(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
+                             uint32_t max_items, uint8_t* keys, uint32_t* hist,
+                             uint32_t* order, cudaStream_t s)
+{
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const uint32_t blocks =
+        std::max(1u, std::min((max_items + 255) / 256, uint32_t(sms) * 4u));
+    LV_CUDA(ctx, cudaMemsetAsync(hist, 0, 2 * kTileBuckets * sizeof(uint32_t), s));
+    batch_key_kernel<<<blocks, 256, 0, s>>>(d_rays, Q, keys, hist);
+    batch_order_kernel<<<blocks, 256, 0, s>>>(Q, keys, hist, order);
     LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;
 }

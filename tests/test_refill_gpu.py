@@ -72,7 +72,9 @@ def test_render_launch_validation(gpu_ctx):
     dict(queue=1, tile_w=16, tile_h=16, samples_per_check=1),
     dict(queue=1, tile_w=32, tile_h=4, samples_per_check=64, ctas_per_sm=2),
     dict(queue=0, tile_w=16, tile_h=8),
+    dict(queue=0, tile_w=16, tile_h=8, order=0),
     dict(queue=0, tile_w=8, tile_h=8, tf_shared=1, ctas_per_sm=3),
+    dict(queue=0, tile_w=8, tile_h=16, tf_shared=1, order=0),
 ])
 def test_batch_queue_kinds_match_single_views(gpu_ctx, cfg):
     """Both work-queue kinds, with and without graphs, give each view the
