@@ -294,6 +294,9 @@ typedef struct lv_frame_stats
     uint32_t error_flags;     /* 0, or the device's index-check code: 1 rendering
                                  set overflow, 2 node outside the octree,
                                  3 brick outside the pool (the access was skipped) */
+    uint32_t n_passes;        /* 1, or the passes of a frame whose visible set
+                                 exceeded the brick pool (renderSync,
+                                 RenderPipeline.cpp:92-158) */
 } lv_frame_stats;
 
 /* One frame of one view: LOD selection, brick residency (streaming misses

@@ -81,6 +81,8 @@ struct RayView
     float tf_mul, tf_add; /* TF texel coordinate = value * tf_mul + tf_add
                              = density * tfn - 0.5 */
     float tf_last;        /* tfn - 1 */
+    uint32_t accumulate;  /* 1: rays start from the colour already in out (a
+                             later pass of a multi-pass frame) */
     uint32_t max_base;    /* last trilinear base voxel of a brick:
                              (N2-2)*N1*N0 + (N1-2)*N0 + N0-2 */
     float early;

@@ -231,6 +231,11 @@ struct Renderer
     /* timing of the last frame: selection and ray cast */
     cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
     uint32_t launches = 0;
+    /* multi-pass frames: the visible set split into pool-sized passes */
+    PinnedBuffer h_pass;     /* visible ids in pass order */
+    DeviceBuffer pass_count; /* visible ids of the current pass */
+    uint32_t passes = 0;     /* passes of the last frame (0: one-pass frame) */
+    lv_frame_stats pass_stats{}; /* summed over the passes */
 };
 
 

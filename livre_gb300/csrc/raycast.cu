@@ -666,6 +666,14 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     return !(r.dst.w > V.early);
 }
 
+/* Colour a ray starts from: the frame so far in a later pass of a
+ * multi-pass frame (RenderPipeline.cpp:92-158 composites every pass into
+ * the same render texture), else transparent black. */
+__device__ __forceinline__ float4 initial_dst(const RayView& V, uint32_t px, uint32_t py)
+{
+    return V.accumulate ? V.out[uint64_t(py) * V.W + px] : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
 /* The whole ray. LOOKAHEAD = 1 loads the voxels of sample k + 1 before
  * sample k is composited, so the two latency chains overlap (a lone long
  * ray runs faster; more registers per thread). Samples, values and the
@@ -673,11 +681,13 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
  * termination the loads of one extra sample are dropped. */
 template <int DT, int FILTER, int TFS, int EDGE, int LOOKAHEAD = 0>
 __device__ float4 march(const RayView& V, const RayGeom& g, float step,
-                        float ac, uint32_t& nsamp)
+                        float ac, uint32_t& nsamp,
+                        float4 init = make_float4(0.f, 0.f, 0.f, 0.f))
 {
     RayState r;
-    if (!ray_begin(g, step, r))
-        return r.dst;
+    if (!ray_begin(g, step, r) || init.w > V.early)
+        return init;
+    r.dst = init;
     if (!LOOKAHEAD)
     {
         while (ray_step<DT, FILTER, TFS, EDGE>(V, r, step, ac, nsamp))
@@ -712,7 +722,8 @@ __global__ void __launch_bounds__(256) raycast_kernel(const RayView V)
     if (px < V.W && py < V.H)
     {
         const RayGeom g = ray_setup(V, px, py);
-        const float4 r = march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp);
+        const float4 r =
+            march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
         V.out[uint64_t(py) * V.W + px] = r;
     }
     /* warp-aggregated 64-bit sample count */
@@ -903,7 +914,7 @@ __global__ void __launch_bounds__(256)
         {
             const RayGeom g = ray_setup(V, px, py);
             V.out[uint64_t(py) * V.W + px] =
-                march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp);
+                march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
         }
     }
     unsigned long long sum = nsamp;
@@ -1116,9 +1127,11 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
                 if (px < V.W && py < V.H)
                 {
                     const RayGeom g = ray_setup(V, px, py);
-                    active = ray_begin(g, K.step, r);
+                    const float4 init = initial_dst(V, px, py);
+                    active = ray_begin(g, K.step, r) && !(init.w > V.early);
+                    r.dst = init;
                     if (!active)
-                        V.out[uint64_t(py) * V.W + px] = r.dst;
+                        V.out[uint64_t(py) * V.W + px] = init;
                 }
             }
         }

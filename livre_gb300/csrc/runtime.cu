@@ -488,6 +488,7 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     V.tf_mul = V.dmul * float(tf->n);
     V.tf_add = V.dadd * float(tf->n) - 0.5f;
     V.tf_last = float(tf->n - 1u);
+    V.accumulate = 0;
     V.max_base = V.edge ? 0u
                         : (V.N[2] - 2u) * V.N[1] * V.N[0] + (V.N[1] - 2u) * V.N[0] + V.N[0] - 2u;
     V.out = reinterpret_cast<float4*>(d_rgba);
@@ -906,6 +907,33 @@ lv_status process_pending(lv_ctx* ctx, cudaStream_t s)
 } // namespace
 } // namespace lv
 
+namespace
+{
+/* Centre of node `id`'s world box, FP32 as LODNode's box
+ * (DataSourcePlugin.cpp:40-71): bricks = rootBlocks << level, the largest
+ * count scales every axis. */
+void node_centre(const lv_volume_info& info, uint64_t id, float c[3])
+{
+    const uint32_t level = nid_level(id);
+    uint32_t bricks[3];
+    for (int i = 0; i < 3; ++i)
+        bricks[i] = info.root_blocks[i] << level;
+    int m = 0;
+    for (int i = 1; i < 3; ++i)
+        if (bricks[i] > bricks[m])
+            m = i;
+    const float denom = float(bricks[m]);
+    const uint32_t pos[3] = {nid_x(id), nid_y(id), nid_z(id)};
+    for (int i = 0; i < 3; ++i)
+    {
+        const float half = info.world_size[i] * 0.5f;
+        const float lo = float(int32_t(pos[i])) / denom * info.world_size[i] - half;
+        const float hi = float(int32_t(pos[i] + 1u)) / denom * info.world_size[i] - half;
+        c[i] = (lo + hi) * 0.5f;
+    }
+}
+} // namespace
+
 extern "C" lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* cfg)
 {
     if (!ctx || !cfg)
@@ -1086,10 +1114,138 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         LV_CUDA(ctx, cudaEventRecord(R.t_ray1, s));
         return LV_OK;
     };
-    st = frame_tail();
+    /* A visible set larger than the brick pool renders in passes of at most
+     * a pool's worth of bricks, front to back by brick distance
+     * (renderSync, RenderPipeline.cpp:92-158; DistanceOperator,
+     * RayCastRenderer.cpp:57-81), each pass compositing on top of the
+     * previous ones. The samples per ray come from the first pass's bricks,
+     * as onFrameStart runs for the first pass only (Renderer.cpp,
+     * RayCastRenderer.cpp:213-233). */
+    auto multipass = [&](uint32_t n_vis, uint64_t per_pass) -> lv_status {
+        const uint32_t m = uint32_t(std::min<uint64_t>(per_pass, 0xFFFFFFFFu));
+        LV_CUDA(ctx, R.h_pass.reserve(sizeof(uint64_t) * n_vis));
+        LV_CUDA(ctx, R.pass_count.reserve(sizeof(uint32_t)));
+        std::vector<uint64_t> ids(n_vis);
+        LV_CUDA(ctx, cudaMemcpyAsync(ids.data(), R.visible.ptr, sizeof(uint64_t) * n_vis,
+                                     cudaMemcpyDeviceToHost, s));
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        std::vector<float> dist(n_vis);
+        std::vector<uint32_t> order(n_vis);
+        const float* mv = desc->camera.modelview; /* column-major */
+        for (uint32_t i = 0; i < n_vis; ++i)
+        {
+            float c[3], e[3];
+            node_centre(info, ids[i], c);
+            for (int k = 0; k < 3; ++k)
+                e[k] = mv[k] * c[0] + mv[4 + k] * c[1] + mv[8 + k] * c[2] + mv[12 + k];
+            dist[i] = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+            order[i] = i;
+        }
+        /* equal distances: lower node id first, so the passes do not depend on
+         * the order the selection emitted the ids in */
+        std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+            return dist[a] < dist[b] || (dist[a] == dist[b] && ids[a] < ids[b]);
+        });
+        uint64_t* hp = R.h_pass.as<uint64_t>();
+        for (uint32_t i = 0; i < n_vis; ++i)
+            hp[i] = ids[order[i]];
+        const uint32_t passes = (n_vis + m - 1) / m;
+        lv_frame_stats agg{};
+        uint32_t n0 = 0;
+        float ray_ms = 0.f;
+        uint32_t* hc = R.h_counters.as<uint32_t>();
+        RV.n_visible_ptr = R.pass_count.as<uint32_t>();
+        RV.synchronous = 1;
+        for (uint32_t p = 0; p < passes; ++p)
+        {
+            const uint32_t fp = p == 0 ? frame : ++R.frame;
+            const uint32_t first = p * m, cnt = std::min(m, n_vis - first);
+            RV.frame = RV.view_frame = fp;
+            LV_CUDA(ctx, cudaMemcpyAsync(R.visible.ptr, hp + first, sizeof(uint64_t) * cnt,
+                                         cudaMemcpyHostToDevice, s));
+            LV_CUDA(ctx, cudaMemcpyAsync(R.pass_count.ptr, &cnt, sizeof(uint32_t),
+                                         cudaMemcpyHostToDevice, s));
+            /* this pass's misses: stream them, evicting earlier passes' bricks
+             * (their stamps are older than fp) */
+            LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
+            lv_status t = launch_resolve(ctx, RV, s);
+            if (t != LV_OK)
+                return t;
+            LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
+                                         cudaMemcpyDeviceToHost, s));
+            LV_CUDA(ctx, cudaStreamSynchronize(s));
+            const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
+            if (missing)
+            {
+                LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
+                                             sizeof(uint64_t) * missing,
+                                             cudaMemcpyDeviceToHost, s));
+                LV_CUDA(ctx, cudaStreamSynchronize(s));
+                uint32_t loaded = 0;
+                uint64_t bytes = 0;
+                t = stream_bricks(ctx, vol, R.h_missing.as<uint64_t>(), missing, fp, s, loaded,
+                                  bytes);
+                R.stats.n_uploaded += loaded;
+                R.stats.bytes_uploaded += bytes;
+                if (t != LV_OK && t != LV_EAGAIN)
+                    return t;
+            }
+            V.accumulate = p > 0 ? 1u : 0u;
+            V.samples_fixed = p > 0 ? n0 : desc->samples_per_ray;
+            t = frame_tail();
+            if (t != LV_OK)
+                return t;
+            LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
+                                         cudaMemcpyDeviceToHost, s));
+            LV_CUDA(ctx, cudaStreamSynchronize(s));
+            if (p == 0)
+                n0 = hc[FC_SAMPLES_PER_RAY];
+            agg.n_rendered += hc[FC_KEPT];
+            agg.n_available += hc[FC_AVAILABLE];
+            agg.n_not_available += hc[FC_NOT_AVAILABLE];
+            agg.max_level = std::max(agg.max_level, hc[FC_MAX_LEVEL]);
+            agg.n_samples += uint64_t(hc[FC_SAMPLES_LO]) | (uint64_t(hc[FC_SAMPLES_HI]) << 32);
+            agg.error_flags = agg.error_flags ? agg.error_flags : hc[FC_ERROR];
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, R.t_ray0, R.t_ray1) == cudaSuccess)
+                ray_ms += ms;
+            else
+                cudaGetLastError();
+        }
+        agg.max_level = agg.max_level ? agg.max_level - 1u : 0u;
+        agg.samples_per_ray = n0;
+        agg.raycast_ms = ray_ms;
+        agg.n_passes = passes;
+        R.pass_stats = agg;
+        R.passes = passes;
+        R.launches += passes * (1u + tail_launches);
+        return LV_OK;
+    };
+    R.passes = 0;
+    bool multi = false;
+    const uint64_t per_pass = ctx->pool->capacity_units / vol->slot_units;
+    if (desc->synchronous && per_pass > 0 && vol->n_nodes > per_pass)
+    {
+        /* the volume may not fit: look at the visible-set size first */
+        uint32_t* hs = R.h_counters.as<uint32_t>() + FC_WORDS;
+        LV_CUDA(ctx, cudaMemcpyAsync(hs, R.sel_result.ptr,
+                                     sizeof(uint32_t) * LV_SELECT_RESULT_WORDS,
+                                     cudaMemcpyDeviceToHost, s));
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        const uint32_t n_vis = hs[LV_SEL_WRITTEN];
+        if (n_vis > per_pass)
+        {
+            multi = true;
+            st = multipass(n_vis, per_pass);
+            if (st != LV_OK)
+                return st;
+        }
+    }
+    if (!multi)
+        st = frame_tail();
     if (st != LV_OK)
         return st;
-    if (desc->synchronous)
+    if (desc->synchronous && !multi)
     {
         uint32_t* hc = R.h_counters.as<uint32_t>();
         LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
@@ -1164,11 +1320,25 @@ extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)
     s.n_samples = uint64_t(hc[FC_SAMPLES_LO]) | (uint64_t(hc[FC_SAMPLES_HI]) << 32);
     s.n_launches = R.launches;
     s.error_flags = hc[FC_ERROR];
+    s.n_passes = 1;
     if (cudaEventElapsedTime(&s.select_ms, R.t_sel0, R.t_sel1) != cudaSuccess ||
         cudaEventElapsedTime(&s.raycast_ms, R.t_ray0, R.t_ray1) != cudaSuccess)
     {
         cudaGetLastError(); /* do not leave the error for the next launch check */
         s.select_ms = s.raycast_ms = 0.f;
+    }
+    if (R.passes)
+    {
+        const lv_frame_stats& P = R.pass_stats;
+        s.n_rendered = P.n_rendered;
+        s.n_available = P.n_available;
+        s.n_not_available = P.n_not_available;
+        s.max_level = P.max_level;
+        s.samples_per_ray = P.samples_per_ray;
+        s.n_samples = P.n_samples;
+        s.raycast_ms = P.raycast_ms;
+        s.error_flags = P.error_flags;
+        s.n_passes = P.n_passes;
     }
     *out = s;
     if (hc[FC_ERROR])

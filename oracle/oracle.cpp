@@ -811,6 +811,10 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
         return -2;
     if (view->n_samples == 0 || tf_n == 0)
         return -1;
+    /* OR_ACCUMULATE: rays start from the colour in `out` (a later pass of a
+     * multi-pass frame, RenderPipeline.cpp:92-158) */
+    const bool accumulate = (mode & OR_ACCUMULATE) != 0;
+    const int base_mode = mode & ~OR_ACCUMULATE;
     RenderSet rs;
     rs.vol = vol;
     rs.dtype = dtype;
@@ -893,6 +897,8 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
     std::atomic<uint64_t> total_samples(0);
 
     auto per_ray = [&](uint32_t px, uint32_t py, double* dst, uint64_t& cnt) {
+        if (dst[3] > sh.early) /* a later pass of an opaque ray */
+            return;
         Ray32 r;
         ray_setup32(fr, gmin, gmax, W, H, px, py, r);
         if (!(r.t0 <= r.t1))
@@ -1076,8 +1082,9 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
             for (uint32_t x = 0; x < W; ++x)
             {
                 double* dst = out + (size_t(y) * W + x) * 4;
-                dst[0] = dst[1] = dst[2] = dst[3] = 0.0;
-                if (mode == OR_MODE_SHADER)
+                if (!accumulate)
+                    dst[0] = dst[1] = dst[2] = dst[3] = 0.0;
+                if (base_mode == OR_MODE_SHADER)
                     shader(x, y, dst, cnt);
                 else
                     per_ray(x, y, dst, cnt);

@@ -106,7 +106,8 @@ float or_exp_neg(float x);
 enum
 {
     OR_MODE_PER_RAY = 0, /* samples on the global grid, per-ray brick order */
-    OR_MODE_SHADER = 1   /* per-brick shader loop, DistanceOperator order */
+    OR_MODE_SHADER = 1,  /* per-brick shader loop, DistanceOperator order */
+    OR_ACCUMULATE = 0x100 /* flag: rays start from the colour in `out` */
 };
 
 typedef struct

@@ -42,6 +42,7 @@ class View(C.Structure):
 
 MODE_PER_RAY = 0
 MODE_SHADER = 1
+ACCUMULATE = 0x100  # flag: rays start from the colour already in `out`
 
 _lib = None
 
@@ -184,11 +185,16 @@ def make_view(mv, proj, width, height, n_samples, alpha_correction=None,
 
 
 def raycast(vol, dtype, node_ids, bricks, tf, view, mode=MODE_PER_RAY, n_threads=0,
-            rows=None):
+            rows=None, init=None):
+    """init: an image to composite behind (mode | ACCUMULATE is implied)."""
     ids = np.ascontiguousarray(node_ids, np.uint64)
     bricks = np.ascontiguousarray(bricks)
     tf = np.ascontiguousarray(tf, np.float32).reshape(-1, 4)
-    out = np.zeros((view.height, view.width, 4), np.float64)
+    if init is None:
+        out = np.zeros((view.height, view.width, 4), np.float64)
+    else:
+        out = np.array(init, np.float64, copy=True, order="C")
+        mode |= ACCUMULATE
     r0, r1 = (0, view.height) if rows is None else rows
     ns = C.c_uint64()
     rc = lib().or_raycast(C.byref(vol), dtype, ids.ctypes.data_as(C.POINTER(C.c_uint64)),
