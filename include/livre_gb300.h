@@ -192,6 +192,38 @@ void lv_volume_destroy(lv_volume* vol);
 /* The derived VolumeInformation of a volume. */
 lv_status lv_volume_get_info(const lv_volume* vol, lv_volume_info* out);
 
+/* Procedural fBm volume: `octaves` octaves of improved Perlin noise
+ * (Perlin 2002) with the given lacunarity and gain, `frequency` noise
+ * periods across the largest volume dimension, the permutation shuffled by
+ * SplitMix64 draws from `seed`; [-1, 1] maps linearly to the full range of
+ * the voxel type. */
+typedef struct lv_fbm_params
+{
+    uint64_t seed;
+    uint32_t octaves;
+    float lacunarity, gain, frequency;
+} lv_fbm_params;
+enum
+{
+    LV_FBM_DEVICE = 0, /* generated on the device, straight into the pool */
+    LV_FBM_HOST = 1    /* generated per brick on the host when it misses (a
+                          data-source callback over host_threads threads),
+                          then streamed host->device */
+};
+lv_status lv_volume_create_fbm(lv_ctx* ctx, const lv_volume_info* info,
+                               const lv_fbm_params* params, uint32_t placement,
+                               uint32_t host_threads, lv_volume** out);
+/* One fBm brick (max_block voxels, x fastest) on the host, as a data-source
+ * plugin's getData would produce it; no context or device needed. The device
+ * generator produces the same bytes. */
+lv_status lv_fbm_brick(const lv_volume_info* info, const lv_fbm_params* params,
+                       uint64_t node_id, void* dst, uint32_t n_threads);
+/* The same bricks for `n` node ids (host array) generated on the device into
+ * d_out (n bricks, packed). Synchronous with `stream`. */
+lv_status lv_fbm_generate(lv_ctx* ctx, const lv_volume_info* info,
+                          const lv_fbm_params* params, const uint64_t* ids, uint32_t n,
+                          void* d_out, void* stream);
+
 /* A volume opened from a URI by the built-in data sources, like
  * livre::DataSource(uri) (livre/data/DataSource.cpp:29-63):
  *   mem://[#w,h,d,block][?datatype=T]   MemoryDataSource (constant bricks)

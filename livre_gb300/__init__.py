@@ -24,7 +24,8 @@ import weakref
 import numpy as np
 
 from . import _abi
-from ._abi import (BLOB_DEVICE, BLOB_HOST, DT_UINT8, DT_UINT16, FILTER_NEAREST,
+from ._abi import (BLOB_DEVICE, BLOB_HOST, DT_UINT8, DT_UINT16, FBM_DEVICE, FBM_HOST,
+                   FILTER_NEAREST,
                    FILTER_TRILINEAR, LAUNCH_GRID, LAUNCH_TILE_QUEUE, LAUNCH_WARP_REFILL,
                    ORDER_LONGEST_FIRST, ORDER_RASTER,
                    QUEUE_CTA_TILES, QUEUE_WARP_REFILL, STEP_HALF_VOXEL,
@@ -252,6 +253,20 @@ def gaussian_peaks_tf(n=256, seed=0, peaks=4):
 
 
 # ------------------------------------------------------------- cameras
+def fbm_params(seed, octaves=6, lacunarity=2.0, gain=0.5, frequency=8.0):
+    return _abi.FbmParams(seed, octaves, lacunarity, gain, frequency)
+
+
+def fbm_brick(vol_info, node_id, seed, octaves=6, lacunarity=2.0, gain=0.5, frequency=8.0,
+              n_threads=0):
+    """One fBm brick generated on the host (lv_fbm_brick): brick_bytes uint8."""
+    out = np.zeros(vol_info.brick_bytes, np.uint8)
+    p = fbm_params(seed, octaves, lacunarity, gain, frequency)
+    check(lib().lv_fbm_brick(C.byref(vol_info.info), C.byref(p), C.c_uint64(int(node_id)),
+                             out.ctypes.data, n_threads))
+    return out
+
+
 def perspective(fovy_deg, aspect, near, far):
     """OpenGL perspective projection, column-major flat (16,) float32."""
     f = 1.0 / math.tan(math.radians(fovy_deg) / 2.0)
@@ -481,6 +496,30 @@ class Context:
         check(lib().lv_volume_create_blob(self.handle, C.byref(vol_info.info), C.byref(d),
                                           placement, C.byref(h)), self.handle)
         return Volume(self, h, vol_info)
+
+    def fbm_volume(self, vol_info, seed, octaves=6, lacunarity=2.0, gain=0.5, frequency=8.0,
+                   placement=FBM_DEVICE, host_threads=0):
+        """Procedural fBm volume (improved Perlin noise), generated per brick on
+        the device (FBM_DEVICE) or on the host when it misses (FBM_HOST)."""
+        p = fbm_params(seed, octaves, lacunarity, gain, frequency)
+        h = C.c_void_p()
+        check(lib().lv_volume_create_fbm(self.handle, C.byref(vol_info.info), C.byref(p),
+                                         placement, host_threads, C.byref(h)), self.handle)
+        return Volume(self, h, vol_info)
+
+    def fbm_bricks(self, vol_info, node_ids, seed, octaves=6, lacunarity=2.0, gain=0.5,
+                   frequency=8.0, stream=None):
+        """fBm bricks of `node_ids` generated on the device, as a device tensor
+        (n, brick_bytes) uint8."""
+        import torch
+        ids = np.ascontiguousarray(node_ids, np.uint64)
+        out = torch.empty((len(ids), vol_info.brick_bytes), dtype=torch.uint8,
+                          device=torch.device("cuda", self.device))
+        p = fbm_params(seed, octaves, lacunarity, gain, frequency)
+        check(lib().lv_fbm_generate(self.handle, C.byref(vol_info.info), C.byref(p),
+                                    ids.ctypes.data_as(C.POINTER(C.c_uint64)), len(ids),
+                                    _ptr(out), _stream(stream)), self.handle)
+        return out
 
     def callback_volume(self, vol_info, get_data):
         """get_data(node_id:int, dst:ctypes buffer address, nbytes:int) -> bool."""

@@ -18,6 +18,7 @@ DT_FLOAT, DT_UINT8, DT_UINT16, DT_UINT32, DT_INT8, DT_INT16, DT_INT32 = range(7)
 FILTER_NEAREST, FILTER_TRILINEAR = 0, 1
 STEP_REFERENCE, STEP_HALF_VOXEL = 0, 1
 BLOB_DEVICE, BLOB_HOST = 0, 1
+FBM_DEVICE, FBM_HOST = 0, 1
 SEL_WRITTEN, SEL_FOUND, SEL_VISITED, SEL_MAX_LEVEL, SEL_OVERFLOW = range(5)
 SELECT_RESULT_WORDS = 8
 
@@ -43,6 +44,11 @@ class LodParams(C.Structure):
 
 class BlobDesc(C.Structure):
     _fields_ = [("n_blobs", C.c_uint32), ("noise", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class FbmParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("octaves", C.c_uint32), ("lacunarity", C.c_float),
+                ("gain", C.c_float), ("frequency", C.c_float)]
 
 
 class RenderDesc(C.Structure):
@@ -153,6 +159,12 @@ _SIGNATURES = {
     "lv_volume_resident": (C.c_int, [C.c_void_p, P(C.c_uint64), C.c_uint32, P(C.c_uint32)]),
     "lv_blob_generate": (C.c_int, [C.c_void_p, P(VolumeInfo), P(BlobDesc), P(C.c_uint64),
                                    C.c_uint32, C.c_void_p, C.c_void_p]),
+    "lv_volume_create_fbm": (C.c_int, [C.c_void_p, P(VolumeInfo), P(FbmParams), C.c_uint32,
+                                       C.c_uint32, P(C.c_void_p)]),
+    "lv_fbm_brick": (C.c_int, [P(VolumeInfo), P(FbmParams), C.c_uint64, C.c_void_p,
+                               C.c_uint32]),
+    "lv_fbm_generate": (C.c_int, [C.c_void_p, P(VolumeInfo), P(FbmParams), P(C.c_uint64),
+                                  C.c_uint32, C.c_void_p, C.c_void_p]),
     "lv_tf_create": (C.c_int, [C.c_void_p, P(C.c_float), C.c_uint32, P(C.c_void_p)]),
     "lv_tf_destroy": (None, [C.c_void_p]),
     "lv_render": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, P(RenderDesc), C.c_void_p,

@@ -186,7 +186,8 @@ enum SourceKind
 {
     SRC_CALLBACK = 0,
     SRC_BLOB_DEVICE = 1,
-    SRC_BLOB_HOST = 2
+    SRC_BLOB_HOST = 2,
+    SRC_FBM_DEVICE = 3
 };
 
 /* One resident brick. */
@@ -256,6 +257,14 @@ int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge);
 /* Longest-first order of a batched group's work items (memset + 2 kernels);
  * hist: 128 words, keys and order: max_items entries (an upper bound of the
  * group's items at every replay of a captured launch). */
+/* fBm bricks for device ids d_ids into `out` (at d_offsets[i] when given,
+ * else packed brick_bytes apart). */
+lv_status launch_fbm_bricks(lv_ctx* ctx, const lv_volume_info& info, const lv_fbm_params& f,
+                            const uint16_t* d_perm, const uint64_t* d_ids, uint32_t n,
+                            uint8_t* out, const uint64_t* d_offsets, uint64_t brick_bytes,
+                            cudaStream_t s);
+std::vector<uint16_t> fbm_permutation(uint64_t seed);
+lv_status volume_init(lv_ctx* ctx, lv_volume* v);
 lv_status launch_batch_order(lv_ctx* ctx, const RayView* d_rays, const TileQueue& Q,
                              uint32_t max_items, uint8_t* keys, uint32_t* hist,
                              uint32_t* order, cudaStream_t s);
@@ -283,6 +292,8 @@ struct lv_volume
     void (*user_free)(void*) = nullptr; /* built-in sources own `user` */
     lv_blob_desc blob{};
     lv::DeviceBuffer d_blobs;
+    lv_fbm_params fbm{};
+    lv::DeviceBuffer d_perm; /* fBm permutation (512 entries) */
     lv::PinnedBuffer host_store;
     uint64_t brick_bytes = 0;
     uint32_t slot_units = 0;

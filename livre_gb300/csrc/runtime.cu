@@ -303,7 +303,7 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                                          cudaMemcpyHostToDevice, up));
             bytes_loaded += vol->brick_bytes;
         }
-        else if (vol->kind == SRC_BLOB_DEVICE)
+        else if (vol->kind == SRC_BLOB_DEVICE || vol->kind == SRC_FBM_DEVICE)
         {
             gen_ids.push_back(id);
             gen_offsets.push_back(uint64_t(unit) * kSlotUnit);
@@ -344,10 +344,14 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                     sizeof(uint64_t) * gen_offsets.size());
         LV_CUDA(ctx, cudaMemcpyAsync(dids.ptr, h.ptr, sizeof(uint64_t) * 2 * gen_ids.size(),
                                      cudaMemcpyHostToDevice, up));
-        lv_status g = launch_blob_bricks(ctx, vol->info, vol->blob,
-                                         vol->d_blobs.as<Blob>(), dids.as<uint64_t>(),
-                                         uint32_t(gen_ids.size()), arena,
-                                         dids.as<uint64_t>() + gen_ids.size(), up);
+        lv_status g =
+            vol->kind == SRC_FBM_DEVICE
+                ? launch_fbm_bricks(ctx, vol->info, vol->fbm, vol->d_perm.as<uint16_t>(),
+                                    dids.as<uint64_t>(), uint32_t(gen_ids.size()), arena,
+                                    dids.as<uint64_t>() + gen_ids.size(), vol->brick_bytes, up)
+                : launch_blob_bricks(ctx, vol->info, vol->blob, vol->d_blobs.as<Blob>(),
+                                     dids.as<uint64_t>(), uint32_t(gen_ids.size()), arena,
+                                     dids.as<uint64_t>() + gen_ids.size(), up);
         if (g != LV_OK)
             return g;
         /* temporaries die at scope exit */

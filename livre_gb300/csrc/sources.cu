@@ -465,6 +465,8 @@ extern "C" lv_status lv_volume_get_data(lv_volume* v, uint64_t node_id, void* ds
         std::memcpy(dst, v->host_store.as<uint8_t>() + idx * v->brick_bytes, v->brick_bytes);
         return LV_OK;
     }
+    if (v->kind == SRC_FBM_DEVICE) /* the host generator gives the same bytes */
+        return lv_fbm_brick(&v->info, &v->fbm, node_id, dst, 0);
     /* device-generated blob bricks */
     lv_ctx* ctx = v->ctx;
     LV_CUDA(ctx, cudaSetDevice(ctx->device));

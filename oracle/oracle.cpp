@@ -800,6 +800,143 @@ int or_blob_brick(const or_volume* vol, const or_blob_params* bp,
     return 0;
 }
 
+/* ---- fBm over improved Perlin noise (the 8192^3 uint16 workload's
+ * synthetic input). Published algorithm: quintic fade 6t^5 - 15t^4 + 10t^3,
+ * gradients (+-1, +-1, 0) and permutations of it chosen by hash & 15 (with
+ * 12..15 repeating four of them), trilinear blend of the eight corner dot
+ * products. */
+namespace
+{
+struct Perlin
+{
+    uint16_t perm[512];
+
+    explicit Perlin(uint64_t seed)
+    {
+        for (uint32_t i = 0; i < 256; ++i)
+            perm[i] = uint16_t(i);
+        uint64_t state = seed;
+        for (uint32_t i = 255; i > 0; --i)
+        {
+            state += 0x9E3779B97F4A7C15ull;
+            uint64_t z = state;
+            z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+            z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+            z ^= z >> 31;
+            const uint32_t j = uint32_t(z % (i + 1u));
+            const uint16_t t = perm[i];
+            perm[i] = perm[j];
+            perm[j] = t;
+        }
+        for (uint32_t i = 0; i < 256; ++i)
+            perm[256 + i] = perm[i];
+    }
+
+    static float smooth(float t)
+    {
+        const float inner = t * (t * 6.0f - 15.0f) + 10.0f;
+        return t * t * t * inner;
+    }
+    static float mix(float w, float a, float b) { return a + w * (b - a); }
+    static float corner(uint32_t h, float x, float y, float z)
+    {
+        switch (h & 15u)
+        {
+        case 0: return x + y;
+        case 1: return -x + y;
+        case 2: return x + -y;
+        case 3: return -x + -y;
+        case 4: return x + z;
+        case 5: return -x + z;
+        case 6: return x + -z;
+        case 7: return -x + -z;
+        case 8: return y + z;
+        case 9: return -y + z;
+        case 10: return y + -z;
+        case 11: return -y + -z;
+        case 12: return y + x;
+        case 13: return -y + z;
+        case 14: return y + -x;
+        default: return -y + -z;
+        }
+    }
+
+    float operator()(float x, float y, float z) const
+    {
+        const float xf = std::floor(x), yf = std::floor(y), zf = std::floor(z);
+        const uint32_t xi = uint32_t(int32_t(xf)) & 255u, yi = uint32_t(int32_t(yf)) & 255u,
+                       zi = uint32_t(int32_t(zf)) & 255u;
+        const float dx = x - xf, dy = y - yf, dz = z - zf;
+        const float u = smooth(dx), v = smooth(dy), w = smooth(dz);
+        float c[2][2][2];
+        for (uint32_t k = 0; k < 2; ++k)
+            for (uint32_t j = 0; j < 2; ++j)
+                for (uint32_t i = 0; i < 2; ++i)
+                {
+                    const uint32_t h = perm[perm[perm[xi + i] + yi + j] + zi + k];
+                    c[k][j][i] = corner(h, i ? dx - 1.0f : dx, j ? dy - 1.0f : dy,
+                                        k ? dz - 1.0f : dz);
+                }
+        const float y0 = mix(v, mix(u, c[0][0][0], c[0][0][1]), mix(u, c[0][1][0], c[0][1][1]));
+        const float y1 = mix(v, mix(u, c[1][0][0], c[1][0][1]), mix(u, c[1][1][0], c[1][1][1]));
+        return mix(w, y0, y1);
+    }
+};
+} // namespace
+
+float or_perlin(uint64_t seed, float x, float y, float z)
+{
+    return Perlin(seed)(x, y, z);
+}
+
+int or_fbm_brick(const or_volume* vol, const or_fbm_params* fp, uint64_t id, void* out)
+{
+    const uint32_t level = nid_level(id);
+    if (level >= vol->depth || fp->octaves == 0)
+        return -1;
+    const Perlin noise(fp->seed);
+    const uint32_t shift = vol->depth - 1u - level;
+    const uint32_t s = 1u << shift;
+    const uint32_t vmax = std::max(vol->voxels[0], std::max(vol->voxels[1], vol->voxels[2]));
+    const float scale = float(s) * (fp->frequency / float(vmax));
+    const uint32_t pos[3] = {nid_x(id), nid_y(id), nid_z(id)};
+    const uint32_t* N = vol->max_block;
+    int32_t base[3], last[3];
+    for (int a = 0; a < 3; ++a)
+    {
+        base[a] = int32_t(pos[a] * (N[a] - 2u * vol->overlap[a])) - int32_t(vol->overlap[a]);
+        last[a] = int32_t((vol->voxels[a] + s - 1u) >> shift) - 1;
+    }
+    const float top = fp->dtype == 2 ? 65535.0f : 255.0f;
+    size_t idx = 0;
+    for (uint32_t k = 0; k < N[2]; ++k)
+        for (uint32_t j = 0; j < N[1]; ++j)
+            for (uint32_t i = 0; i < N[0]; ++i, ++idx)
+            {
+                const uint32_t off[3] = {i, j, k};
+                float p[3];
+                for (int a = 0; a < 3; ++a)
+                {
+                    const int32_t g = std::min(std::max(base[a] + int32_t(off[a]), 0), last[a]);
+                    p[a] = (float(g) + 0.5f) * scale;
+                }
+                float sum = 0.0f, amp = 1.0f, f = 1.0f;
+                for (uint32_t o = 0; o < fp->octaves; ++o)
+                {
+                    sum = sum + amp * noise(p[0] * f, p[1] * f, p[2] * f);
+                    amp = amp * fp->gain;
+                    f = f * fp->lacunarity;
+                }
+                const float v = std::min(std::max(sum, -1.0f), 1.0f);
+                const uint32_t q = uint32_t(std::floor((v + 1.0f) * 0.5f * top + 0.5f));
+                if (fp->dtype == 2)
+                    static_cast<uint16_t*>(out)[idx] = uint16_t(q);
+                else
+                    static_cast<uint8_t*>(out)[idx] = uint8_t(q);
+            }
+    return 0;
+}
+
 int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
                uint32_t n_nodes, const void* bricks, const float* tf_rgba,
                uint32_t tf_n, const or_view* view, int mode, int n_threads,

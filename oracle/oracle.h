@@ -102,6 +102,26 @@ float or_blob_value(const or_volume* vol, const or_blob_params* bp, float x,
                     float y, float z);
 float or_exp_neg(float x);
 
+/* Procedural fBm volume (the out-of-core workload): improved Perlin noise
+ * (Perlin 2002) summed over octaves, the permutation a SplitMix64-seeded
+ * Fisher-Yates shuffle, [-1, 1] mapped to the voxel type's range. Every
+ * float operation is a single IEEE round-to-nearest op in a fixed order
+ * (built without contraction) so the device generator produces identical
+ * bytes. Parity unpinned: no reference test or golden vector covers it; it
+ * is the synthetic input of the 8192^3 uint16 workload. */
+typedef struct
+{
+    uint64_t seed;
+    uint32_t octaves;
+    float lacunarity, gain, frequency;
+    uint32_t dtype; /* 1 = uint8, 2 = uint16 */
+} or_fbm_params;
+
+int or_fbm_brick(const or_volume* vol, const or_fbm_params* fp, uint64_t node_id,
+                 void* out);
+/* The noise field itself (one octave) at a point, for spot checks. */
+float or_perlin(uint64_t seed, float x, float y, float z);
+
 /* Ray cast. */
 enum
 {

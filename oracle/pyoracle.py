@@ -31,6 +31,11 @@ class BlobParams(C.Structure):
                 ("dtype", C.c_uint32), ("seed", C.c_uint64)]
 
 
+class FbmParams(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("octaves", C.c_uint32), ("lacunarity", C.c_float),
+                ("gain", C.c_float), ("frequency", C.c_float), ("dtype", C.c_uint32)]
+
+
 class View(C.Structure):
     _fields_ = [("mv", C.c_float * 16), ("proj", C.c_float * 16),
                 ("width", C.c_uint32), ("height", C.c_uint32),
@@ -66,6 +71,10 @@ def lib():
         L.or_blob_brick.argtypes = [C.POINTER(Volume), C.POINTER(BlobParams), C.c_uint64, C.c_void_p]
         L.or_blob_value.argtypes = [C.POINTER(Volume), C.POINTER(BlobParams), C.c_float, C.c_float, C.c_float]
         L.or_blob_value.restype = C.c_float
+        L.or_fbm_brick.argtypes = [C.POINTER(Volume), C.POINTER(FbmParams), C.c_uint64,
+                                   C.c_void_p]
+        L.or_perlin.argtypes = [C.c_uint64, C.c_float, C.c_float, C.c_float]
+        L.or_perlin.restype = C.c_float
         L.or_exp_neg.argtypes = [C.c_float]
         L.or_exp_neg.restype = C.c_float
         L.or_raycast.argtypes = [
@@ -160,6 +169,25 @@ def blob_brick(vol, bp, node_id):
     if lib().or_blob_brick(C.byref(vol), C.byref(bp), C.c_uint64(node_id), out.ctypes.data) != 0:
         raise ValueError("bad node")
     return out
+
+
+def fbm_params(seed, octaves=6, lacunarity=2.0, gain=0.5, frequency=8.0, dtype=2):
+    p = FbmParams()
+    p.seed, p.octaves, p.lacunarity, p.gain, p.frequency, p.dtype = (
+        seed, octaves, lacunarity, gain, frequency, dtype)
+    return p
+
+
+def fbm_brick(vol, fp, node_id):
+    n = vol.max_block[0] * vol.max_block[1] * vol.max_block[2]
+    out = np.zeros(n, np.uint16 if fp.dtype == 2 else np.uint8)
+    if lib().or_fbm_brick(C.byref(vol), C.byref(fp), C.c_uint64(node_id), out.ctypes.data) != 0:
+        raise ValueError("bad node")
+    return out
+
+
+def perlin(seed, x, y, z):
+    return lib().or_perlin(seed, float(x), float(y), float(z))
 
 
 def exp_neg(x):
