@@ -548,6 +548,17 @@ void lv_server_destroy(lv_server* server);
 lv_status lv_frame_to_rgba8(lv_ctx* ctx, const float* d_rgba, uint32_t width,
                             uint32_t height, uint8_t* d_out, void* stream);
 
+/* The frame grab (livre/eq/FrameGrabber.cpp:55-111 encodes the channel image
+ * as JPEG): an RGBA8 frame (host, row 0 at the bottom) as a lossless PNG
+ * written top row first. out = NULL returns the size only; LV_ENOMEM when
+ * capacity is too small. No context or device needed. */
+lv_status lv_frame_encode_png(const uint8_t* rgba8, uint32_t width, uint32_t height,
+                              uint8_t* out, size_t capacity, size_t* size);
+/* An RGBA32F device frame converted like lv_frame_to_rgba8 and written to
+ * `path` as PNG. Synchronous. */
+lv_status lv_frame_write_png(lv_ctx* ctx, const float* d_rgba, uint32_t width,
+                             uint32_t height, const char* path);
+
 #ifdef __cplusplus
 }
 #endif

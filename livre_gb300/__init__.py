@@ -253,6 +253,17 @@ def gaussian_peaks_tf(n=256, seed=0, peaks=4):
 
 
 # ------------------------------------------------------------- cameras
+def encode_png(rgba8):
+    """PNG bytes of an (H, W, 4) uint8 frame whose row 0 is the bottom row."""
+    a = np.ascontiguousarray(rgba8, np.uint8)
+    H, W = a.shape[:2]
+    size = C.c_size_t()
+    check(lib().lv_frame_encode_png(a.ctypes.data, W, H, None, 0, C.byref(size)))
+    out = (C.c_uint8 * size.value)()
+    check(lib().lv_frame_encode_png(a.ctypes.data, W, H, out, size.value, C.byref(size)))
+    return bytes(out)
+
+
 def fbm_params(seed, octaves=6, lacunarity=2.0, gain=0.5, frequency=8.0):
     return _abi.FbmParams(seed, octaves, lacunarity, gain, frequency)
 
@@ -586,6 +597,12 @@ class Context:
         check(lib().lv_render(self.handle, volume.handle, tf.handle, C.byref(desc), _ptr(out),
                               _stream(stream)), self.handle)
         return out
+
+    def write_png(self, frame, path):
+        """Writes an (H, W, 4) float32 device frame as a PNG file."""
+        H, W = frame.shape[:2]
+        check(lib().lv_frame_write_png(self.handle, C.c_void_p(frame.data_ptr()), W, H,
+                                       str(path).encode()), self.handle)
 
     def render_launch(self):
         """lv_render's ray-cast launch shape (lv_get_render_launch)."""

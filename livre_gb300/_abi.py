@@ -159,6 +159,10 @@ _SIGNATURES = {
     "lv_volume_resident": (C.c_int, [C.c_void_p, P(C.c_uint64), C.c_uint32, P(C.c_uint32)]),
     "lv_blob_generate": (C.c_int, [C.c_void_p, P(VolumeInfo), P(BlobDesc), P(C.c_uint64),
                                    C.c_uint32, C.c_void_p, C.c_void_p]),
+    "lv_frame_encode_png": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p,
+                                      C.c_size_t, P(C.c_size_t)]),
+    "lv_frame_write_png": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                     C.c_char_p]),
     "lv_volume_create_fbm": (C.c_int, [C.c_void_p, P(VolumeInfo), P(FbmParams), C.c_uint32,
                                        C.c_uint32, P(C.c_void_p)]),
     "lv_fbm_brick": (C.c_int, [P(VolumeInfo), P(FbmParams), C.c_uint64, C.c_void_p,
