@@ -329,6 +329,7 @@ typedef struct lv_frame_stats
     uint32_t n_passes;        /* 1, or the passes of a frame whose visible set
                                  exceeded the brick pool (renderSync,
                                  RenderPipeline.cpp:92-158) */
+    float stream_ms;          /* host time spent fetching and streaming bricks */
 } lv_frame_stats;
 
 /* One frame of one view: LOD selection, brick residency (streaming misses

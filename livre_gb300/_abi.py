@@ -67,7 +67,7 @@ class FrameStats(C.Structure):
                 ("n_samples", C.c_uint64), ("bytes_uploaded", C.c_uint64),
                 ("n_launches", C.c_uint32), ("select_ms", C.c_float),
                 ("raycast_ms", C.c_float), ("error_flags", C.c_uint32),
-                ("n_passes", C.c_uint32)]
+                ("n_passes", C.c_uint32), ("stream_ms", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -305,6 +305,7 @@ struct lv_volume
      * requests are never evicted (empty until a server uses the volume) */
     std::vector<uint16_t> pins;
     uint32_t time_step = 0;
+    bool streamed_last = false; /* the last synchronous frame streamed bricks */
     /* pinned staging ring for callback sources */
     std::vector<lv::PinnedBuffer*> staging;
     std::vector<cudaEvent_t> staging_ev;

@@ -18,6 +18,7 @@
  * full the oldest brick not in use by the frame being built is evicted
  * (objects still referenced are skipped, Cache.cpp:141-156).
  */
+#include <chrono>
 #include <algorithm>
 #include <cmath>
 #include <list>
@@ -1102,6 +1103,15 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     /* residency pass, leaf grid and ray cast, enqueued without a host round
      * trip; the synchronous mode checks for misses once the frame is done
      * and, only if some brick was missing, streams it and renders again */
+    auto timed_stream = [&](const uint64_t* ids, uint32_t n, uint32_t protect,
+                            uint32_t& loaded, uint64_t& bytes) -> lv_status {
+        const auto t0 = std::chrono::steady_clock::now();
+        const lv_status r = stream_bricks(ctx, vol, ids, n, protect, s, loaded, bytes);
+        R.stats.stream_ms += std::chrono::duration<float, std::milli>(
+                                 std::chrono::steady_clock::now() - t0)
+                                 .count();
+        return r;
+    };
     auto frame_tail = [&]() -> lv_status {
         LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
         lv_status t = launch_resolve(ctx, RV, s);
@@ -1187,8 +1197,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                 LV_CUDA(ctx, cudaStreamSynchronize(s));
                 uint32_t loaded = 0;
                 uint64_t bytes = 0;
-                t = stream_bricks(ctx, vol, R.h_missing.as<uint64_t>(), missing, fp, s, loaded,
-                                  bytes);
+                t = timed_stream(R.h_missing.as<uint64_t>(), missing, fp, loaded, bytes);
                 R.stats.n_uploaded += loaded;
                 R.stats.bytes_uploaded += bytes;
                 if (t != LV_OK && t != LV_EAGAIN)
@@ -1245,6 +1254,36 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                 return st;
         }
     }
+    if (!multi && desc->synchronous && vol->streamed_last)
+    {
+        /* this volume's last frame streamed bricks: find this frame's misses
+         * and stream them before the ray cast, instead of ray casting, then
+         * streaming and ray casting again */
+        uint32_t* hc = R.h_counters.as<uint32_t>();
+        LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
+        st = launch_resolve(ctx, RV, s);
+        if (st != LV_OK)
+            return st;
+        LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
+                                     cudaMemcpyDeviceToHost, s));
+        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
+        if (missing)
+        {
+            LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
+                                         sizeof(uint64_t) * missing,
+                                         cudaMemcpyDeviceToHost, s));
+            LV_CUDA(ctx, cudaStreamSynchronize(s));
+            uint32_t loaded = 0;
+            uint64_t bytes = 0;
+            st = timed_stream(R.h_missing.as<uint64_t>(), missing, frame, loaded, bytes);
+            R.stats.n_uploaded += loaded;
+            R.stats.bytes_uploaded += bytes;
+            if (st != LV_OK && st != LV_EAGAIN)
+                return st;
+        }
+        R.launches += 1;
+    }
     if (!multi)
         st = frame_tail();
     if (st != LV_OK)
@@ -1264,8 +1303,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             LV_CUDA(ctx, cudaStreamSynchronize(s));
             uint32_t loaded = 0;
             uint64_t bytes = 0;
-            st = stream_bricks(ctx, vol, R.h_missing.as<uint64_t>(), missing, frame, s,
-                               loaded, bytes);
+            st = timed_stream(R.h_missing.as<uint64_t>(), missing, frame, loaded, bytes);
             R.stats.n_uploaded += loaded;
             R.stats.bytes_uploaded += bytes;
             if (st != LV_OK && st != LV_EAGAIN)
@@ -1296,6 +1334,8 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         R.pending_max = desc->max_uploads;
         R.pending_frame = frame;
     }
+    if (desc->synchronous)
+        vol->streamed_last = R.stats.n_uploaded > 0;
     R.last_stream = s;
     R.have_last = true;
     return LV_OK;
