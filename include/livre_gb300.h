@@ -410,8 +410,12 @@ enum
 {
     LV_QUEUE_CTA_TILES = 0,  /* a CTA per work item: tile_w x tile_h threads,
                                 one ray each */
-    LV_QUEUE_WARP_REFILL = 1 /* a warp per work item: the tile's pixels are
-                                handed to lanes as their rays finish */
+    LV_QUEUE_WARP_REFILL = 1, /* a warp per work item: the tile's pixels are
+                                 handed to lanes as their rays finish */
+    LV_QUEUE_VIEW_KERNELS = 2 /* one tile-queue ray cast per view (lv_render's
+                                 kernel, view constants as kernel parameters)
+                                 on parallel streams, so a view's last tiles
+                                 overlap the next view; no CUDA graph */
 };
 
 /* Launch shape of the persistent ray-cast kernel. */
@@ -459,8 +463,8 @@ lv_status lv_batch_graph_stats(lv_batch* batch, uint64_t* captures,
                                uint64_t* replays, uint32_t* cached);
 /* Times the persistent ray cast on this batch (reps timed launches each)
  * for CTA tiles of {8x8, 16x8, 8x16, 16x16, 32x4, 32x8} pixels with and
- * without transfer-function staging in raster and longest-first order, and
- * for warp-refill tiles of {8x4, 8x8,
+ * without transfer-function staging in raster and longest-first order, per-view
+ * kernels of {8x8, 8x16} tiles in both orders, and for warp-refill tiles of {8x4, 8x8,
  * 16x8, 16x16} pixels with refills every {2, 8, 32} samples, all on a
  * resident grid; keeps the fastest configuration and returns it in
  * `chosen`. */

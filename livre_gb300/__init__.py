@@ -28,7 +28,7 @@ from ._abi import (BLOB_DEVICE, BLOB_HOST, DT_UINT8, DT_UINT16, FBM_DEVICE, FBM_
                    FILTER_NEAREST,
                    FILTER_TRILINEAR, LAUNCH_GRID, LAUNCH_TILE_QUEUE, LAUNCH_WARP_REFILL,
                    ORDER_LONGEST_FIRST, ORDER_RASTER,
-                   QUEUE_CTA_TILES, QUEUE_WARP_REFILL, STEP_HALF_VOXEL,
+                   QUEUE_CTA_TILES, QUEUE_VIEW_KERNELS, QUEUE_WARP_REFILL, STEP_HALF_VOXEL,
                    STEP_REFERENCE, LivreError, check, lib)
 
 __all__ = ["NodeId", "VolumeInformation", "VolumeRendererParameters", "TransferFunction1D",
@@ -671,8 +671,8 @@ class Batch:
         """order: ORDER_LONGEST_FIRST (default for CTA tiles) or ORDER_RASTER
         (the only order of warp refill)."""
         if order is None:
-            order = (_abi.ORDER_LONGEST_FIRST if queue == _abi.QUEUE_CTA_TILES
-                     else _abi.ORDER_RASTER)
+            order = (_abi.ORDER_RASTER if queue == _abi.QUEUE_WARP_REFILL
+                     else _abi.ORDER_LONGEST_FIRST)
         c = _abi.BatchConfig(tile_w, tile_h, ctas_per_sm, tf_shared, use_graph, queue,
                              samples_per_check, order)
         check(lib().lv_batch_set_config(self.handle, C.byref(c)), self.ctx.handle)

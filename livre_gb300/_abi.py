@@ -80,6 +80,7 @@ class BatchView(C.Structure):
 
 QUEUE_CTA_TILES = 0
 QUEUE_WARP_REFILL = 1
+QUEUE_VIEW_KERNELS = 2
 
 
 class BatchConfig(C.Structure):

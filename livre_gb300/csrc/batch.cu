@@ -56,7 +56,7 @@ struct lv_batch
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr, user_ready = nullptr;
     cudaEvent_t t_sel0 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
-    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_CTA_TILES, 8, LV_ORDER_LONGEST_FIRST};
+    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_VIEW_KERNELS, 8, LV_ORDER_RASTER};
     /* per-group longest-first order: hist (128 words) | keys | order, each
      * group at a fixed offset sized for order_cap items (grow-only) */
     lv::DeviceBuffer order_buf;
@@ -64,7 +64,23 @@ struct lv_batch
     /* one stream per non-first group: the groups' persistent launches run
      * side by side, so one group's last tiles overlap the next group */
     cudaStream_t aux[8] = {};
+    cudaStream_t aux_low[8] = {}; /* lowest priority: a batch overlapping another */
+    bool low_priority = false;
     cudaEvent_t fork = nullptr, join[8] = {};
+    /* per-view kernels: tile-order scratch and ray-cast timing */
+    lv::DeviceBuffer view_scratch;
+    cudaEvent_t t_vk0 = nullptr, t_vk1 = nullptr;
+    bool vk_timed = false;
+    /* per-view completion hook (per-view kernels only) */
+    lv::BatchViewDone hook = nullptr;
+    void* hook_user = nullptr;
+    lv::PinnedBuffer h_view_words;
+    struct HookArg
+    {
+        lv_batch* b;
+        uint32_t view;
+    };
+    std::vector<HookArg> hook_args;
     /* per-view region strides (grow-only) */
     uint64_t nodes_stride = 0, cells_stride = 0, missing_stride = 0;
     uint32_t views_cap = 0;
@@ -106,12 +122,18 @@ struct lv_batch
             cudaEventDestroy(t_ray1);
         if (fork)
             cudaEventDestroy(fork);
+        if (t_vk0)
+            cudaEventDestroy(t_vk0);
+        if (t_vk1)
+            cudaEventDestroy(t_vk1);
         for (int g = 0; g < 8; ++g)
         {
             if (join[g])
                 cudaEventDestroy(join[g]);
             if (aux[g])
                 cudaStreamDestroy(aux[g]);
+            if (aux_low[g])
+                cudaStreamDestroy(aux_low[g]);
         }
         if (stream)
             cudaStreamDestroy(stream);
@@ -394,6 +416,14 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n, uint3
     return LV_OK;
 }
 
+void CUDART_CB view_done_trampoline(void* p)
+{
+    const auto* a = static_cast<const lv_batch::HookArg*>(p);
+    lv_batch* b = a->b;
+    if (b->hook)
+        b->hook(b->hook_user, a->view, b->h_view_words.as<uint32_t>() + kOutWords * a->view);
+}
+
 lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& groups,
                         uint32_t total_roots, uint32_t tfn_max)
 {
@@ -419,10 +449,68 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     uint32_t* heads = b->zeroed.as<uint32_t>() + kOutWords * n; /* kGroups words */
     unsigned long long* clock = reinterpret_cast<unsigned long long*>(heads + kGroups);
     const RayView* d_rays = reinterpret_cast<RayView*>(d + PL.ray);
+    b->vk_timed = false;
+    cudaStream_t* aux = b->low_priority ? b->aux_low : b->aux;
+    if (b->cfg.queue == LV_QUEUE_VIEW_KERNELS)
+    {
+        /* lv_render's ray cast per view, views spread over the aux streams */
+        const RayView* h_rays = reinterpret_cast<const RayView*>(b->h_params.as<uint8_t>() + PL.ray);
+        const lv_render_launch L{LV_LAUNCH_TILE_QUEUE, b->cfg.tile_w, b->cfg.tile_h, 0,
+                                 b->cfg.order, 0};
+        std::vector<uint64_t> offs(n + 1, 0);
+        for (uint32_t i = 0; i < n; ++i)
+            offs[i + 1] = offs[i] + ((tile_order_bytes(h_rays[i], L) + 255) & ~size_t(255));
+        if (b->cfg.order == LV_ORDER_LONGEST_FIRST && b->view_scratch.bytes < offs[n])
+        {
+            LV_CUDA(ctx, cudaStreamSynchronize(s));
+            LV_CUDA(ctx, b->view_scratch.reserve(offs[n] + offs[n] / 2));
+        }
+        if (b->hook)
+        {
+            LV_CUDA(ctx, b->h_view_words.reserve(sizeof(uint32_t) * kOutWords * n));
+            b->hook_args.resize(n);
+            for (uint32_t i = 0; i < n; ++i)
+                b->hook_args[i] = lv_batch::HookArg{b, i};
+        }
+        LV_CUDA(ctx, cudaEventRecord(b->t_vk0, s));
+        LV_CUDA(ctx, cudaEventRecord(b->fork, s));
+        const uint32_t n_streams = std::min<uint32_t>(n, kGroups);
+        for (uint32_t k = 0; k < n_streams; ++k)
+            LV_CUDA(ctx, cudaStreamWaitEvent(aux[k], b->fork, 0));
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            if (h_rays[i].W == 0) /* padding view */
+                continue;
+            uint8_t* scratch = b->cfg.order == LV_ORDER_LONGEST_FIRST
+                                   ? b->view_scratch.as<uint8_t>() + offs[i]
+                                   : nullptr;
+            cudaStream_t vs = aux[i % n_streams];
+            st = launch_view_raycast(ctx, h_rays[i], L, scratch, vs);
+            if (st != LV_OK)
+                return st;
+            if (b->hook)
+            {
+                /* this view is done: its counters to the host, then the hook */
+                LV_CUDA(ctx, cudaMemcpyAsync(b->h_view_words.as<uint32_t>() + kOutWords * i,
+                                             b->zeroed.as<uint32_t>() + kOutWords * i,
+                                             sizeof(uint32_t) * kOutWords,
+                                             cudaMemcpyDeviceToHost, vs));
+                LV_CUDA(ctx, cudaLaunchHostFunc(vs, view_done_trampoline, &b->hook_args[i]));
+            }
+        }
+        for (uint32_t k = 0; k < n_streams; ++k)
+        {
+            LV_CUDA(ctx, cudaEventRecord(b->join[k], aux[k]));
+            LV_CUDA(ctx, cudaStreamWaitEvent(s, b->join[k], 0));
+        }
+        LV_CUDA(ctx, cudaEventRecord(b->t_vk1, s));
+        b->vk_timed = true;
+    }
     const bool ordered = b->cfg.order == LV_ORDER_LONGEST_FIRST;
     bool first = true;
-    LV_CUDA(ctx, cudaEventRecord(b->fork, s));
-    for (int g = 0; g < kGroups; ++g)
+    if (!b->vk_timed)
+        LV_CUDA(ctx, cudaEventRecord(b->fork, s));
+    for (int g = 0; g < kGroups && !b->vk_timed; ++g)
     {
         if (groups[g].views.empty())
             continue;
@@ -436,7 +524,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         Q.clock = clock;
         Q.order = nullptr;
         /* the first group on the batch stream, the others each on its own */
-        cudaStream_t gs = first ? s : b->aux[g];
+        cudaStream_t gs = first ? s : aux[g];
         if (!first)
             LV_CUDA(ctx, cudaStreamWaitEvent(gs, b->fork, 0));
         if (ordered)
@@ -475,6 +563,38 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
 
 } // namespace
 
+namespace lv
+{
+void batch_set_low_priority(lv_batch* b, bool low)
+{
+    std::lock_guard<std::mutex> lock(b->ctx->mutex);
+    b->low_priority = low;
+}
+
+void batch_set_view_hook(lv_batch* b, BatchViewDone fn, void* user)
+{
+    std::lock_guard<std::mutex> lock(b->ctx->mutex);
+    b->hook = fn;
+    b->hook_user = user;
+}
+
+void batch_decode_stats(const uint32_t* c, lv_frame_stats& s)
+{
+    const uint32_t* sel = c + FC_WORDS;
+    s = lv_frame_stats{};
+    s.n_visible = sel[LV_SEL_WRITTEN];
+    s.n_visited = sel[LV_SEL_VISITED];
+    s.n_rendered = c[FC_KEPT];
+    s.n_available = c[FC_AVAILABLE];
+    s.n_not_available = c[FC_NOT_AVAILABLE];
+    s.max_level = c[FC_MAX_LEVEL] ? c[FC_MAX_LEVEL] - 1u : 0u;
+    s.samples_per_ray = c[FC_SAMPLES_PER_RAY];
+    s.n_samples = uint64_t(c[FC_SAMPLES_LO]) | (uint64_t(c[FC_SAMPLES_HI]) << 32);
+    s.error_flags = c[FC_ERROR];
+    s.n_passes = 1;
+}
+} // namespace lv
+
 /* ================================================================ C ABI */
 extern "C" lv_status lv_batch_create(lv_ctx* ctx, lv_batch** out)
 {
@@ -492,13 +612,21 @@ extern "C" lv_status lv_batch_create(lv_ctx* ctx, lv_batch** out)
         cudaEventCreateWithFlags(&b->user_ready, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreate(&b->t_sel0) != cudaSuccess || cudaEventCreate(&b->t_ray0) != cudaSuccess ||
         cudaEventCreate(&b->t_ray1) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&b->t_vk0) != cudaSuccess || cudaEventCreate(&b->t_vk1) != cudaSuccess)
     {
         delete b;
         return fail(ctx, LV_EDEVICE, "batch stream/events");
     }
+    /* ray-cast streams one step below the highest priority (kept for
+     * admission work); the low set at the lowest priority */
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    const int high = greatest < least ? greatest + 1 : greatest;
     for (int g = 0; g < kGroups; ++g)
-        if (cudaStreamCreateWithFlags(&b->aux[g], cudaStreamNonBlocking) != cudaSuccess ||
+        if (cudaStreamCreateWithPriority(&b->aux[g], cudaStreamNonBlocking, high) != cudaSuccess ||
+            cudaStreamCreateWithPriority(&b->aux_low[g], cudaStreamNonBlocking, least) !=
+                cudaSuccess ||
             cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming) != cudaSuccess)
         {
             delete b;
@@ -541,6 +669,13 @@ extern "C" lv_status lv_batch_set_config(lv_batch* b, const lv_batch_config* cfg
                         "warp refill: 32..1024 pixels per tile, samples_per_check in 1..64, "
                         "no shared transfer function, raster order");
     }
+    else if (cfg->queue == LV_QUEUE_VIEW_KERNELS)
+    {
+        if (pixels == 0 || pixels > 256 || pixels % 32 != 0 || cfg->tf_shared)
+            return fail(b->ctx, LV_EINVAL,
+                        "view kernels: tile_w * tile_h a multiple of 32 up to 256, no shared "
+                        "transfer function");
+    }
     else
         return fail(b->ctx, LV_EINVAL, "unknown queue kind");
     if (cfg->order != LV_ORDER_RASTER && cfg->order != LV_ORDER_LONGEST_FIRST)
@@ -581,7 +716,8 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     /* the host staging is read by the previous launch until it completes */
     LV_CUDA(ctx, cudaEventSynchronize(b->done));
     uint32_t n_run = n;
-    if (b->cfg.use_graph)
+    const bool graphed = b->cfg.use_graph && b->cfg.queue != LV_QUEUE_VIEW_KERNELS;
+    if (graphed)
         while (n_run & (n_run - 1))
             n_run += n_run & (~n_run + 1); /* round up to a power of two */
     st = ensure_regions(b, views, n, user, n_run);
@@ -624,7 +760,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     LV_CUDA(ctx, cudaEventRecord(b->user_ready, user));
     LV_CUDA(ctx, cudaStreamWaitEvent(b->stream, b->user_ready, 0));
     LV_CUDA(ctx, cudaEventRecord(b->t_sel0, b->stream));
-    if (b->cfg.use_graph)
+    if (graphed)
     {
         const auto key = std::make_tuple(
             n_run, mask, b->cfg.tile_w, b->cfg.tile_h,
@@ -676,9 +812,11 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     b->pending = true;
     /* selection: roots + levels + finish; resolve, prune, leaf, step; per
      * non-empty group one persistent launch (+ key and order passes) */
+    const uint32_t per = b->cfg.order == LV_ORDER_LONGEST_FIRST ? 3u : 1u;
     b->launches = b->depth_max + 2u + 4u +
-                  uint32_t(__builtin_popcount(mask)) *
-                      (b->cfg.order == LV_ORDER_LONGEST_FIRST ? 3u : 1u);
+                  (b->cfg.queue == LV_QUEUE_VIEW_KERNELS
+                       ? n * per
+                       : uint32_t(__builtin_popcount(mask)) * per);
     return LV_OK;
 }
 
@@ -694,18 +832,8 @@ extern "C" lv_status lv_batch_stats(lv_batch* b, lv_frame_stats* out, uint32_t n
     const uint32_t* h = b->h_out.as<uint32_t>();
     for (uint32_t i = 0; i < m; ++i)
     {
-        const uint32_t* c = h + kOutWords * i;
-        const uint32_t* sel = c + FC_WORDS;
-        lv_frame_stats s{};
-        s.n_visible = sel[LV_SEL_WRITTEN];
-        s.n_visited = sel[LV_SEL_VISITED];
-        s.n_rendered = c[FC_KEPT];
-        s.n_available = c[FC_AVAILABLE];
-        s.n_not_available = c[FC_NOT_AVAILABLE];
-        s.max_level = c[FC_MAX_LEVEL] ? c[FC_MAX_LEVEL] - 1u : 0u;
-        s.samples_per_ray = c[FC_SAMPLES_PER_RAY];
-        s.n_samples = uint64_t(c[FC_SAMPLES_LO]) | (uint64_t(c[FC_SAMPLES_HI]) << 32);
-        s.error_flags = c[FC_ERROR];
+        lv_frame_stats s;
+        batch_decode_stats(h + kOutWords * i, s);
         if (i == 0)
         {
             s.n_uploaded = b->uploaded;
@@ -727,6 +855,11 @@ extern "C" lv_status lv_batch_stats(lv_batch* b, lv_frame_stats* out, uint32_t n
         const unsigned long long* clock = reinterpret_cast<const unsigned long long*>(
             h + kOutWords * b->last_n + kGroups);
         *raycast_ms = clock[1] > clock[0] ? float(double(clock[1] - clock[0]) * 1e-6) : 0.f;
+        if (b->vk_timed && cudaEventElapsedTime(raycast_ms, b->t_vk0, b->t_vk1) != cudaSuccess)
+        {
+            cudaGetLastError();
+            *raycast_ms = 0.f;
+        }
     }
     return LV_OK;
 }
@@ -772,6 +905,20 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
                 c.order = ord;
                 cands.push_back(c);
             }
+    static const uint32_t view_shapes[][2] = {{8, 8}, {8, 16}};
+    for (const auto& sh : view_shapes)
+        for (uint32_t ord = 0; ord < 2; ++ord)
+        {
+            lv_batch_config c = start;
+            c.queue = LV_QUEUE_VIEW_KERNELS;
+            c.tile_w = sh[0];
+            c.tile_h = sh[1];
+            c.ctas_per_sm = 0;
+            c.tf_shared = 0;
+            c.samples_per_check = 8;
+            c.order = ord;
+            cands.push_back(c);
+        }
     for (const auto& sh : warp_shapes)
         for (uint32_t k : checks)
         {

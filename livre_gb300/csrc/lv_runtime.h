@@ -254,6 +254,24 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
                         uint32_t* leaf, uint32_t* counters, RayView& V);
 /* Index of the ray-cast kernel instantiation for a view. */
 int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge);
+/* Per-view completion of a batch of per-view kernels (LV_QUEUE_VIEW_KERNELS):
+ * called on a CUDA host-function thread once view `view`'s image is written,
+ * with its counter words (FrameCounter words, then the selection result).
+ * The callback must not call CUDA. */
+typedef void (*BatchViewDone)(void* user, uint32_t view, const uint32_t* words);
+void batch_set_view_hook(lv_batch* b, BatchViewDone fn, void* user);
+/* Ray casts of the next launches on the lowest-priority streams (a batch
+ * that overlaps another takes only the SM slots the other leaves free). */
+void batch_set_low_priority(lv_batch* b, bool low);
+/* Frame statistics from a view's counter words. */
+void batch_decode_stats(const uint32_t* words, lv_frame_stats& s);
+
+/* One view's ray cast with launch shape L, its longest-first tile order (if
+ * any) in `order_scratch` (tile_order_bytes; nullptr: the context's lv_render
+ * scratch). The view's samples per ray must already be in its counters. */
+lv_status launch_view_raycast(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                              uint8_t* order_scratch, cudaStream_t s);
+size_t tile_order_bytes(const RayView& V, const lv_render_launch& L);
 /* Longest-first order of a batched group's work items (memset + 2 kernels);
  * hist: 128 words, keys and order: max_items entries (an upper bound of the
  * group's items at every replay of a captured launch). */

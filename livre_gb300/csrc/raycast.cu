@@ -1287,10 +1287,19 @@ lv_status refill_views_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQu
     return LV_OK;
 }
 
-/* Longest-first order of the tiles of V (two small launches); nullptr for
- * raster order. */
+/* Scratch bytes of the longest-first order of V's tiles. */
+size_t order_bytes_of(const RayView& V, const lv_render_launch& L)
+{
+    const size_t total =
+        size_t((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
+    return 2 * kTileBuckets * sizeof(uint32_t) + ((total + 15) & ~size_t(15)) +
+           sizeof(uint32_t) * total;
+}
+
+/* Longest-first order of the tiles of V (a memset and two small launches)
+ * in `scratch` (tile_order_bytes); nullptr for raster order. */
 const uint32_t* tile_order(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
-                           cudaStream_t s, lv_status& st)
+                           uint8_t* scratch, cudaStream_t s, lv_status& st)
 {
     st = LV_OK;
     if (L.order != LV_ORDER_LONGEST_FIRST)
@@ -1299,17 +1308,14 @@ const uint32_t* tile_order(lv_ctx* ctx, const RayView& V, const lv_render_launch
     const uint32_t total = tiles_x * ((V.H + L.tile_h - 1) / L.tile_h);
     const size_t hist_bytes = 2 * kTileBuckets * sizeof(uint32_t);
     const size_t key_bytes = (size_t(total) + 15) & ~size_t(15);
-    DeviceBuffer& buf = ctx->renderer->tiles;
-    cudaError_t e = buf.reserve(hist_bytes + key_bytes + sizeof(uint32_t) * total);
-    if (e == cudaSuccess)
-        e = cudaMemsetAsync(buf.ptr, 0, hist_bytes, s);
+    cudaError_t e = cudaMemsetAsync(scratch, 0, hist_bytes, s);
     if (e != cudaSuccess)
     {
         st = cuda_fail(ctx, e, "tile order");
         return nullptr;
     }
-    uint32_t* hist = buf.as<uint32_t>();
-    uint8_t* keys = buf.as<uint8_t>() + hist_bytes;
+    uint32_t* hist = reinterpret_cast<uint32_t*>(scratch);
+    uint8_t* keys = scratch + hist_bytes;
     uint32_t* order = reinterpret_cast<uint32_t*>(keys + key_bytes);
     float diag = 0.f;
     for (int a = 0; a < 3; ++a)
@@ -1328,12 +1334,29 @@ const uint32_t* tile_order(lv_ctx* ctx, const RayView& V, const lv_render_launch
     return order;
 }
 
+/* lv_render's scratch for the tile order of V. */
+uint8_t* render_order_scratch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                              lv_status& st)
+{
+    st = LV_OK;
+    if (L.order != LV_ORDER_LONGEST_FIRST)
+        return nullptr;
+    DeviceBuffer& buf = ctx->renderer->tiles;
+    const cudaError_t e = buf.reserve(order_bytes_of(V, L));
+    if (e != cudaSuccess)
+        st = cuda_fail(ctx, e, "tile order");
+    return buf.as<uint8_t>();
+}
+
 template <int DT, int F, int EDGE>
 lv_status refill_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                           cudaStream_t s)
 {
     lv_status st = LV_OK;
-    const uint32_t* order = tile_order(ctx, V, L, s, st);
+    uint8_t* scratch = render_order_scratch(ctx, V, L, st);
+    if (st != LV_OK)
+        return st;
+    const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
     if (st != LV_OK)
         return st;
     auto k = raycast_refill_kernel<DT, F, EDGE>;
@@ -1348,12 +1371,16 @@ lv_status refill_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch&
 
 template <int DT, int F, int EDGE, int LA>
 lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
-                            cudaStream_t s)
+                            cudaStream_t s, uint8_t* scratch)
 {
     if (L.kind == LV_LAUNCH_TILE_QUEUE)
     {
         lv_status st = LV_OK;
-        const uint32_t* order = tile_order(ctx, V, L, s, st);
+        if (!scratch)
+            scratch = render_order_scratch(ctx, V, L, st);
+        if (st != LV_OK)
+            return st;
+        const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
         if (st != LV_OK)
             return st;
         auto k = raycast_queue_kernel<DT, F, EDGE, LA>;
@@ -1375,13 +1402,13 @@ lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launc
 
 template <int DT, int F, int EDGE>
 lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
-                         cudaStream_t s)
+                         cudaStream_t s, uint8_t* scratch)
 {
     if (L.kind == LV_LAUNCH_WARP_REFILL)
         return refill_dispatch<DT, F, EDGE>(ctx, V, L, s);
     if (L.lookahead)
-        return plain_dispatch_la<DT, F, EDGE, 1>(ctx, V, L, s);
-    return plain_dispatch_la<DT, F, EDGE, 0>(ctx, V, L, s);
+        return plain_dispatch_la<DT, F, EDGE, 1>(ctx, V, L, s, scratch);
+    return plain_dispatch_la<DT, F, EDGE, 0>(ctx, V, L, s, scratch);
 }
 
 /* combination index: dtype (u8 0 / u16 1), filter, edge */
@@ -1419,6 +1446,11 @@ lv_status refill_views_by_index(int idx, lv_ctx* ctx, const RayView* d, const Ti
 }
 } // namespace
 
+size_t tile_order_bytes(const RayView& V, const lv_render_launch& L)
+{
+    return order_bytes_of(V, L);
+}
+
 int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge)
 {
     return (dtype == LV_DT_UINT16 ? 4 : 0) + (filter == LV_FILTER_TRILINEAR ? 2 : 0) +
@@ -1432,17 +1464,22 @@ lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
     step_kernel<<<1, 1, 0, s>>>(V.counters, V.samples_fixed, V.step_policy,
                                 V.max_voxel_dim, V.depth);
     LV_CUDA(ctx, cudaGetLastError());
-    const lv_render_launch L = ctx->launch;
+    return launch_view_raycast(ctx, V, ctx->launch, nullptr, s);
+}
+
+lv_status launch_view_raycast(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                              uint8_t* order_scratch, cudaStream_t s)
+{
     switch (kernel_variant(V.dtype, V.filter, V.edge))
     {
-    case 0: return plain_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, L, s);
-    case 1: return plain_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, L, s);
-    case 2: return plain_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, L, s);
-    case 3: return plain_dispatch<LV_DT_UINT8, 1, 1>(ctx, V, L, s);
-    case 4: return plain_dispatch<LV_DT_UINT16, 0, 0>(ctx, V, L, s);
-    case 5: return plain_dispatch<LV_DT_UINT16, 0, 1>(ctx, V, L, s);
-    case 6: return plain_dispatch<LV_DT_UINT16, 1, 0>(ctx, V, L, s);
-    default: return plain_dispatch<LV_DT_UINT16, 1, 1>(ctx, V, L, s);
+    case 0: return plain_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, L, s, order_scratch);
+    case 1: return plain_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, L, s, order_scratch);
+    case 2: return plain_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, L, s, order_scratch);
+    case 3: return plain_dispatch<LV_DT_UINT8, 1, 1>(ctx, V, L, s, order_scratch);
+    case 4: return plain_dispatch<LV_DT_UINT16, 0, 0>(ctx, V, L, s, order_scratch);
+    case 5: return plain_dispatch<LV_DT_UINT16, 0, 1>(ctx, V, L, s, order_scratch);
+    case 6: return plain_dispatch<LV_DT_UINT16, 1, 0>(ctx, V, L, s, order_scratch);
+    default: return plain_dispatch<LV_DT_UINT16, 1, 1>(ctx, V, L, s, order_scratch);
     }
 }
 

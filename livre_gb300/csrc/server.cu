@@ -70,9 +70,20 @@ void CUDART_CB stamp_done(void* p)
 struct Inflight
 {
     lv_batch* batch = nullptr;
-    std::vector<Req*> reqs;
+    /* tickets, not Req pointers: a request completed early by its view's
+     * hook may be collected (and freed) by lv_server_wait before the batch
+     * ends */
+    std::vector<uint64_t> tickets;
+    std::vector<std::pair<lv_volume*, std::vector<uint64_t>>> pins;
+    lv_status status = LV_OK;
     cudaEvent_t ev = nullptr;
     std::shared_ptr<DoneClock> clock;
+};
+
+struct lv_server_hook
+{
+    lv_server* S;
+    int batch;
 };
 } // namespace
 
@@ -91,7 +102,11 @@ struct lv_server
     int cur = 0;
     std::deque<Inflight> inflight;
     std::vector<cudaEvent_t> free_events;
-    cudaStream_t sel_stream = nullptr, launch_stream = nullptr;
+    cudaStream_t sel_stream = nullptr;
+    /* one launch stream per batch object: consecutive batches overlap */
+    cudaStream_t launch_stream[2] = {nullptr, nullptr};
+    lv_server_hook hooks[2];
+    std::vector<uint64_t> current[2]; /* tickets of the views in flight per batch object */
     cudaEvent_t uploads_done = nullptr;
     /* dry-run selection buffers */
     SelectScratch sel;
@@ -110,30 +125,36 @@ void complete(lv_server* S, Inflight& f)
     double t = now_ms();
     if (f.clock && f.clock->t.load() > 0.0)
         t = f.clock->t.load();
-    std::vector<lv_frame_stats> st(f.reqs.size());
+    const uint32_t n = uint32_t(f.tickets.size());
+    std::vector<lv_frame_stats> st(n);
     float batch_ms = 0.f, ray_ms = 0.f;
-    if (f.batch && !f.reqs.empty())
-        lv_batch_stats(f.batch, st.data(), uint32_t(st.size()), &batch_ms, &ray_ms);
+    if (f.batch && n)
+        lv_batch_stats(f.batch, st.data(), n, &batch_ms, &ray_ms);
     {
         std::lock_guard<std::mutex> lk(S->ctx->mutex);
-        for (Req* r : f.reqs)
+        for (auto& vp : f.pins)
         {
-            lv_volume* v = r->r.volume;
-            for (uint64_t idx : r->pinned)
+            lv_volume* v = vp.first;
+            for (uint64_t idx : vp.second)
                 if (v->pins[idx] && --v->pins[idx] == 0 && v->host_table[idx] >= 0)
                     --S->ctx->pool->pinned_count[v->slot_units];
-            r->pinned.clear();
         }
+        f.pins.clear();
     }
     std::lock_guard<std::mutex> lk(S->m);
     S->prof.device_ms += batch_ms;
     S->prof.raycast_ms += ray_ms;
-    S->prof.requests += f.reqs.size();
-    for (size_t i = 0; i < f.reqs.size(); ++i)
+    S->prof.requests += n;
+    for (uint32_t i = 0; i < n; ++i)
     {
-        Req* r = f.reqs[i];
+        auto it = S->reqs.find(f.tickets[i]);
+        if (it == S->reqs.end() || it->second->done)
+            continue; /* completed by its view's hook */
+        Req* r = it->second;
         r->t_done = t;
         r->stats = st[i];
+        if (r->status == LV_OK)
+            r->status = f.status;
         if (r->status == LV_OK && st[i].error_flags)
             r->status = LV_EDEVICE;
         r->done = true;
@@ -141,6 +162,30 @@ void complete(lv_server* S, Inflight& f)
     }
     if (f.ev)
         S->free_events.push_back(f.ev);
+    S->cv_done.notify_all();
+}
+
+/* A view of a per-view-kernel batch is complete (CUDA host-function
+ * thread): its request is done, with the view's own statistics. */
+void view_done(void* user, uint32_t view, const uint32_t* words)
+{
+    const lv_server_hook* h = static_cast<const lv_server_hook*>(user);
+    lv_server* S = h->S;
+    const double t = now_ms();
+    std::lock_guard<std::mutex> lk(S->m);
+    const std::vector<uint64_t>& cur = S->current[h->batch];
+    if (view >= cur.size())
+        return;
+    auto it = S->reqs.find(cur[view]);
+    if (it == S->reqs.end() || it->second->done)
+        return;
+    Req* r = it->second;
+    batch_decode_stats(words, r->stats);
+    if (r->stats.error_flags)
+        r->status = LV_EDEVICE;
+    r->t_done = t;
+    r->done = true;
+    ++S->n_done;
     S->cv_done.notify_all();
 }
 
@@ -430,14 +475,34 @@ void loop_batched(lv_server* S)
             bv[i].d_rgba = admitted[i]->r.d_rgba;
             admitted[i]->batch_size = uint32_t(admitted.size());
         }
-        lv_batch* b = S->batches[S->cur];
+        const int bi = S->cur;
+        lv_batch* b = S->batches[bi];
         S->cur ^= 1;
-        cudaStreamWaitEvent(S->launch_stream, S->uploads_done, 0);
-        const double t_launch = now_ms();
-        const lv_status st = lv_batch_render(b, bv.data(), uint32_t(bv.size()), S->launch_stream);
-        add_time(S, &lv_server_profile::launch_ms, now_ms() - t_launch);
+        cudaStream_t ls = S->launch_stream[bi];
         Inflight f;
         f.batch = b;
+        for (Req* r : admitted)
+        {
+            f.tickets.push_back(r->ticket);
+            f.pins.emplace_back(r->r.volume, std::move(r->pinned));
+            r->pinned.clear();
+        }
+        {
+            /* the batch object's previous launch (and its hooks) ended
+             * before this one is enqueued: lv_batch_render waits for it */
+            std::lock_guard<std::mutex> lk(S->m);
+            S->current[bi] = f.tickets;
+        }
+        bool overlapping;
+        {
+            std::lock_guard<std::mutex> lk(S->m);
+            overlapping = !S->inflight.empty();
+        }
+        batch_set_low_priority(b, overlapping);
+        cudaStreamWaitEvent(ls, S->uploads_done, 0);
+        const double t_launch = now_ms();
+        const lv_status st = lv_batch_render(b, bv.data(), uint32_t(bv.size()), ls);
+        add_time(S, &lv_server_profile::launch_ms, now_ms() - t_launch);
         {
             std::lock_guard<std::mutex> lk(S->m);
             if (!S->free_events.empty())
@@ -449,17 +514,15 @@ void loop_batched(lv_server* S)
         if (!f.ev)
             cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming);
         f.clock = std::make_shared<DoneClock>();
-        cudaLaunchHostFunc(S->launch_stream, stamp_done, f.clock.get());
-        cudaEventRecord(f.ev, S->launch_stream);
+        cudaLaunchHostFunc(ls, stamp_done, f.clock.get());
+        cudaEventRecord(f.ev, ls);
         if (st != LV_OK)
         {
-            for (Req* r : admitted)
-                r->status = st;
+            f.status = st;
             f.batch = nullptr;
         }
-        f.reqs = admitted;
         std::lock_guard<std::mutex> lk(S->m);
-        S->inflight.push_back(f);
+        S->inflight.push_back(std::move(f));
         ++S->n_batches;
     }
 }
@@ -483,7 +546,8 @@ void loop_plain(lv_server* S)
         lv_render_desc d = r->r.desc;
         d.synchronous = 1;
         const double t0 = now_ms();
-        lv_status st = lv_render(S->ctx, r->r.volume, r->r.tf, &d, r->r.d_rgba, S->launch_stream);
+        lv_status st = lv_render(S->ctx, r->r.volume, r->r.tf, &d, r->r.d_rgba,
+                                 S->launch_stream[0]);
         if (st == LV_OK)
             st = lv_last_stats(S->ctx, &r->stats); /* synchronises */
         std::lock_guard<std::mutex> lk(S->m);
@@ -522,7 +586,8 @@ extern "C" lv_status lv_server_create(lv_ctx* ctx, const lv_server_config* cfg, 
     cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     if (cudaStreamCreateWithPriority(&S->sel_stream, cudaStreamNonBlocking, hi_prio) !=
             cudaSuccess ||
-        cudaStreamCreateWithFlags(&S->launch_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&S->launch_stream[0], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&S->launch_stream[1], cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&S->uploads_done, cudaEventDisableTiming) != cudaSuccess)
     {
         delete S;
@@ -546,6 +611,8 @@ extern "C" lv_status lv_server_create(lv_ctx* ctx, const lv_server_config* cfg, 
             bc.ctas_per_sm = cfg->ctas_per_sm ? cfg->ctas_per_sm : bc.ctas_per_sm;
         }
         lv_batch_set_config(S->batches[i], &bc);
+        S->hooks[i] = lv_server_hook{S, i};
+        batch_set_view_hook(S->batches[i], view_done, &S->hooks[i]);
     }
     S->th = std::thread(cfg->mode == LV_SERVE_PLAIN ? loop_plain : loop_batched, S);
     *out = S;
@@ -650,7 +717,8 @@ extern "C" void lv_server_destroy(lv_server* S)
     for (auto& f : S->inflight)
     {
         cudaEventSynchronize(f.ev);
-        cudaStreamSynchronize(S->launch_stream); /* host functions done */
+        for (cudaStream_t ls : S->launch_stream)
+            cudaStreamSynchronize(ls); /* host functions done */
         complete(S, f);
     }
     for (int i = 0; i < 2; ++i)
@@ -661,8 +729,9 @@ extern "C" void lv_server_destroy(lv_server* S)
         delete kv.second;
     if (S->sel_stream)
         cudaStreamDestroy(S->sel_stream);
-    if (S->launch_stream)
-        cudaStreamDestroy(S->launch_stream);
+    for (cudaStream_t ls : S->launch_stream)
+        if (ls)
+            cudaStreamDestroy(ls);
     if (S->uploads_done)
         cudaEventDestroy(S->uploads_done);
     delete S;

@@ -75,6 +75,8 @@ def test_render_launch_validation(gpu_ctx):
     dict(queue=0, tile_w=16, tile_h=8, order=0),
     dict(queue=0, tile_w=8, tile_h=8, tf_shared=1, ctas_per_sm=3),
     dict(queue=0, tile_w=8, tile_h=16, tf_shared=1, order=0),
+    dict(queue=2, tile_w=8, tile_h=16),
+    dict(queue=2, tile_w=16, tile_h=16, order=0),
 ])
 def test_batch_queue_kinds_match_single_views(gpu_ctx, cfg):
     """Both work-queue kinds, with and without graphs, give each view the
@@ -117,6 +119,7 @@ def test_padded_batches_share_graphs(gpu_ctx):
                                               device="cuda")))
     singles = [gpu_ctx.render(v, t, d).clone() for v, t, d, _ in views]
     batch = lv.Batch(gpu_ctx)
+    batch.set_config(queue=lv.QUEUE_CTA_TILES, tile_w=8, tile_h=16)  # the graphed kind
     for n in (5, 6, 7, 8, 5):
         batch.render(views[:n])
         for (_, _, _, o), ref in zip(views[:n], singles):
