@@ -357,16 +357,22 @@ lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
  * lookahead (grid and tile queue): 1 loads the voxels of a ray's next sample
  * before compositing the current one (shorter latency per ray, more
  * registers per thread); 0 does not.
- * Default: {LV_LAUNCH_TILE_QUEUE, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 0}, the
- * fastest on a 2048^3 volume at 1920x1080 (0.43 ms per frame against 0.52 ms
- * for the 8 x 16 grid).
+ * Default: {LV_LAUNCH_TILE_GRID, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 0}, the
+ * fastest on a 2048^3 volume at 1920x1080 (0.46 ms per frame against 0.47 ms
+ * for the 8 x 16 grid in raster order and 0.43-0.53 ms for the persistent
+ * queue, whose time varies from run to run), and the friendliest to other
+ * work on the device.
  * No reference counterpart (the reference rasterises one brick at a time,
  * RayCastRenderer.cpp:503-571). */
 enum
 {
     LV_LAUNCH_GRID = 0,
     LV_LAUNCH_TILE_QUEUE = 1,
-    LV_LAUNCH_WARP_REFILL = 2
+    LV_LAUNCH_WARP_REFILL = 2,
+    LV_LAUNCH_TILE_GRID = 3 /* one tile_w x tile_h-thread CTA per tile, block i
+                               taking the i-th tile of the order: no resident
+                               grid, so CTAs retire tile by tile and other
+                               kernels (the next frame's selection) interleave */
 };
 enum
 {
@@ -412,10 +418,11 @@ enum
                                 one ray each */
     LV_QUEUE_WARP_REFILL = 1, /* a warp per work item: the tile's pixels are
                                  handed to lanes as their rays finish */
-    LV_QUEUE_VIEW_KERNELS = 2 /* one tile-queue ray cast per view (lv_render's
-                                 kernel, view constants as kernel parameters)
-                                 on parallel streams, so a view's last tiles
-                                 overlap the next view; no CUDA graph */
+    LV_QUEUE_VIEW_KERNELS = 2 /* one ray cast per view (lv_render's one-CTA-per-
+                                 tile kernel, view constants as kernel
+                                 parameters) on parallel streams, so a view's
+                                 last tiles overlap the next view; no CUDA
+                                 graph. The default. */
 };
 
 /* Launch shape of the persistent ray-cast kernel. */

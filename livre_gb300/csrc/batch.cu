@@ -56,7 +56,7 @@ struct lv_batch
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr, user_ready = nullptr;
     cudaEvent_t t_sel0 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
-    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_VIEW_KERNELS, 8, LV_ORDER_RASTER};
+    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_VIEW_KERNELS, 8, LV_ORDER_LONGEST_FIRST};
     /* per-group longest-first order: hist (128 words) | keys | order, each
      * group at a fixed offset sized for order_cap items (grow-only) */
     lv::DeviceBuffer order_buf;
@@ -455,7 +455,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     {
         /* lv_render's ray cast per view, views spread over the aux streams */
         const RayView* h_rays = reinterpret_cast<const RayView*>(b->h_params.as<uint8_t>() + PL.ray);
-        const lv_render_launch L{LV_LAUNCH_TILE_QUEUE, b->cfg.tile_w, b->cfg.tile_h, 0,
+        const lv_render_launch L{LV_LAUNCH_TILE_GRID, b->cfg.tile_w, b->cfg.tile_h, 0,
                                  b->cfg.order, 0};
         std::vector<uint64_t> offs(n + 1, 0);
         for (uint32_t i = 0; i < n; ++i)

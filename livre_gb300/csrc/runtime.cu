@@ -947,7 +947,8 @@ extern "C" lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* c
     const bool ok = cfg->kind == LV_LAUNCH_WARP_REFILL
                         ? pixels >= 32 && pixels <= 1024 && cfg->samples_per_check >= 1 &&
                               cfg->samples_per_check <= 64
-                        : (cfg->kind == LV_LAUNCH_GRID || cfg->kind == LV_LAUNCH_TILE_QUEUE) &&
+                        : (cfg->kind == LV_LAUNCH_GRID || cfg->kind == LV_LAUNCH_TILE_QUEUE ||
+                           cfg->kind == LV_LAUNCH_TILE_GRID) &&
                               pixels >= 32 && pixels <= 256 && pixels % 32 == 0;
     const bool order_ok = (cfg->order == LV_ORDER_RASTER ||
                            (cfg->order == LV_ORDER_LONGEST_FIRST && cfg->kind != LV_LAUNCH_GRID)) &&

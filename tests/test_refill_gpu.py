@@ -10,7 +10,8 @@ pytestmark = pytest.mark.gpu
 LAUNCHES = [(0, 8, 4, 0, 0, 0), (0, 16, 16, 0, 0, 1), (0, 32, 2, 0, 0, 0),
             (1, 8, 16, 0, 0, 1), (1, 16, 16, 0, 1, 0), (1, 8, 8, 0, 1, 1), (1, 32, 1, 0, 0, 0),
             (2, 8, 8, 8, 0, 0), (2, 8, 4, 1, 1, 0), (2, 16, 8, 2, 0, 0), (2, 16, 16, 32, 1, 0),
-            (2, 32, 32, 64, 0, 0), (2, 32, 1, 5, 0, 0)]
+            (2, 32, 32, 64, 0, 0), (2, 32, 1, 5, 0, 0), (3, 8, 16, 0, 1, 0),
+            (3, 16, 16, 0, 0, 1), (3, 32, 1, 0, 1, 0)]
 
 
 def scenes(ctx, lv):
@@ -59,11 +60,11 @@ def test_refill_launches_bit_identical(gpu_ctx):
 def test_render_launch_validation(gpu_ctx):
     import livre_gb300 as lv
     for bad in [(2, 4, 4, 8), (2, 64, 32, 8), (2, 8, 8, 0), (2, 8, 8, 65), (0, 8, 3, 0),
-                (0, 32, 16, 0), (1, 4, 4, 0), (3, 8, 8, 8), (0, 8, 16, 0, 1),
+                (0, 32, 16, 0), (1, 4, 4, 0), (4, 8, 8, 8), (0, 8, 16, 0, 1),
                 (1, 8, 16, 0, 2), (1, 8, 16, 0, 0, 2), (2, 8, 8, 8, 0, 1)]:
         with pytest.raises(lv.LivreError):
             gpu_ctx.set_render_launch(*bad)
-    assert gpu_ctx.render_launch() == {"kind": 1, "tile_w": 8, "tile_h": 16,
+    assert gpu_ctx.render_launch() == {"kind": 3, "tile_w": 8, "tile_h": 16,
                                        "samples_per_check": 0, "order": 1, "lookahead": 0}
 
 
