@@ -157,6 +157,19 @@ def cpu_frame_estimate(cfg, k=0, rows=12):
     return t_lod + t_rows * H / rows, t_lod, t_rows
 
 
+def workload_config(cfg, world):
+    """The `config` object of both arms' JSON lines."""
+    return {"workload": cfg["workload"], "volume": "%d^3 u8" % cfg["voxels"],
+            "brick": "%d^3 + overlap %d" % (cfg["block"], cfg["overlap"]),
+            "viewport": "%dx%d" % (cfg["width"], cfg["height"]), "frames": cfg["frames"],
+            "lod_px": cfg["sse"], "step": "0.5 voxel of finest rendered level",
+            "filter": "trilinear", "early_exit": cfg["early"],
+            "tf": "%d-entry RGBA f32" % cfg["tf_entries"],
+            "mode": "plain per-view launch (synchronous residency)",
+            "l2": "flushed between frames (256 MiB write)",
+            "parallelism": "replicas" if world > 1 else "single"}
+
+
 def reference_arm(args, cfg):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -175,8 +188,9 @@ def reference_arm(args, cfg):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": cfg["workload"], "note": "CPU restatement of the reference "
-                       "path (the reference renders through OpenGL, unavailable on this box)"},
+            "config": workload_config(cfg, 1),
+            "note": "CPU restatement of the reference path (the reference renders through "
+                    "OpenGL, unavailable on this box)",
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
                              "sample": "per step: full-frame FP32 LOD selection (1 thread) + "
                                        "FP64 ray cast of %d evenly spaced rows (all threads), "
@@ -527,14 +541,7 @@ def gb300_arm(args, cfg):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": cfg["workload"], "volume": "%d^3 u8" % cfg["voxels"],
-                   "brick": "%d^3 + overlap %d" % (cfg["block"], cfg["overlap"]),
-                   "viewport": "%dx%d" % (W, H), "frames": cfg["frames"], "lod_px": cfg["sse"],
-                   "step": "0.5 voxel of finest rendered level", "filter": "trilinear",
-                   "early_exit": cfg["early"], "tf": "%d-entry RGBA f32" % cfg["tf_entries"],
-                   "mode": "plain per-view launch (synchronous residency)",
-                   "l2": "flushed between frames (256 MiB write)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": workload_config(cfg, world),
         "p50_ms": float(np.percentile(frame_ms, 50)), "p99_ms": float(np.percentile(frame_ms, 99)),
         "samples_per_s": float(n_samples.sum() / (total_ms / 1000.0)),
         "raycast_ms_mean": float(ray_ms.mean()),
