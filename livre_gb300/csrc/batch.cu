@@ -178,7 +178,9 @@ uint64_t order_region_bytes(uint32_t cap)
  * reallocation drops the captured graphs (they hold the old addresses). */
 lv_status ensure_order(lv_batch* b, uint32_t items)
 {
-    if (b->cfg.order != LV_ORDER_LONGEST_FIRST || items <= b->order_cap)
+    /* per-view kernels order each view's tiles in their own scratch */
+    if (b->cfg.order != LV_ORDER_LONGEST_FIRST || b->cfg.queue == LV_QUEUE_VIEW_KERNELS ||
+        items <= b->order_cap)
         return LV_OK;
     lv_ctx* ctx = b->ctx;
     LV_CUDA(ctx, cudaStreamSynchronize(b->stream));
