@@ -79,6 +79,13 @@ __device__ void resolve_body(const ResolveView& R, uint32_t first, uint32_t stri
             R.view_stamp[idx] = R.view_frame;
             atomicAdd(&R.counters[FC_AVAILABLE], 1u);
             emit_render(R, id, uint32_t(slot));
+            if (R.synchronous)
+            {
+                /* no ancestor fallback: the rendering set is part of the
+                 * visible cut, nothing to prune */
+                atomicAdd(&R.counters[FC_KEPT], 1u);
+                atomicMax(&R.counters[FC_MAX_LEVEL], L + 1u);
+            }
             continue;
         }
         atomicAdd(&R.counters[FC_NOT_AVAILABLE], 1u);
@@ -223,10 +230,33 @@ __device__ void step_body(uint32_t* counters, uint32_t fixed, uint32_t policy,
     counters[FC_SAMPLES_PER_RAY] = n;
 }
 
-__global__ void step_kernel(uint32_t* counters, uint32_t fixed, uint32_t policy,
-                            uint32_t max_voxel_dim, uint32_t depth)
+/* nSamplesPerRay of a view from its finest rendered level (the rule of
+ * step_body); every ray-cast CTA of lv_render evaluates it, the first one
+ * also stores it for the frame statistics. */
+__device__ __forceinline__ uint32_t view_samples(const RayView& V)
 {
-    step_body(counters, fixed, policy, max_voxel_dim, depth);
+    uint32_t n = V.samples_fixed;
+    if (n == 0)
+    {
+        const uint32_t ml = V.counters[FC_MAX_LEVEL];
+        const uint32_t L = ml ? ml - 1u : 0u;
+        const uint32_t shift = V.depth - L - 1u;
+        if (V.step_policy == LV_STEP_HALF_VOXEL)
+            n = (2u * V.max_voxel_dim) >> shift;
+        else
+            n = uint32_t(fmaxf(float(V.max_voxel_dim) / float(1u << shift), 512.0f));
+        if (n == 0)
+            n = 1;
+    }
+    return n;
+}
+
+__device__ __forceinline__ uint32_t frame_samples(const RayView& V)
+{
+    const uint32_t n = view_samples(V);
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        V.counters[FC_SAMPLES_PER_RAY] = n;
+    return n;
 }
 
 __global__ void step_views_kernel(const RayView* __restrict__ views, uint32_t n)
@@ -715,7 +745,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const RayView V)
 {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t py = blockIdx.y * blockDim.y + threadIdx.y;
-    const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
+    const uint32_t n = frame_samples(V);
     const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
     const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
     uint32_t nsamp = 0;
@@ -897,7 +927,7 @@ __global__ void __launch_bounds__(256)
                          const uint32_t* __restrict__ order)
 {
     __shared__ uint32_t s_item;
-    const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
+    const uint32_t n = frame_samples(V);
     const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
     const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
     const uint32_t tiles_x = (V.W + tile_w - 1) / tile_w;
@@ -937,7 +967,7 @@ __global__ void __launch_bounds__(256)
     raycast_tiles_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h,
                          const uint32_t* __restrict__ order)
 {
-    const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
+    const uint32_t n = frame_samples(V);
     const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
     const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
     const uint32_t tiles_x = (V.W + tile_w - 1) / tile_w;
@@ -1098,7 +1128,7 @@ struct ViewConsts
 __device__ __forceinline__ ViewConsts view_consts(const RayView& V, uint32_t tile_w)
 {
     ViewConsts k;
-    const uint32_t n = V.counters[FC_SAMPLES_PER_RAY];
+    const uint32_t n = view_samples(V);
     k.step = __fdiv_rn(1.0f, __uint2float_rn(n));
     k.ac = __fdiv_rn(32.0f, __uint2float_rn(n));
     k.tiles_x = (V.W + tile_w - 1) / tile_w;
@@ -1212,6 +1242,7 @@ __global__ void __launch_bounds__(kRefillThreads, kRefillMinCtas)
     TileQueue Q{};
     Q.tile_w = tile_w;
     Q.tile_h = tile_h;
+    frame_samples(V);
     const uint32_t tiles = ((V.W + tile_w - 1) / tile_w) * ((V.H + tile_h - 1) / tile_h);
     refill_body<DT, FILTER, EDGE, false>(V, nullptr, nullptr, Q, V.counters + FC_QUEUE, 1u,
                                          tiles, checks, order);
@@ -1262,7 +1293,8 @@ lv_status launch_leaf_fill(lv_ctx* ctx, const ResolveView& R, cudaStream_t s)
 {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    prune_kernel<<<sms, 256, 0, s>>>(R);
+    if (!R.synchronous) /* ancestors may shadow entries: drop them */
+        prune_kernel<<<sms, 256, 0, s>>>(R);
     LV_CUDA(ctx, cudaGetLastError());
     leaf_fill_kernel<<<2 * sms, 256, 0, s>>>(R);
     LV_CUDA(ctx, cudaGetLastError());
@@ -1518,9 +1550,7 @@ lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
 {
     if (V.dtype != LV_DT_UINT8 && V.dtype != LV_DT_UINT16)
         return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
-    step_kernel<<<1, 1, 0, s>>>(V.counters, V.samples_fixed, V.step_policy,
-                                V.max_voxel_dim, V.depth);
-    LV_CUDA(ctx, cudaGetLastError());
+    /* the ray-cast kernels derive the samples per ray themselves */
     return launch_view_raycast(ctx, V, ctx->launch, nullptr, s);
 }
 

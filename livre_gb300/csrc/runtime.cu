@@ -1049,12 +1049,13 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     LV.out_ids = R.visible.as<uint64_t>();
     LV.capacity = uint32_t(std::min<uint64_t>(R.visible_capacity, 0xFFFFFFFFu));
     LV.result = R.sel_result.as<uint32_t>();
-    /* kernels: roots + one per level + finish, resolve, prune, leaf fill,
-     * step, ray cast (+ tile keys and order when longest first); the last
-     * five to seven again on a synchronous miss */
+    /* kernels: roots + one per level + finish, resolve, prune (asynchronous
+     * mode only), leaf fill, ray cast (+ tile keys and order when longest
+     * first); the last three to six again on a synchronous miss */
     const lv_render_launch& RL = ctx->launch;
     const uint32_t tail_launches =
-        5u + (RL.kind != LV_LAUNCH_GRID && RL.order == LV_ORDER_LONGEST_FIRST ? 2u : 0u);
+        3u + (desc->synchronous ? 0u : 1u) +
+        (RL.kind != LV_LAUNCH_GRID && RL.order == LV_ORDER_LONGEST_FIRST ? 2u : 0u);
     R.launches = info.depth + 2u + tail_launches;
     LV_CUDA(ctx, cudaEventRecord(R.t_sel0, s));
     st = run_selection(ctx, &LV, 1, info.depth, s);
