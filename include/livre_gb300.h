@@ -96,7 +96,9 @@ enum
     LV_SEL_FOUND = 1,     /* visible ids found (after the range slice) */
     LV_SEL_VISITED = 2,   /* octree nodes visited */
     LV_SEL_MAX_LEVEL = 3, /* finest level among the visible ids */
-    LV_SEL_OVERFLOW = 4,  /* nonzero: a traversal frontier overflowed */
+    LV_SEL_OVERFLOW = 4,  /* 1: a traversal frontier overflowed; 2: the
+                             single-launch selection's grid barrier gave up
+                             waiting (the ids are unusable) */
     LV_SELECT_RESULT_WORDS = 8
 };
 
@@ -325,7 +327,8 @@ typedef struct lv_frame_stats
     float raycast_ms;         /* device time of the ray-cast kernel */
     uint32_t error_flags;     /* 0, or the device's index-check code: 1 rendering
                                  set overflow, 2 node outside the octree,
-                                 3 brick outside the pool (the access was skipped) */
+                                 3 brick outside the pool (the access was skipped),
+                                 4 the selection's grid barrier gave up */
     uint32_t n_passes;        /* 1, or the passes of a frame whose visible set
                                  exceeded the brick pool (renderSync,
                                  RenderPipeline.cpp:92-158) */

@@ -202,17 +202,19 @@ __global__ void lod_roots_kernel(const LodView* __restrict__ views,
     }
 }
 
-__global__ void __launch_bounds__(256)
-    lod_level_kernel(const LodView* __restrict__ views,
-                     const uint64_t* __restrict__ in_ids,
-                     const uint32_t* __restrict__ in_view,
-                     const uint32_t* __restrict__ in_count,
-                     uint64_t* __restrict__ out_ids,
-                     uint32_t* __restrict__ out_view,
-                     uint32_t* __restrict__ out_count, uint32_t capacity,
-                     uint32_t* __restrict__ overflow)
+/* One level of the traversal over frontier items [0, n) strided by the
+ * grid: visit, warp-aggregated emission of visible ids per view, 8 child
+ * pushes per descending lane. COHERENT: the frontier was written by other
+ * CTAs of the same launch, so it is read through L2 (not the SM's L1). */
+template <bool COHERENT>
+__device__ __forceinline__ void level_items(const LodView* __restrict__ views,
+                                            const uint64_t* __restrict__ in_ids,
+                                            const uint32_t* __restrict__ in_view, uint32_t n,
+                                            uint64_t* __restrict__ out_ids,
+                                            uint32_t* __restrict__ out_view,
+                                            uint32_t* __restrict__ out_count, uint32_t capacity,
+                                            uint32_t* __restrict__ overflow)
 {
-    const uint32_t n = min(*in_count, capacity);
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt = lanemask_lt();
     for (uint32_t base = blockIdx.x * blockDim.x; base < n;
@@ -225,8 +227,8 @@ __global__ void __launch_bounds__(256)
         int decision = 0;
         if (active)
         {
-            id = in_ids[i];
-            v = in_view[i];
+            id = COHERENT ? __ldcg(in_ids + i) : in_ids[i];
+            v = COHERENT ? __ldcg(in_view + i) : in_view[i];
             decision = visit(views[v], id);
         }
         /* per-view groups of active lanes: visited + emitted counts */
@@ -282,6 +284,20 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+__global__ void __launch_bounds__(256)
+    lod_level_kernel(const LodView* __restrict__ views,
+                     const uint64_t* __restrict__ in_ids,
+                     const uint32_t* __restrict__ in_view,
+                     const uint32_t* __restrict__ in_count,
+                     uint64_t* __restrict__ out_ids,
+                     uint32_t* __restrict__ out_view,
+                     uint32_t* __restrict__ out_count, uint32_t capacity,
+                     uint32_t* __restrict__ overflow)
+{
+    level_items<false>(views, in_ids, in_view, min(*in_count, capacity), out_ids, out_view,
+                       out_count, capacity, overflow);
+}
+
 /* WRITTEN = min(FOUND, capacity); OVERFLOW from the frontier flag. */
 __global__ void lod_finish_kernel(const LodView* __restrict__ views,
                                   uint32_t n_views,
@@ -293,6 +309,93 @@ __global__ void lod_finish_kernel(const LodView* __restrict__ views,
     uint32_t* res = views[v].result;
     res[LV_SEL_WRITTEN] = min(res[LV_SEL_FOUND], views[v].capacity);
     res[LV_SEL_OVERFLOW] = *overflow;
+}
+
+/* ---- single-view selection in one cooperative launch ------------------
+ * Roots, every level and the result words of one view in one launch whose
+ * CTAs are all resident (cooperative launch), separated by a grid barrier
+ * instead of a kernel boundary. The view's constants are a kernel
+ * parameter. bar[0] counts arrivals, bar[1] is the barrier generation,
+ * bar[2] an error flag set when a wait gives up (kSpinLimit polls); the
+ * words are zeroed before the launch, with the level counters. */
+constexpr uint32_t kSpinLimit = 1u << 22; /* ~0.3 s of 64 ns sleeps */
+
+__device__ __forceinline__ void grid_barrier(uint32_t* bar)
+{
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        volatile uint32_t* gen = bar + 1;
+        const uint32_t g = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == gridDim.x - 1u)
+        {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicExch(bar + 1, g + 1u);
+        }
+        else
+        {
+            uint32_t polls = 0;
+            while (*gen == g)
+            {
+                if (++polls > kSpinLimit)
+                {
+                    atomicExch(bar + 2, 1u); /* gave up: results unusable */
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256)
+    lod_fused_kernel(const __grid_constant__ LodView V, uint32_t max_depth,
+                     uint64_t* __restrict__ ids0, uint32_t* __restrict__ view0,
+                     uint64_t* __restrict__ ids1, uint32_t* __restrict__ view1,
+                     uint32_t* __restrict__ counts, uint32_t capacity)
+{
+    uint32_t* overflow = counts + kMaxLevels + 1;
+    uint32_t* bar = counts + kMaxLevels + 2;
+    const LodView* views = &V;
+    const uint32_t rx = V.root_blocks[0], ry = V.root_blocks[1], rz = V.root_blocks[2];
+    const uint32_t n_roots = rx * ry * rz;
+    if (blockIdx.x == 0)
+    {
+        if (threadIdx.x == 0)
+            counts[0] = min(n_roots, capacity);
+        if (threadIdx.x < LV_SELECT_RESULT_WORDS)
+            V.result[threadIdx.x] = 0u;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < min(n_roots, capacity);
+         i += gridDim.x * blockDim.x)
+    {
+        const uint32_t x = i / (ry * rz), y = (i / rz) % ry, z = i % rz;
+        ids0[i] = nid_make(0, x, y, z, V.time_step);
+        view0[i] = 0u;
+    }
+    grid_barrier(bar);
+    for (uint32_t l = 0; l < max_depth; ++l)
+    {
+        const uint32_t n = min(__ldcg(counts + l), capacity);
+        if (n == 0 || __ldcg(bar + 2))
+            break; /* the same value in every CTA: read after the barrier */
+        const bool even = (l & 1u) == 0;
+        level_items<true>(views, even ? ids0 : ids1, even ? view0 : view1, n,
+                          even ? ids1 : ids0, even ? view1 : view0, counts + l + 1, capacity,
+                          overflow);
+        grid_barrier(bar);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        uint32_t* res = V.result;
+        res[LV_SEL_WRITTEN] = min(__ldcg(res + LV_SEL_FOUND), V.capacity);
+        /* 2: a barrier wait gave up (nothing of the selection is usable) */
+        res[LV_SEL_OVERFLOW] = __ldcg(bar + 2) ? 2u : __ldcg(overflow);
+    }
 }
 
 /* DFS preorder key: root index then the child index (x*4 + y*2 + z) of
@@ -477,6 +580,35 @@ uint64_t max_frontier(const lv_volume_info& vol)
     return m;
 }
 
+namespace
+{
+/* Grid of the cooperative single-view selection on the context's device
+ * (0: cooperative launch unavailable). */
+uint32_t fused_grid(lv_ctx* ctx)
+{
+    static std::mutex m;
+    static std::vector<int> grids;
+    std::lock_guard<std::mutex> lock(m);
+    if (grids.size() <= size_t(ctx->device))
+        grids.resize(size_t(ctx->device) + 1, -1);
+    int& g = grids[size_t(ctx->device)];
+    if (g < 0)
+    {
+        int coop = 0, sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lod_fused_kernel, 256, 0) !=
+            cudaSuccess)
+        {
+            cudaGetLastError();
+            per_sm = 0;
+        }
+        g = coop && per_sm > 0 ? sms * std::min(per_sm, 2) : 0;
+    }
+    return uint32_t(g);
+}
+} // namespace
+
 lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                         uint32_t n_views, uint32_t max_depth,
                         cudaStream_t stream)
@@ -484,6 +616,27 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
     SelectScratch& S = ctx->sel;
     if (S.frontier_capacity == 0)
         return fail(ctx, LV_EINVAL, "selection scratch not reserved");
+    const uint32_t grid = n_views == 1 ? fused_grid(ctx) : 0u;
+    if (grid)
+    {
+        /* one view: one cooperative launch, its constants a kernel parameter */
+        LodView V = host_views[0];
+        V.root_offset = 0;
+        const uint32_t cap = S.frontier_capacity;
+        if (V.root_blocks[0] * V.root_blocks[1] * V.root_blocks[2] > cap)
+            return fail(ctx, LV_ENOMEM, "root frontier exceeds scratch capacity");
+        uint32_t* counts = S.counts.as<uint32_t>();
+        LV_CUDA(ctx, cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (kMaxLevels + 8), stream));
+        uint64_t* ids0 = S.ids[0].as<uint64_t>();
+        uint64_t* ids1 = S.ids[1].as<uint64_t>();
+        uint32_t* view0 = S.view[0].as<uint32_t>();
+        uint32_t* view1 = S.view[1].as<uint32_t>();
+        void* args[] = {&V, &max_depth, &ids0, &view0, &ids1, &view1, &counts,
+                        const_cast<uint32_t*>(&cap)};
+        LV_CUDA(ctx, cudaLaunchCooperativeKernel(reinterpret_cast<void*>(lod_fused_kernel),
+                                                 dim3(grid), dim3(256), args, 0, stream));
+        return LV_OK;
+    }
     LV_CUDA(ctx, S.staging.reserve(sizeof(LodView) * n_views));
     LV_CUDA(ctx, S.views.reserve(sizeof(LodView) * n_views));
     /* The pinned staging copy may still be read by a previous in-flight
@@ -551,7 +704,8 @@ lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaSt
         LV_CUDA(ctx, S.ids[i].reserve(sizeof(uint64_t) * cap));
         LV_CUDA(ctx, S.view[i].reserve(sizeof(uint32_t) * cap));
     }
-    LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 2)));
+    /* level counters, overflow flag, fused-launch barrier words */
+    LV_CUDA(ctx, S.counts.reserve(sizeof(uint32_t) * (kMaxLevels + 8)));
     S.frontier_capacity = uint32_t(cap);
     ++S.generation; /* captured graphs referencing the old queues are stale */
     return LV_OK;

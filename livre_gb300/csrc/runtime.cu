@@ -1387,6 +1387,11 @@ extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)
         s.n_passes = P.n_passes;
     }
     *out = s;
+    if (sel[LV_SEL_OVERFLOW] == 2u)
+    {
+        out->error_flags = 4u;
+        return fail(ctx, LV_EDEVICE, "the selection's grid barrier gave up waiting");
+    }
     if (hc[FC_ERROR])
         return fail(ctx, hc[FC_ERROR] == 1 ? LV_ENOMEM : LV_EDEVICE,
                     hc[FC_ERROR] == 1 ? "rendering set overflowed its buffer"
