@@ -65,6 +65,12 @@ def parse():
     return p.parse_args()
 
 
+# DRAM bytes (read + write) of one ray-cast launch of the 2048^3 / 1080p
+# orbit, measured by ncu on a GB300 (18.63 MB read, 0.13 MB written: the
+# visible bricks once; the 8-byte-per-sample gather is served by L1/L2).
+RAYCAST_DRAM_BYTES_PER_LAUNCH = 18.76e6
+
+
 def transfer_function(cfg):
     import livre_gb300 as lv
     if cfg["tf_seed"] is None:
@@ -436,6 +442,7 @@ def gb300_arm(args, cfg):
     import torch
     import livre_gb300 as lv
     from livre_gb300 import build as nb
+    from livre_gb300 import replicas
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -460,7 +467,7 @@ def gb300_arm(args, cfg):
     descs = [ctx.render_desc(mv, pr, W, H, sse=cfg["sse"], early_exit=cfg["early"],
                              step_policy=lv.STEP_HALF_VOXEL, filt=lv.FILTER_TRILINEAR,
                              synchronous=True) for mv, pr in cams]
-    my_frames = [k for k in range(cfg["frames"]) if k % world == rank] or [0]
+    my_frames = replicas.shard(cfg["frames"], rank, world)
     out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
     out8 = torch.empty((H, W, 4), dtype=torch.uint8, device=dev)
     host8 = torch.empty((H, W, 4), dtype=torch.uint8).pin_memory()
@@ -517,14 +524,10 @@ def gb300_arm(args, cfg):
         dist.barrier()
     frame_ms = np.array([a.elapsed_time(b) for a, b in zip(ev0, ev1)])
     total_ms = float(frame_ms.sum())
-    if dist:
-        t = torch.tensor([total_ms, e2e_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_total = float(t[0]), float(t[1])
+    total_ms, e2e_total = replicas.max_over_ranks([total_ms, e2e_total], dist, dev)
     if rank != 0:
         return
-    frames_all = args.steps * world
-    value = frames_all / (total_ms / 1000.0)
+    value = replicas.job_rate(args.steps, world, total_ms / 1000.0)
     ray_ms = np.array([s["raycast_ms"] for s in stats])
     n_samples = np.array([s["n_samples"] for s in stats], dtype=np.float64)
     bpv = vi.bytes_per_voxel
@@ -549,10 +552,15 @@ def gb300_arm(args, cfg):
         "wall_s": wall, "volume_generation_s": gen_s,
         "gpu_launches": int(sum(s["n_launches"] for s in stats)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "raycast_kernel<u8,trilinear>",
+                     "frac": achieved / peak,
+                     "traffic": RAYCAST_DRAM_BYTES_PER_LAUNCH if args.config == "plain2048"
+                     else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                       "one raycast_tiles_kernel launch of this workload",
+                     "algorithmic_bytes_per_launch": float(alg_bytes.mean()),
+                     "kernel": "raycast_tiles_kernel<u8,trilinear>",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800"},
-        "e2e": {"value": args.steps * world / e2e_total, "unit": "frames/s",
+        "e2e": {"value": replicas.job_rate(args.steps, world, e2e_total), "unit": "frames/s",
                 "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": W * H * 4,
                 "note": "pool purged before the timed steps; bricks streamed from pinned host "

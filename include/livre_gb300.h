@@ -372,10 +372,14 @@ enum
     LV_LAUNCH_GRID = 0,
     LV_LAUNCH_TILE_QUEUE = 1,
     LV_LAUNCH_WARP_REFILL = 2,
-    LV_LAUNCH_TILE_GRID = 3 /* one tile_w x tile_h-thread CTA per tile, block i
-                               taking the i-th tile of the order: no resident
-                               grid, so CTAs retire tile by tile and other
-                               kernels (the next frame's selection) interleave */
+    LV_LAUNCH_TILE_GRID = 3, /* one tile_w x tile_h-thread CTA per tile, block i
+                                taking the i-th tile of the order: no resident
+                                grid, so CTAs retire tile by tile and other
+                                kernels (the next frame's selection) interleave */
+    LV_LAUNCH_WARP_TILES = 4 /* a resident grid whose warps each take
+                                tile_w x tile_h = 32-pixel tiles from the queue
+                                on their own (no CTA-wide wait for the slowest
+                                warp of a tile) */
 };
 enum
 {

@@ -27,7 +27,7 @@ from . import _abi
 from ._abi import (BLOB_DEVICE, BLOB_HOST, DT_UINT8, DT_UINT16, FBM_DEVICE, FBM_HOST,
                    FILTER_NEAREST,
                    FILTER_TRILINEAR, LAUNCH_GRID, LAUNCH_TILE_GRID, LAUNCH_TILE_QUEUE,
-                   LAUNCH_WARP_REFILL,
+                   LAUNCH_WARP_REFILL, LAUNCH_WARP_TILES,
                    ORDER_LONGEST_FIRST, ORDER_RASTER,
                    QUEUE_CTA_TILES, QUEUE_VIEW_KERNELS, QUEUE_WARP_REFILL, STEP_HALF_VOXEL,
                    STEP_REFERENCE, LivreError, check, lib)

@@ -96,6 +96,7 @@ LAUNCH_GRID = 0
 LAUNCH_TILE_QUEUE = 1
 LAUNCH_WARP_REFILL = 2
 LAUNCH_TILE_GRID = 3
+LAUNCH_WARP_TILES = 4
 ORDER_RASTER = 0
 ORDER_LONGEST_FIRST = 1
 

@@ -989,6 +989,47 @@ __global__ void __launch_bounds__(256)
         atomicAdd(reinterpret_cast<unsigned long long*>(V.counters + FC_SAMPLES_LO), sum);
 }
 
+/* Resident grid, warp-granular queue: each warp pops a 32-pixel tile (one
+ * ray per lane) from the view's FC_QUEUE counter, in the given order. */
+template <int DT, int FILTER, int EDGE, int LA>
+__global__ void __launch_bounds__(128)
+    raycast_warp_tiles_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h,
+                              const uint32_t* __restrict__ order)
+{
+    const uint32_t n = frame_samples(V);
+    const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
+    const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
+    const uint32_t tiles_x = (V.W + tile_w - 1) / tile_w;
+    const uint32_t total = tiles_x * ((V.H + tile_h - 1) / tile_h);
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t nsamp = 0;
+    for (;;)
+    {
+        uint32_t item = 0;
+        if (lane == 0)
+            item = atomicAdd(V.counters + FC_QUEUE, 1u);
+        item = __shfl_sync(0xFFFFFFFFu, item, 0);
+        if (item >= total)
+            break;
+        const uint32_t tile = order ? order[item] : item;
+        const uint32_t px = (tile % tiles_x) * tile_w + lane % tile_w;
+        const uint32_t py = (tile / tiles_x) * tile_h + lane / tile_w;
+        if (px < V.W && py < V.H)
+        {
+            const RayGeom g = ray_setup(V, px, py);
+            V.out[uint64_t(py) * V.W + px] =
+                march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
+        }
+        __syncwarp();
+    }
+    unsigned long long sum = nsamp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        sum += __shfl_down_sync(0xFFFFFFFFu, sum, o);
+    if (lane == 0 && sum)
+        atomicAdd(reinterpret_cast<unsigned long long*>(V.counters + FC_SAMPLES_LO), sum);
+}
+
 /* ---------------------------------------------------------------- refill
  * Persistent ray cast with lane refill. Every warp takes tile_w x tile_h
  * pixel tiles from a device queue (one atomic per tile) and hands the tile's
@@ -1445,6 +1486,25 @@ template <int DT, int F, int EDGE, int LA>
 lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                             cudaStream_t s, uint8_t* scratch)
 {
+    if (L.kind == LV_LAUNCH_WARP_TILES)
+    {
+        lv_status st = LV_OK;
+        if (!scratch)
+            scratch = render_order_scratch(ctx, V, L, st);
+        if (st != LV_OK)
+            return st;
+        const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+        if (st != LV_OK)
+            return st;
+        auto k = raycast_warp_tiles_kernel<DT, F, EDGE, LA>;
+        const uint32_t tiles =
+            ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
+        const uint32_t grid =
+            std::max(1u, std::min(resident_ctas(ctx, k, 128, 0), (tiles + 3) / 4));
+        k<<<grid, 128, 0, s>>>(V, L.tile_w, L.tile_h, order);
+        LV_CUDA(ctx, cudaGetLastError());
+        return LV_OK;
+    }
     if (L.kind == LV_LAUNCH_TILE_GRID)
     {
         lv_status st = LV_OK;

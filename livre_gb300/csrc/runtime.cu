@@ -944,7 +944,9 @@ extern "C" lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* c
     if (!ctx || !cfg)
         return LV_EINVAL;
     const uint32_t pixels = cfg->tile_w * cfg->tile_h;
-    const bool ok = cfg->kind == LV_LAUNCH_WARP_REFILL
+    const bool ok = cfg->kind == LV_LAUNCH_WARP_TILES
+                        ? pixels == 32
+                    : cfg->kind == LV_LAUNCH_WARP_REFILL
                         ? pixels >= 32 && pixels <= 1024 && cfg->samples_per_check >= 1 &&
                               cfg->samples_per_check <= 64
                         : (cfg->kind == LV_LAUNCH_GRID || cfg->kind == LV_LAUNCH_TILE_QUEUE ||

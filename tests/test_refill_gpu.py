@@ -60,7 +60,7 @@ def test_refill_launches_bit_identical(gpu_ctx):
 def test_render_launch_validation(gpu_ctx):
     import livre_gb300 as lv
     for bad in [(2, 4, 4, 8), (2, 64, 32, 8), (2, 8, 8, 0), (2, 8, 8, 65), (0, 8, 3, 0),
-                (0, 32, 16, 0), (1, 4, 4, 0), (4, 8, 8, 8), (0, 8, 16, 0, 1),
+                (0, 32, 16, 0), (1, 4, 4, 0), (5, 8, 8, 8), (4, 8, 8, 0), (0, 8, 16, 0, 1),
                 (1, 8, 16, 0, 2), (1, 8, 16, 0, 0, 2), (2, 8, 8, 8, 0, 1)]:
         with pytest.raises(lv.LivreError):
             gpu_ctx.set_render_launch(*bad)
