@@ -310,13 +310,16 @@ struct Taps
 /* Voxels around slot coordinate s (nearest: s = local position; trilinear:
  * s = local position - 0.5, texel centres on integers). EDGE = 1 clamps every
  * tap to the brick (GL_CLAMP_TO_EDGE, needed without overlap); EDGE = 0 uses
- * one base address and immediate offsets, valid when every overlap >= 1. */
+ * one base address and offsets to the other taps, valid when every overlap
+ * >= 1; EDGE = n > 1 is EDGE = 0 for bricks of n x n voxels in x and y (the
+ * row and slice pitches become immediate offsets of one pointer). */
 template <int DT, int FILTER, int EDGE>
 __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick,
                                           const float s[3], Taps<FILTER>& T)
 {
     constexpr int bpv = DT == LV_DT_UINT16 ? 2 : 1;
-    const int n0 = int(V.N[0]), n1 = int(V.N[1]), n2 = int(V.N[2]);
+    constexpr int NX = EDGE > 1 ? EDGE : 0;
+    const int n0 = NX ? NX : int(V.N[0]), n1 = NX ? NX : int(V.N[1]), n2 = int(V.N[2]);
     if (FILTER == LV_FILTER_NEAREST)
     {
         const int x = min(max(int(floorf(s[0])), 0), n0 - 1);
@@ -330,7 +333,7 @@ __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick
     T.fy = s[1] - fy0;
     T.fz = s[2] - fz0;
     const int ix = int(fx0), iy = int(fy0), iz = int(fz0);
-    if (EDGE)
+    if (EDGE == 1)
     {
         const int x0 = min(max(ix, 0), n0 - 1), x1 = min(max(ix + 1, 0), n0 - 1);
         const int y0 = min(max(iy, 0), n1 - 1), y1 = min(max(iy + 1, 0), n1 - 1);
@@ -1549,10 +1552,34 @@ lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launc
     return LV_OK;
 }
 
+/* The default launch (one CTA per tile, no look-ahead) for bricks of 66 x 66
+ * voxels in x and y (64^3 + overlap 1), pitches as immediates. */
+template <int DT, int F>
+lv_status tiles66_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                           cudaStream_t s, uint8_t* scratch)
+{
+    lv_status st = LV_OK;
+    if (!scratch)
+        scratch = render_order_scratch(ctx, V, L, st);
+    if (st != LV_OK)
+        return st;
+    const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+    if (st != LV_OK)
+        return st;
+    const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
+    raycast_tiles_kernel<DT, F, 66, 0><<<tiles, L.tile_w * L.tile_h, 0, s>>>(V, L.tile_w,
+                                                                           L.tile_h, order);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
 template <int DT, int F, int EDGE>
 lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                          cudaStream_t s, uint8_t* scratch)
 {
+    if (EDGE == 0 && F == LV_FILTER_TRILINEAR && L.kind == LV_LAUNCH_TILE_GRID &&
+        !L.lookahead && V.N[0] == 66 && V.N[1] == 66)
+        return tiles66_dispatch<DT, F>(ctx, V, L, s, scratch);
     if (L.kind == LV_LAUNCH_WARP_REFILL)
         return refill_dispatch<DT, F, EDGE>(ctx, V, L, s);
     if (L.lookahead)

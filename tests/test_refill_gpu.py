@@ -21,7 +21,10 @@ def scenes(ctx, lv):
     specs = [(lv.VolumeInformation(128, 32, 1), 1, 0, (96, 80)),
              (lv.VolumeInformation(96, 16, 1, dtype=lv.DT_UINT16), 1, 3, (33, 57)),
              (lv.VolumeInformation((128, 96, 64), 16, 0), 0, 0, (70, 41)),
-             (lv.VolumeInformation(64, 16, 0, dtype=lv.DT_UINT16), 1, 0, (5, 3))]
+             (lv.VolumeInformation(64, 16, 0, dtype=lv.DT_UINT16), 1, 0, (5, 3)),
+             # 64^3 bricks + overlap 1: the default launch's 66-voxel pitch path
+             (lv.VolumeInformation(192, 64, 1), 1, 2, (64, 48)),
+             (lv.VolumeInformation((128, 192, 96), 64, 1, dtype=lv.DT_UINT16), 1, 0, (50, 70))]
     for k, (vi, filt, noise, (W, H)) in enumerate(specs):
         vol = ctx.blob_volume(vi, 9, 20 + k, noise)
         mv, proj = lv.orbit_camera(k, 8, vi.world_size, W, H, radius_scale=1.1 + 0.2 * k)
