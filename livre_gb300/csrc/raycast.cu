@@ -1552,11 +1552,12 @@ lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launc
     return LV_OK;
 }
 
-/* The default launch (one CTA per tile, no look-ahead) for bricks of 66 x 66
- * voxels in x and y (64^3 + overlap 1), pitches as immediates. */
-template <int DT, int F>
-lv_status tiles66_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
-                           cudaStream_t s, uint8_t* scratch)
+/* The default launch (one CTA per tile, no look-ahead) for bricks of NX x NX
+ * voxels in x and y, the pitches as immediates: 34, 66 and 130 are the
+ * 32^3, 64^3 and 128^3 bricks with an overlap of 1. */
+template <int DT, int F, int NX>
+lv_status tiles_nx_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                            cudaStream_t s, uint8_t* scratch)
 {
     lv_status st = LV_OK;
     if (!scratch)
@@ -1567,7 +1568,7 @@ lv_status tiles66_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch
     if (st != LV_OK)
         return st;
     const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
-    raycast_tiles_kernel<DT, F, 66, 0><<<tiles, L.tile_w * L.tile_h, 0, s>>>(V, L.tile_w,
+    raycast_tiles_kernel<DT, F, NX, 0><<<tiles, L.tile_w * L.tile_h, 0, s>>>(V, L.tile_w,
                                                                            L.tile_h, order);
     LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;
@@ -1578,8 +1579,15 @@ lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& 
                          cudaStream_t s, uint8_t* scratch)
 {
     if (EDGE == 0 && F == LV_FILTER_TRILINEAR && L.kind == LV_LAUNCH_TILE_GRID &&
-        !L.lookahead && V.N[0] == 66 && V.N[1] == 66)
-        return tiles66_dispatch<DT, F>(ctx, V, L, s, scratch);
+        !L.lookahead && V.N[0] == V.N[1])
+    {
+        if (V.N[0] == 66)
+            return tiles_nx_dispatch<DT, F, 66>(ctx, V, L, s, scratch);
+        if (V.N[0] == 34)
+            return tiles_nx_dispatch<DT, F, 34>(ctx, V, L, s, scratch);
+        if (V.N[0] == 130)
+            return tiles_nx_dispatch<DT, F, 130>(ctx, V, L, s, scratch);
+    }
     if (L.kind == LV_LAUNCH_WARP_REFILL)
         return refill_dispatch<DT, F, EDGE>(ctx, V, L, s);
     if (L.lookahead)

@@ -22,8 +22,11 @@ def scenes(ctx, lv):
              (lv.VolumeInformation(96, 16, 1, dtype=lv.DT_UINT16), 1, 3, (33, 57)),
              (lv.VolumeInformation((128, 96, 64), 16, 0), 0, 0, (70, 41)),
              (lv.VolumeInformation(64, 16, 0, dtype=lv.DT_UINT16), 1, 0, (5, 3)),
-             # 64^3 bricks + overlap 1: the default launch's 66-voxel pitch path
+             # 32^3 / 64^3 / 128^3 bricks + overlap 1: the default launch's
+             # fixed-pitch paths
+             (lv.VolumeInformation(96, 32, 1, dtype=lv.DT_UINT16), 1, 1, (40, 24)),
              (lv.VolumeInformation(192, 64, 1), 1, 2, (64, 48)),
+             (lv.VolumeInformation(256, 128, 1), 1, 0, (48, 40)),
              (lv.VolumeInformation((128, 192, 96), 64, 1, dtype=lv.DT_UINT16), 1, 0, (50, 70))]
     for k, (vi, filt, noise, (W, H)) in enumerate(specs):
         vol = ctx.blob_volume(vi, 9, 20 + k, noise)
