@@ -289,8 +289,6 @@ lv_status launch_batch_order(lv_ctx* ctx, const RayView* d_rays, const TileQueue
 lv_status launch_persistent(lv_ctx* ctx, int variant, const lv_batch_config& cfg,
                             const RayView* d_rays, const TileQueue& Q, uint32_t tfn_max,
                             cudaStream_t s);
-lv_status launch_resolve_views(lv_ctx* ctx, const ResolveView* d_views,
-                               uint32_t n_views, cudaStream_t s);
 } // namespace lv
 
 struct lv_tf
