@@ -62,6 +62,8 @@ def parse():
                         "persistent launch), served (Poisson request stream), outofcore "
                         "(8192^3 u16 fly-through through a 64 GiB pool)")
     p.add_argument("--serve-seconds", type=float, default=1.5)
+    p.add_argument("--serve-rates", type=lambda t: [int(x) for x in t.split(",")],
+                   default=[200, 500, 1000, 2000], help="Poisson request rates (req/s)")
     return p.parse_args()
 
 
@@ -347,10 +349,15 @@ def served_mode(ctx, args, dev, seed=11):
         prof = srv.profile()
         srv.close()
         lat = np.array([r["latency_ms"] for r in res])
+        queued = np.array([r["queue_ms"] for r in res])
         return {"rate_req_s": rate, "requests": len(reqs),
                 "frames_per_s": len(reqs) / wall, "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)),
                 "mean_batch": float(np.mean([r["batch_size"] for r in res])),
+                "queue_p50_ms": float(np.percentile(queued, 50)),
+                "queue_p99_ms": float(np.percentile(queued, 99)),
+                "service_p50_ms": float(np.percentile(lat - queued, 50)),
+                "service_p99_ms": float(np.percentile(lat - queued, 99)),
                 "failed": int(sum(r["status"] != 0 for r in res)),
                 "profile": {k: (round(v - prof0[k], 2) if isinstance(v, float)
                                 else v - prof0[k]) for k, v in prof.items()}}
@@ -362,7 +369,7 @@ def served_mode(ctx, args, dev, seed=11):
     ctx.last_stats()
     out = {"volumes": "8 blob volumes 256^3..4096^3 u8/u16, 64^3 bricks",
            "pool_gib": args.pool_gib or 96, "rates": []}
-    for rate in (200, 500, 1000, 2000):
+    for rate in args.serve_rates:
         reqs = [make_request() for _ in range(max(64, int(rate * args.serve_seconds)))]
         served = run(0, rate, reqs)
         plain = run(1, rate, reqs)
