@@ -864,6 +864,26 @@ __global__ void __launch_bounds__(256)
  * zeroed before the key pass. */
 constexpr uint32_t kTileBuckets = 64;
 
+/* Slot of an item of class `key` in the sorted order: the class's first
+ * slot (base, shared memory) plus the item's rank among the class's items
+ * claimed so far, one global atomic per class present in the warp (items of
+ * one class are many: per-item atomics on one cursor serialised). key =
+ * kTileBuckets: no item (the lane still takes part in the warp-wide
+ * match). */
+__device__ __forceinline__ uint32_t base_of_item(const uint32_t* base, uint32_t* hist,
+                                                 uint32_t key)
+{
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t leader = __ffs(peers) - 1u;
+    uint32_t first = 0;
+    if (lane == leader && key < kTileBuckets)
+        first = atomicAdd(&hist[kTileBuckets + key], __popc(peers));
+    first = __shfl_sync(0xFFFFFFFFu, first, leader); /* each lane: its class's leader */
+    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+    return key < kTileBuckets ? base[key] + first + rank : 0xFFFFFFFFu;
+}
+
 __global__ void __launch_bounds__(256)
     tile_key_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h, uint32_t tiles_x,
                     uint32_t total, float buckets_per_length, uint8_t* __restrict__ keys,
@@ -913,13 +933,10 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < total)
-    {
-        const uint32_t key = keys[t];
-        const uint32_t pos = base[key] + atomicAdd(&hist[kTileBuckets + key], 1u);
-        if (pos < total)
-            order[pos] = t;
-    }
+    const uint32_t key = t < total ? keys[t] : kTileBuckets;
+    const uint32_t pos = base_of_item(base, hist, key);
+    if (t < total && pos < total)
+        order[pos] = t;
 }
 
 /* Single view on a resident grid: CTAs take tile_w x tile_h pixel tiles
@@ -1143,12 +1160,13 @@ __global__ void __launch_bounds__(256)
     }
     __syncthreads();
     const uint32_t total = Q.tile_start[*Q.n_views];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total;
-         i += gridDim.x * blockDim.x)
+    /* warp-uniform trip count: every lane reaches the warp-wide match */
+    for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < total; b0 += gridDim.x * blockDim.x)
     {
-        const uint32_t key = keys[i];
-        const uint32_t pos = base[key] + atomicAdd(&hist[kTileBuckets + key], 1u);
-        if (pos < total)
+        const uint32_t i = b0 + threadIdx.x;
+        const uint32_t key = i < total ? keys[i] : kTileBuckets;
+        const uint32_t pos = base_of_item(base, hist, key);
+        if (i < total && pos < total)
             order[pos] = i;
     }
 }
