@@ -226,6 +226,46 @@ lv_status lv_fbm_generate(lv_ctx* ctx, const lv_volume_info* info,
                           const lv_fbm_params* params, const uint64_t* ids, uint32_t n,
                           void* d_out, void* stream);
 
+/* Data sources registered at run time, tried by lv_volume_open before the
+ * built-in ones in registration order: the plugin factory of the reference
+ * (livre/data/DataSource.cpp:29-63), which a C++ plugin reaches through
+ * lunchbox::PluginRegisterer (include/lunchbox/pluginRegisterer.h).
+ * handles(user, uri) != 0 when the source opens `uri`; open fills the
+ * volume description (fillRegularVolumeInfo applied) and the brick callback,
+ * whose `source` pointer source_free releases with the volume. */
+typedef int (*lv_source_handles_fn)(void* user, const char* uri);
+typedef lv_status (*lv_source_open_fn)(void* user, const char* uri, lv_volume_info* info,
+                                       lv_get_data_fn* get_data, void** source,
+                                       void (**source_free)(void*));
+lv_status lv_register_source(lv_source_handles_fn handles, lv_source_open_fn open, void* user,
+                             const char* description);
+lv_status lv_unregister_source(lv_source_handles_fn handles, lv_source_open_fn open);
+/* The data source for `uri` without a context or device, as
+ * livre::DataSource(uri) constructs it (livre/data/DataSource.cpp:29-56): a
+ * registered source that handles `uri`, else a built-in one (mem://, raw://).
+ * Fills the volume description and the brick callback; source_free(*source)
+ * releases it. LV_EINVAL when no source handles `uri` or it fails to open. */
+lv_status lv_source_open(const char* uri, lv_volume_info* info, lv_get_data_fn* get_data,
+                         void** source, void (**source_free)(void*));
+/* The description of the volume lv_source_open gives for `uri` (the source is
+ * opened and closed again). */
+lv_status lv_source_probe(const char* uri, lv_volume_info* info);
+/* DataSource::loadPlugins (livre/data/DataSource.cpp:58-62): loads every
+ * shared library ending in ".so" whose file name contains a match of the
+ * regular expression `pattern` (NULL: "Livre.*Source"), found in the
+ * ':'-separated directories `paths` (NULL: LD_LIBRARY_PATH). Their static
+ * PluginRegisterer objects register their sources; the libraries stay loaded.
+ * *n_loaded (may be NULL) counts the libraries newly loaded. A library that
+ * fails to load is skipped, as the reference's factory does. */
+lv_status lv_load_plugins(const char* paths, const char* pattern, uint32_t* n_loaded);
+/* DataSource::getDescriptions (livre/data/DataSource.cpp:64-68): the
+ * descriptions of the registered sources, then of the built-in ones, as one
+ * NUL-terminated string; out = NULL asks for the size (with the NUL). */
+lv_status lv_source_descriptions(char* out, size_t capacity, size_t* size);
+/* DataSource::handles (livre/data/DataSource.cpp:70-74): 1 when a
+ * registered or built-in source opens `uri`, else 0. */
+int lv_source_handles(const char* uri);
+
 /* A volume opened from a URI by the built-in data sources, like
  * livre::DataSource(uri) (livre/data/DataSource.cpp:29-63):
  *   mem://[#w,h,d,block][?datatype=T]   MemoryDataSource (constant bricks)

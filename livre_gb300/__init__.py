@@ -265,6 +265,87 @@ def encode_png(rgba8):
     return bytes(out)
 
 
+# ------------------------------------------------------------- data-source plugins
+def load_plugins(paths=None, pattern=None):
+    """DataSource::loadPlugins: loads the plugin libraries matching `pattern`
+    (default "Livre.*Source") from the ':'-separated `paths` (default
+    LD_LIBRARY_PATH); returns how many were newly loaded."""
+    n = C.c_uint32()
+    check(lib().lv_load_plugins(None if paths is None else paths.encode(),
+                                None if pattern is None else pattern.encode(), C.byref(n)))
+    return n.value
+
+
+def source_handles(uri):
+    """DataSource::handles: True when a registered or built-in source opens `uri`."""
+    return bool(lib().lv_source_handles(uri.encode()))
+
+
+def probe_source(uri):
+    """The VolumeInformation a registered plugin source gives for `uri`."""
+    info = _abi.VolumeInfo()
+    check(lib().lv_source_probe(uri.encode(), C.byref(info)))
+    vi = VolumeInformation.__new__(VolumeInformation)
+    vi.info = info
+    return vi
+
+
+def source_descriptions():
+    """DataSource::getDescriptions: registered sources first, then built-in."""
+    n = C.c_size_t()
+    check(lib().lv_source_descriptions(None, 0, C.byref(n)))
+    buf = C.create_string_buffer(n.value)
+    check(lib().lv_source_descriptions(buf, n.value, C.byref(n)))
+    return buf.value.decode()
+
+
+class DataSource:
+    """livre::DataSource on the host (lv_source_open): the volume description
+    and bricks of a URI, read without a context or device."""
+
+    def __init__(self, uri):
+        info = _abi.VolumeInfo()
+        fn, src, free = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(lib().lv_source_open(uri.encode(), C.byref(info), C.byref(fn), C.byref(src),
+                                   C.byref(free)))
+        self._fn = _abi.GET_DATA_FN(fn.value)
+        self._free = C.CFUNCTYPE(None, C.c_void_p)(free.value) if free.value else None
+        self._src = src.value
+        self.info = VolumeInformation.__new__(VolumeInformation)
+        self.info.info = info
+
+    def get_data(self, node_id):
+        """The brick of `node_id` (brick_bytes uint8), or None when the
+        source has no data for it or it lies outside the octree."""
+        nid = NodeId(int(node_id)) if not isinstance(node_id, NodeId) else node_id
+        r = self.info.root_blocks
+        L = nid.level
+        if (not nid.is_valid() or L >= self.info.depth or
+                any(p >= (b << L) for p, b in zip(nid.position, r))):
+            return None
+        out = np.zeros(self.info.brick_bytes, np.uint8)
+        if self._fn(self._src, int(nid), out.ctypes.data, out.size) != 0:
+            return None
+        return out
+
+    def close(self):
+        if self._free is not None:
+            self._free(self._src)
+            self._free = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def fbm_params(seed, octaves=6, lacunarity=2.0, gain=0.5, frequency=8.0):
     return _abi.FbmParams(seed, octaves, lacunarity, gain, frequency)
 

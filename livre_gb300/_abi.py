@@ -199,6 +199,14 @@ _SIGNATURES = {
     "lv_server_destroy": (None, [C.c_void_p]),
     "lv_frame_to_rgba8": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
                                     C.c_void_p, C.c_void_p]),
+    "lv_register_source": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p]),
+    "lv_source_descriptions": (C.c_int, [C.c_void_p, C.c_size_t, P(C.c_size_t)]),
+    "lv_unregister_source": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lv_source_probe": (C.c_int, [C.c_char_p, P(VolumeInfo)]),
+    "lv_source_open": (C.c_int, [C.c_char_p, P(VolumeInfo), P(C.c_void_p), P(C.c_void_p),
+                                 P(C.c_void_p)]),
+    "lv_load_plugins": (C.c_int, [C.c_char_p, C.c_char_p, P(C.c_uint32)]),
+    "lv_source_handles": (C.c_int, [C.c_char_p]),
 }
 
 _lib = None

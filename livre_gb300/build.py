@@ -61,8 +61,10 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(_compile, sources()))
     tmp = LIB + ".tmp%d" % os.getpid()
+    # the soname lets a plugin library linked with -llivre_gb300 bind to the
+    # copy already loaded (one source registry per process)
     cmd = [NVCC, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static",
-           "-Xcompiler", "-fPIC", "-lpthread"]
+           "-Xcompiler", "-fPIC", "-Xlinker", "-soname=liblivre_gb300.so", "-lpthread", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

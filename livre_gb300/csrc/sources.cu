@@ -12,12 +12,19 @@
  *
  * Both feed the pool through the same lv_get_data_fn path as user plugins.
  */
+#include <dirent.h>
+#include <dlfcn.h>
 #include <fcntl.h>
 #include <sys/mman.h>
 #include <sys/stat.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <regex>
+#include <set>
+#include <vector>
 #include <cstdlib>
 #include <fstream>
 #include <sstream>
@@ -37,11 +44,14 @@ struct Uri
 Uri parse_uri(const std::string& s)
 {
     Uri u;
+    /* no scheme: the whole string is a path (a bare file name) */
     const size_t sep = s.find("://");
-    if (sep == std::string::npos)
-        return u;
-    u.scheme = s.substr(0, sep);
-    std::string rest = s.substr(sep + 3);
+    std::string rest = s;
+    if (sep != std::string::npos)
+    {
+        u.scheme = s.substr(0, sep);
+        rest = s.substr(sep + 3);
+    }
     const size_t hash = rest.find('#');
     if (hash != std::string::npos)
     {
@@ -271,17 +281,193 @@ bool ends_with(const std::string& s, const std::string& e)
 }
 } // namespace
 
-extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** out)
+namespace
 {
-    if (!ctx || !uri_c || !out)
-        return fail(ctx, LV_EINVAL, "null argument");
+/* RawDataSource::handles (RawDataSource.cpp:241-252): the raw scheme, or no
+ * scheme and a .raw / .img / .nrrd file */
+bool is_raw_uri(const Uri& uri)
+{
+    if (uri.scheme == "raw")
+        return true;
+    return uri.scheme.empty() && (ends_with(uri.path, ".raw") || ends_with(uri.path, ".img") ||
+                                  ends_with(uri.path, ".nrrd"));
+}
+
+/* Data sources registered at run time (plugins), in registration order. */
+struct SourceEntry
+{
+    lv_source_handles_fn handles;
+    lv_source_open_fn open;
+    void* user;
+    std::string description;
+};
+std::mutex g_sources_mutex;
+std::vector<SourceEntry>& registered_sources()
+{
+    static std::vector<SourceEntry> v;
+    return v;
+}
+
+/* The first registered source that handles `uri` (copied under the lock). */
+bool find_source(const char* uri, SourceEntry& out)
+{
+    std::vector<SourceEntry> copy;
+    {
+        std::lock_guard<std::mutex> lock(g_sources_mutex);
+        copy = registered_sources();
+    }
+    for (const SourceEntry& e : copy)
+        if (e.handles && e.handles(e.user, uri))
+        {
+            out = e;
+            return true;
+        }
+    return false;
+}
+} // namespace
+
+extern "C" lv_status lv_register_source(lv_source_handles_fn handles, lv_source_open_fn open,
+                                        void* user, const char* description)
+{
+    if (!handles || !open)
+        return LV_EINVAL;
+    std::lock_guard<std::mutex> lock(g_sources_mutex);
+    registered_sources().push_back(
+        SourceEntry{handles, open, user, description ? description : ""});
+    return LV_OK;
+}
+
+extern "C" lv_status lv_source_descriptions(char* out, size_t capacity, size_t* size)
+{
+    if (!size)
+        return LV_EINVAL;
+    /* the registered sources, then the built-in ones, one blank line apart */
+    std::string text;
+    {
+        std::lock_guard<std::mutex> lock(g_sources_mutex);
+        for (const SourceEntry& e : registered_sources())
+            if (!e.description.empty())
+                text += e.description + "\n\n";
+    }
+    text += "Memory volume: mem://[#w,h,d,block][?datatype=T], one constant value per brick, "
+            "overlap 4\n\n"
+            "Raw volume: raw://file.raw#x,y,z[,T] or raw://file.nrrd[?output=T], the whole "
+            "file as one brick";
+    *size = text.size() + 1;
+    if (!out)
+        return LV_OK; /* size query */
+    if (capacity < text.size() + 1)
+        return LV_ENOMEM;
+    std::memcpy(out, text.c_str(), text.size() + 1);
+    return LV_OK;
+}
+
+extern "C" lv_status lv_unregister_source(lv_source_handles_fn handles, lv_source_open_fn open)
+{
+    std::lock_guard<std::mutex> lock(g_sources_mutex);
+    auto& v = registered_sources();
+    const size_t before = v.size();
+    v.erase(std::remove_if(v.begin(), v.end(),
+                           [&](const SourceEntry& e) {
+                               return e.handles == handles && e.open == open;
+                           }),
+            v.end());
+    return v.size() < before ? LV_OK : LV_ENOTFOUND;
+}
+
+extern "C" int lv_source_handles(const char* uri_c)
+{
+    if (!uri_c)
+        return 0;
+    SourceEntry e;
+    if (find_source(uri_c, e))
+        return 1;
+    /* MemoryDataSource::handles and RawDataSource::handles
+     * (MemoryDataSource.cpp:153-156, RawDataSource.cpp:241-252) */
     const Uri uri = parse_uri(uri_c);
-    lv_volume_info info{};
+    return uri.scheme == "mem" || is_raw_uri(uri) ? 1 : 0;
+}
+
+extern "C" lv_status lv_load_plugins(const char* paths, const char* pattern, uint32_t* n_loaded)
+{
+    if (n_loaded)
+        *n_loaded = 0;
+    const char* env = std::getenv("LD_LIBRARY_PATH");
+    const std::string dirs = paths ? paths : (env ? env : "");
+    std::regex re;
+    try
+    {
+        re = std::regex(pattern ? pattern : "Livre.*Source");
+    }
+    catch (const std::regex_error&)
+    {
+        return LV_EINVAL;
+    }
+    static std::mutex m;
+    static std::set<std::string> loaded; /* canonical paths, never unloaded */
+    std::lock_guard<std::mutex> lock(m);
+    uint32_t count = 0;
+    for (const std::string& dir : split(dirs, ':'))
+    {
+        if (dir.empty())
+            continue;
+        DIR* d = opendir(dir.c_str());
+        if (!d)
+            continue;
+        std::vector<std::string> names;
+        while (const dirent* e = readdir(d))
+        {
+            const std::string name = e->d_name;
+            if (ends_with(name, ".so") && std::regex_search(name, re))
+                names.push_back(name);
+        }
+        closedir(d);
+        std::sort(names.begin(), names.end());
+        for (const std::string& name : names)
+        {
+            const std::string path = dir + "/" + name;
+            char* real = realpath(path.c_str(), nullptr);
+            const std::string key = real ? real : path;
+            std::free(real);
+            if (loaded.count(key))
+                continue;
+            if (dlopen(key.c_str(), RTLD_NOW | RTLD_LOCAL))
+            {
+                loaded.insert(key);
+                ++count;
+            }
+        }
+    }
+    if (n_loaded)
+        *n_loaded = count;
+    return LV_OK;
+}
+
+namespace
+{
+/* The data source for `uri`: the first registered source that handles it,
+ * else a built-in one. On failure `err` says why and nothing is left open. */
+lv_status open_source(const char* uri_c, lv_volume_info& info, lv_get_data_fn& fn, void*& user,
+                      void (*&user_free)(void*), std::string& err)
+{
+    const Uri uri = parse_uri(uri_c);
+    info = lv_volume_info{};
     info.comp_count = 1;
-    lv_get_data_fn fn = nullptr;
-    void* user = nullptr;
-    void (*user_free)(void*) = nullptr;
-    if (uri.scheme == "mem")
+    fn = nullptr;
+    user = nullptr;
+    user_free = nullptr;
+    const auto bad = [&err](lv_status st, const std::string& why) {
+        err = why;
+        return st;
+    };
+    SourceEntry plugin;
+    if (find_source(uri_c, plugin))
+    {
+        const lv_status st = plugin.open(plugin.user, uri_c, &info, &fn, &user, &user_free);
+        if (st != LV_OK)
+            return bad(st, std::string("the registered source failed to open ") + uri_c);
+    }
+    else if (uri.scheme == "mem")
     {
         /* MemoryDataSource::MemoryDataSource (MemoryDataSource.cpp:63-117) */
         int dt = LV_DT_UINT8;
@@ -289,10 +475,10 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
         if (!t.empty())
             dt = parse_type(t);
         if (dt < 0)
-            return fail(ctx, LV_EINVAL, "unsupported mem:// datatype " + t);
+            return bad(LV_EINVAL, "unsupported mem:// datatype " + t);
         if (!query_value(uri.query, "sparsity").empty() &&
             std::atof(query_value(uri.query, "sparsity").c_str()) < 1.0)
-            return fail(ctx, LV_EINVAL, "mem:// sparsity < 1 is not supported");
+            return bad(LV_EINVAL, "mem:// sparsity < 1 is not supported");
         uint32_t dims[3] = {4096, 4096, 4096}, block = 32;
         const std::vector<std::string> p = split(uri.fragment, ',');
         if (p.size() >= 4)
@@ -302,7 +488,7 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
             block = uint32_t(std::strtoul(p[3].c_str(), nullptr, 10));
         }
         if (!dims[0] || !dims[1] || !dims[2] || !block)
-            return fail(ctx, LV_EINVAL, "invalid mem:// fragment");
+            return bad(LV_EINVAL, "invalid mem:// fragment");
         for (int i = 0; i < 3; ++i)
         {
             info.voxels[i] = dims[i];
@@ -311,13 +497,13 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
         }
         info.dtype = uint32_t(dt);
         if (lv_fill_regular_volume_info(&info) != LV_OK)
-            return fail(ctx, LV_EINVAL, "cannot set up the regular tree");
+            return bad(LV_EINVAL, "cannot set up the regular tree");
         MemorySource* m = new MemorySource{dt};
         fn = memory_get_data;
         user = m;
         user_free = memory_free;
     }
-    else if (uri.scheme == "raw")
+    else if (is_raw_uri(uri))
     {
         /* RawDataSource::Impl (RawDataSource.cpp:67-262) */
         RawSource* r = new RawSource();
@@ -331,7 +517,7 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
             if (p.size() < 3)
             {
                 delete r;
-                return fail(ctx, LV_EINVAL, "not enough parameters for the raw file");
+                return bad(LV_EINVAL, "not enough parameters for the raw file");
             }
             for (int i = 0; i < 3; ++i)
                 dims[i] = uint32_t(std::strtoul(p[i].c_str(), nullptr, 10));
@@ -340,7 +526,7 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
             if (!map_file(*r, uri.path))
             {
                 delete r;
-                return fail(ctx, LV_ENOTFOUND, "cannot mmap file " + uri.path);
+                return bad(LV_ENOTFOUND, "cannot mmap file " + uri.path);
             }
         }
         else if (is_nrrd)
@@ -350,7 +536,7 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
             if (!parse_nrrd(uri.path, kv, header))
             {
                 delete r;
-                return fail(ctx, LV_EINVAL, "cannot parse nrrd file " + uri.path);
+                return bad(LV_EINVAL, "cannot parse nrrd file " + uri.path);
             }
             std::string data_file = uri.path;
             if (kv.count("data file") || kv.count("datafile"))
@@ -368,13 +554,13 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
             if (kv.count("encoding") && kv["encoding"] != "raw")
             {
                 delete r;
-                return fail(ctx, LV_EINVAL, "only raw nrrd encoding is supported");
+                return bad(LV_EINVAL, "only raw nrrd encoding is supported");
             }
             const std::vector<std::string> sz = split(kv["sizes"], ' ');
             if (sz.size() < 3)
             {
                 delete r;
-                return fail(ctx, LV_EINVAL, "nrrd sizes must have 3 entries");
+                return bad(LV_EINVAL, "nrrd sizes must have 3 entries");
             }
             for (int i = 0; i < 3; ++i)
                 dims[i] = uint32_t(std::strtoul(sz[i].c_str(), nullptr, 10));
@@ -382,19 +568,19 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
             if (!map_file(*r, data_file))
             {
                 delete r;
-                return fail(ctx, LV_ENOTFOUND, "cannot mmap file " + data_file);
+                return bad(LV_ENOTFOUND, "cannot mmap file " + data_file);
             }
             r->header = header;
         }
         else
         {
             delete r;
-            return fail(ctx, LV_EINVAL, "volume extension does not include raw or nrrd");
+            return bad(LV_EINVAL, "volume extension does not include raw or nrrd");
         }
         if (in_type < 0 || !dims[0] || !dims[1] || !dims[2])
         {
             delete r;
-            return fail(ctx, LV_EINVAL, "unsupported raw volume description");
+            return bad(LV_EINVAL, "unsupported raw volume description");
         }
         int out_type = in_type;
         const std::string o = query_value(uri.query, "output");
@@ -403,7 +589,7 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
         if (out_type < 0)
         {
             delete r;
-            return fail(ctx, LV_EINVAL, "unsupported output type " + o);
+            return bad(LV_EINVAL, "unsupported output type " + o);
         }
         r->in_type = in_type;
         r->out_type = out_type;
@@ -411,7 +597,7 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
         if (r->header + r->voxels * type_bytes(in_type) > r->map_bytes)
         {
             delete r;
-            return fail(ctx, LV_EINVAL, "raw file smaller than its volume");
+            return bad(LV_EINVAL, "raw file smaller than its volume");
         }
         const uint32_t maxv = std::max(dims[0], std::max(dims[1], dims[2]));
         info.world_space_per_voxel = 1.0f / float(maxv);
@@ -430,12 +616,51 @@ extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** 
         user_free = raw_free;
     }
     else
-        return fail(ctx, LV_EINVAL, "no data source handles '" + uri.scheme + "://'");
+        return bad(LV_EINVAL, "no data source handles '" + uri.scheme + "://'");
+    return LV_OK;
+}
+} // namespace
+
+extern "C" lv_status lv_source_open(const char* uri, lv_volume_info* info, lv_get_data_fn* get_data,
+                                    void** source, void (**source_free)(void*))
+{
+    if (!uri || !info || !get_data || !source || !source_free)
+        return LV_EINVAL;
+    std::string err;
+    return open_source(uri, *info, *get_data, *source, *source_free, err);
+}
+
+extern "C" lv_status lv_source_probe(const char* uri, lv_volume_info* info)
+{
+    if (!uri || !info)
+        return LV_EINVAL;
+    lv_get_data_fn fn = nullptr;
+    void* source = nullptr;
+    void (*source_free)(void*) = nullptr;
+    const lv_status st = lv_source_open(uri, info, &fn, &source, &source_free);
+    if (st == LV_OK && source_free)
+        source_free(source);
+    return st;
+}
+
+extern "C" lv_status lv_volume_open(lv_ctx* ctx, const char* uri_c, lv_volume** out)
+{
+    if (!ctx || !uri_c || !out)
+        return fail(ctx, LV_EINVAL, "null argument");
+    lv_volume_info info{};
+    lv_get_data_fn fn = nullptr;
+    void* user = nullptr;
+    void (*user_free)(void*) = nullptr;
+    std::string err;
+    const lv_status opened = open_source(uri_c, info, fn, user, user_free, err);
+    if (opened != LV_OK)
+        return fail(ctx, opened, err);
     lv_volume* v = nullptr;
     lv_status st = lv_volume_create(ctx, &info, fn, user, &v);
     if (st != LV_OK)
     {
-        user_free(user);
+        if (user_free)
+            user_free(user);
         return st;
     }
     v->user_free = user_free;

@@ -13,7 +13,7 @@ def declared_symbols():
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        for m in re.finditer(r"\b(lv_[a-z0-9_]+)\s*\(", text):
+        for m in re.finditer(r"\b(lv_[a-z0-9_]+)\s*\((?!\*)", text):  # not "T (*fn)("
             names.add(m.group(1))
     return names
 
