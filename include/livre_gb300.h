@@ -160,8 +160,10 @@ lv_status lv_pool_purge(lv_ctx* ctx);
 /* livre::DataSourcePlugin::getData (livre/data/DataSourcePlugin.h:81) as a C
  * callback: fill `dst` (page-locked host memory, `bytes` long: the node's
  * (block + 2 * overlap)^3 voxels, x fastest) for `node_id` and return 0, or
- * return nonzero for a null MemoryUnitPtr. Called from library worker
- * threads; must be thread-safe like the reference plugin contract. */
+ * return nonzero for a null MemoryUnitPtr. Called from the thread that
+ * renders, one brick at a time (the reference's single upload thread,
+ * livre/lib/pipeline/RenderPipeline.cpp:42), unless the volume's fetch
+ * threads are raised. */
 typedef int (*lv_get_data_fn)(void* user, uint64_t node_id, void* dst,
                               size_t bytes);
 
@@ -169,6 +171,13 @@ typedef int (*lv_get_data_fn)(void* user, uint64_t node_id, void* dst,
 lv_status lv_volume_create(lv_ctx* ctx, const lv_volume_info* info,
                            lv_get_data_fn get_data, void* user,
                            lv_volume** out);
+/* Host threads that call the volume's get_data at once for a frame's missing
+ * bricks (0: one per hardware thread, at most 64; default 1). Above 1 the
+ * callback must be re-entrant. Each thread fills its own page-locked staging
+ * buffer; a group's copies to the device overlap the next group's fetch.
+ * LV_EINVAL for a volume that is not fed by a callback. */
+lv_status lv_volume_set_fetch_threads(lv_volume* vol, uint32_t threads);
+lv_status lv_volume_get_fetch_threads(const lv_volume* vol, uint32_t* threads);
 
 /* Synthetic blob volume: sum of n_blobs isotropic Gaussians (centres uniform
  * in the volume, sigma U[8,32] voxels, amplitude U[0.3,1], cut off at
@@ -208,9 +217,10 @@ typedef struct lv_fbm_params
 enum
 {
     LV_FBM_DEVICE = 0, /* generated on the device, straight into the pool */
-    LV_FBM_HOST = 1    /* generated per brick on the host when it misses (a
-                          data-source callback over host_threads threads),
-                          then streamed host->device */
+    LV_FBM_HOST = 1    /* generated on the host when it misses (a
+                          data-source callback, one brick per fetch thread,
+                          host_threads of them: 0 = one per hardware
+                          thread), then streamed host->device */
 };
 lv_status lv_volume_create_fbm(lv_ctx* ctx, const lv_volume_info* info,
                                const lv_fbm_params* params, uint32_t placement,

@@ -466,6 +466,17 @@ class Volume:
                                  acc.ctypes.data_as(C.POINTER(C.c_uint64))), self.ctx.handle)
         return (acc, pb) if per_brick else acc
 
+    @property
+    def fetch_threads(self):
+        """Host threads calling the source's getData at once (callback sources)."""
+        n = C.c_uint32()
+        check(lib().lv_volume_get_fetch_threads(self.handle, C.byref(n)), self.ctx.handle)
+        return n.value
+
+    @fetch_threads.setter
+    def fetch_threads(self, n):
+        check(lib().lv_volume_set_fetch_threads(self.handle, int(n)), self.ctx.handle)
+
     def resident(self):
         """Resident node ids, oldest load first."""
         n = C.c_uint32()

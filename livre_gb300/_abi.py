@@ -203,6 +203,8 @@ _SIGNATURES = {
     "lv_source_descriptions": (C.c_int, [C.c_void_p, C.c_size_t, P(C.c_size_t)]),
     "lv_unregister_source": (C.c_int, [C.c_void_p, C.c_void_p]),
     "lv_source_probe": (C.c_int, [C.c_char_p, P(VolumeInfo)]),
+    "lv_volume_set_fetch_threads": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "lv_volume_get_fetch_threads": (C.c_int, [C.c_void_p, P(C.c_uint32)]),
     "lv_source_open": (C.c_int, [C.c_char_p, P(VolumeInfo), P(C.c_void_p), P(C.c_void_p),
                                  P(C.c_void_p)]),
     "lv_load_plugins": (C.c_int, [C.c_char_p, C.c_char_p, P(C.c_uint32)]),

@@ -361,9 +361,8 @@ extern "C" lv_status lv_volume_create_fbm(lv_ctx* ctx, const lv_volume_info* inf
         return fail(ctx, LV_EINVAL, "fBm: 1..16 octaves, a positive frequency");
     if (placement == LV_FBM_HOST)
     {
-        FbmSource* src = new FbmSource{*info, *params, fbm_permutation(params->seed),
-                                       host_threads ? host_threads
-                                                    : std::max(1u, std::thread::hardware_concurrency())};
+        /* one brick per fetch thread (the generator is re-entrant) */
+        FbmSource* src = new FbmSource{*info, *params, fbm_permutation(params->seed), 1u};
         lv_status st = lv_volume_create(ctx, info, fbm_source_get, src, out);
         if (st != LV_OK)
         {
@@ -371,7 +370,13 @@ extern "C" lv_status lv_volume_create_fbm(lv_ctx* ctx, const lv_volume_info* inf
             return st;
         }
         (*out)->user_free = fbm_source_free;
-        return LV_OK;
+        st = lv_volume_set_fetch_threads(*out, std::min(host_threads, 64u));
+        if (st != LV_OK)
+        {
+            lv_volume_destroy(*out);
+            *out = nullptr;
+        }
+        return st;
     }
     if (placement != LV_FBM_DEVICE)
         return fail(ctx, LV_EINVAL, "unknown fBm placement");

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "host_pool.h"
 #include "lv_internal.h"
 
 namespace lv
@@ -121,6 +122,8 @@ struct lv_ctx
     size_t pool_bytes = size_t(3072) << 20;
     /* lv_render's ray cast */
     lv_render_launch launch{LV_LAUNCH_TILE_GRID, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 0};
+    /* host fetchers of callback sources (created on first use) */
+    lv::HostPool* host_pool = nullptr;
     std::mutex mutex;
 };
 
@@ -322,9 +325,11 @@ struct lv_volume
     std::vector<uint16_t> pins;
     uint32_t time_step = 0;
     bool streamed_last = false; /* the last synchronous frame streamed bricks */
-    /* pinned staging ring for callback sources */
+    /* pinned staging ring for callback sources: 2 * fetch_threads buffers
+     * (at least 4), one group fetching while the previous one copies */
     std::vector<lv::PinnedBuffer*> staging;
     std::vector<cudaEvent_t> staging_ev;
+    uint32_t fetch_threads = 1; /* > 1: get_data is called concurrently */
     ~lv_volume()
     {
         for (auto* p : staging)

@@ -23,7 +23,10 @@
 #include <cmath>
 #include <list>
 #include <map>
+#include <functional>
+#include <thread>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "lv_runtime.h"
@@ -259,9 +262,23 @@ lv_status apply_updates(
     return LV_OK;
 }
 
+/* The context's host fetchers: one worker per hardware thread but the
+ * caller's, at most 63 (created on first use, under the context lock). */
+HostPool* host_pool(lv_ctx* ctx)
+{
+    if (!ctx->host_pool)
+    {
+        const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+        ctx->host_pool = new HostPool(std::min(hw, 64u) - 1u);
+    }
+    return ctx->host_pool;
+}
+
 /* Streams bricks `ids` of `vol` into the pool (DataUploadFilter::load):
  * allocate / evict, fetch from the source, copy on the upload stream, then
- * publish the node-table entries; `render` waits for all of it. */
+ * publish the node-table entries; `render` waits for all of it. Callback
+ * sources are fetched in groups of half the staging ring, by up to
+ * fetch_threads host threads at once, while the previous group copies. */
 lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                         uint32_t n, uint32_t protect_frame, cudaStream_t render,
                         uint32_t& n_loaded, uint64_t& bytes_loaded)
@@ -280,60 +297,102 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>> updates;
     std::vector<uint64_t> gen_ids, gen_offsets;
     uint8_t* arena = P.arena.as<uint8_t>();
-    size_t ring = 0;
     lv_status st = LV_OK;
-    for (uint32_t i = 0; i < n; ++i)
-    {
-        const uint64_t id = ids[i];
-        if (nid_level(id) >= vol->info.depth)
-            continue;
-        const uint64_t idx = node_index(vol->level_offset, vol->info.root_blocks, id);
-        if (idx >= vol->n_nodes || vol->host_table[idx] >= 0)
-            continue;
-        uint32_t unit = 0;
-        if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit))
-        {
-            st = fail(ctx, LV_EAGAIN, "brick pool full of bricks in use");
-            break;
-        }
-        uint8_t* dst = arena + uint64_t(unit) * kSlotUnit;
-        if (vol->kind == SRC_BLOB_HOST)
-        {
-            const uint8_t* src = vol->host_store.as<uint8_t>() + idx * vol->brick_bytes;
-            LV_CUDA(ctx, cudaMemcpyAsync(dst, src, vol->brick_bytes,
-                                         cudaMemcpyHostToDevice, up));
-            bytes_loaded += vol->brick_bytes;
-        }
-        else if (vol->kind == SRC_BLOB_DEVICE || vol->kind == SRC_FBM_DEVICE)
-        {
-            gen_ids.push_back(id);
-            gen_offsets.push_back(uint64_t(unit) * kSlotUnit);
-        }
-        else
-        {
-            PinnedBuffer* buf = vol->staging[ring];
-            LV_CUDA(ctx, cudaEventSynchronize(vol->staging_ev[ring]));
-            const int rc = vol->fn(vol->user, id, buf->ptr, vol->brick_bytes);
-            if (rc != 0)
-            {
-                /* null MemoryUnitPtr: the brick is skipped
-                 * (DataUploadFilter.cpp:56-64); give the slot back */
-                P.free_by_units[vol->slot_units].push_back(unit);
-                continue;
-            }
-            LV_CUDA(ctx, cudaMemcpyAsync(dst, buf->ptr, vol->brick_bytes,
-                                         cudaMemcpyHostToDevice, up));
-            LV_CUDA(ctx, cudaEventRecord(vol->staging_ev[ring], up));
-            ring = (ring + 1) % vol->staging.size();
-            bytes_loaded += vol->brick_bytes;
-        }
+    /* the bookkeeping of a brick placed in `unit` */
+    const auto place = [&](uint64_t idx, uint32_t unit) {
         vol->host_table[idx] = int32_t(unit);
         updates.push_back({vol, {idx, int32_t(unit)}});
         P.lru.push_back(Resident{vol, idx, unit, vol->slot_units});
         P.resident_bytes += uint64_t(vol->slot_units) * kSlotUnit;
         ++P.resident_count[vol->slot_units];
         ++n_loaded;
+    };
+    if (vol->kind == SRC_CALLBACK)
+    {
+        /* first occurrences of the bricks that are not resident */
+        std::vector<std::pair<uint64_t, uint64_t>> todo; /* (id, table index) */
+        std::unordered_set<uint64_t> seen;
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            if (nid_level(ids[i]) >= vol->info.depth)
+                continue;
+            const uint64_t idx = node_index(vol->level_offset, vol->info.root_blocks, ids[i]);
+            if (idx < vol->n_nodes && vol->host_table[idx] < 0 && seen.insert(idx).second)
+                todo.push_back({ids[i], idx});
+        }
+        const size_t ring_n = vol->staging.size();
+        const size_t group = std::max<size_t>(1, ring_n / 2);
+        const uint32_t threads = std::max(1u, vol->fetch_threads);
+        HostPool* pool = threads > 1 ? host_pool(ctx) : nullptr;
+        std::vector<int> rc(group);
+        size_t ring = 0;
+        for (size_t g0 = 0; g0 < todo.size() && st == LV_OK; g0 += group)
+        {
+            const size_t m = std::min(group, todo.size() - g0);
+            /* these staging buffers are free once their last copies ended */
+            for (size_t j = 0; j < m; ++j)
+                LV_CUDA(ctx, cudaEventSynchronize(vol->staging_ev[(ring + j) % ring_n]));
+            const std::function<void(uint32_t)> fetch = [&](uint32_t j) {
+                rc[j] = vol->fn(vol->user, todo[g0 + j].first,
+                                vol->staging[(ring + j) % ring_n]->ptr, vol->brick_bytes);
+            };
+            if (pool)
+                pool->parallel_for(uint32_t(m), threads, fetch);
+            else
+                for (uint32_t j = 0; j < uint32_t(m); ++j)
+                    fetch(j);
+            for (size_t j = 0; j < m; ++j)
+            {
+                /* null MemoryUnitPtr: the brick is skipped
+                 * (DataUploadFilter.cpp:56-64) */
+                if (rc[j] != 0)
+                    continue;
+                uint32_t unit = 0;
+                if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit))
+                {
+                    st = fail(ctx, LV_EAGAIN, "brick pool full of bricks in use");
+                    break;
+                }
+                const size_t slot = (ring + j) % ring_n;
+                LV_CUDA(ctx, cudaMemcpyAsync(arena + uint64_t(unit) * kSlotUnit,
+                                             vol->staging[slot]->ptr, vol->brick_bytes,
+                                             cudaMemcpyHostToDevice, up));
+                LV_CUDA(ctx, cudaEventRecord(vol->staging_ev[slot], up));
+                bytes_loaded += vol->brick_bytes;
+                place(todo[g0 + j].second, unit);
+            }
+            ring = (ring + m) % ring_n;
+        }
     }
+    else
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            const uint64_t id = ids[i];
+            if (nid_level(id) >= vol->info.depth)
+                continue;
+            const uint64_t idx = node_index(vol->level_offset, vol->info.root_blocks, id);
+            if (idx >= vol->n_nodes || vol->host_table[idx] >= 0)
+                continue;
+            uint32_t unit = 0;
+            if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit))
+            {
+                st = fail(ctx, LV_EAGAIN, "brick pool full of bricks in use");
+                break;
+            }
+            if (vol->kind == SRC_BLOB_HOST)
+            {
+                const uint8_t* src = vol->host_store.as<uint8_t>() + idx * vol->brick_bytes;
+                LV_CUDA(ctx, cudaMemcpyAsync(arena + uint64_t(unit) * kSlotUnit, src,
+                                             vol->brick_bytes, cudaMemcpyHostToDevice, up));
+                bytes_loaded += vol->brick_bytes;
+            }
+            else /* generated on the device below */
+            {
+                gen_ids.push_back(id);
+                gen_offsets.push_back(uint64_t(unit) * kSlotUnit);
+            }
+            place(idx, unit);
+        }
     if (!gen_ids.empty())
     {
         DeviceBuffer dids;
@@ -578,6 +637,7 @@ extern "C" void lv_ctx_destroy(lv_ctx* ctx)
         delete ctx->renderer;
     }
     delete ctx->pool;
+    delete ctx->host_pool;
     if (ctx->upload_stream)
         cudaStreamDestroy(ctx->upload_stream);
     delete ctx;
@@ -634,6 +694,56 @@ extern "C" lv_status lv_pool_purge(lv_ctx* ctx)
     return LV_OK;
 }
 
+namespace
+{
+/* At least `count` pinned staging buffers of one brick each. */
+lv_status grow_staging(lv_ctx* ctx, lv_volume* v, size_t count)
+{
+    while (v->staging.size() < count)
+    {
+        PinnedBuffer* b = new PinnedBuffer();
+        if (b->reserve(v->brick_bytes) != cudaSuccess)
+        {
+            delete b;
+            return fail(ctx, LV_ENOMEM, "pinned staging allocation");
+        }
+        cudaEvent_t e;
+        LV_CUDA(ctx, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        v->staging.push_back(b);
+        v->staging_ev.push_back(e);
+    }
+    return LV_OK;
+}
+} // namespace
+
+extern "C" lv_status lv_volume_set_fetch_threads(lv_volume* v, uint32_t threads)
+{
+    if (!v)
+        return LV_EINVAL;
+    lv_ctx* ctx = v->ctx;
+    if (v->kind != SRC_CALLBACK)
+        return fail(ctx, LV_EINVAL, "only callback sources are fetched on the host");
+    if (threads == 0)
+        threads = std::min(64u, std::max(1u, std::thread::hardware_concurrency()));
+    if (threads > 64)
+        return fail(ctx, LV_EINVAL, "at most 64 fetch threads");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    const lv_status st = grow_staging(ctx, v, std::max<size_t>(4, 2 * size_t(threads)));
+    if (st != LV_OK)
+        return st;
+    v->fetch_threads = threads;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_volume_get_fetch_threads(const lv_volume* v, uint32_t* threads)
+{
+    if (!v || !threads)
+        return LV_EINVAL;
+    *threads = v->fetch_threads;
+    return LV_OK;
+}
+
 extern "C" lv_status lv_volume_create(lv_ctx* ctx, const lv_volume_info* info,
                                       lv_get_data_fn get_data, void* user,
                                       lv_volume** out)
@@ -650,21 +760,7 @@ extern "C" lv_status lv_volume_create(lv_ctx* ctx, const lv_volume_info* info,
     v->user = user;
     lv_status st = volume_init(ctx, v);
     if (st == LV_OK)
-    {
-        for (int i = 0; i < 4; ++i)
-        {
-            PinnedBuffer* b = new PinnedBuffer();
-            v->staging.push_back(b);
-            cudaEvent_t e;
-            cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
-            v->staging_ev.push_back(e);
-            if (b->reserve(v->brick_bytes) != cudaSuccess)
-            {
-                st = fail(ctx, LV_ENOMEM, "pinned staging allocation");
-                break;
-            }
-        }
-    }
+        st = grow_staging(ctx, v, 4);
     if (st != LV_OK)
     {
         delete v;
