@@ -483,26 +483,41 @@ def gb300_arm(args, cfg):
     def frame_of(i):
         return my_frames[i % len(my_frames)]
 
-    # ---- e2e: cold pool, bricks streamed from the host store, RGBA8 back
+    # ---- e2e: cold pool, bricks streamed from the host store, RGBA8 back.
+    # Each frame's RGBA8 copy to the host runs on a copy stream while the
+    # next frame renders (two RGBA8 buffers); the clock stops once the last
+    # copy has landed.
     for i in range(args.warmup):
         ctx.render(vol, tf, descs[frame_of(i)], out)
         ctx.last_stats()
     ctx.purge()
+    copy_stream = torch.cuda.Stream(dev)
+    out8s = [out8, torch.empty_like(out8)]
+    host8s = [host8, torch.empty_like(host8).pin_memory()]
+    copied = [None, None]
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    e2e_t, h2d, launches_e2e = [], 0, 0
+    h2d, launches_e2e = 0, 0
+    t1 = time.perf_counter()
     for i in range(args.steps):
-        t1 = time.perf_counter()
+        b = i & 1
+        if copied[b] is not None:
+            copied[b].synchronize()  # the copy of frame i - 2 has landed
         ctx.render(vol, tf, descs[frame_of(i)], out)
-        ctx.to_rgba8(out, out8)
-        host8.copy_(out8, non_blocking=True)
-        stream.synchronize()
-        e2e_t.append(time.perf_counter() - t1)
         st = ctx.last_stats()
+        ctx.to_rgba8(out, out8s[b])
+        ready = torch.cuda.Event()
+        ready.record(stream)
+        copy_stream.wait_event(ready)
+        with torch.cuda.stream(copy_stream):
+            host8s[b].copy_(out8s[b], non_blocking=True)
+            copied[b] = torch.cuda.Event()
+            copied[b].record(copy_stream)
         h2d += st["bytes_uploaded"]
         launches_e2e += st["n_launches"] + 1
-    e2e_total = sum(e2e_t)
+    copy_stream.synchronize()
+    e2e_total = time.perf_counter() - t1
 
     # ---- value: every brick of the orbit resident, L2 flushed between frames
     for k in my_frames:
@@ -571,7 +586,8 @@ def gb300_arm(args, cfg):
                 "h2d_bytes_per_step": int(h2d / args.steps),
                 "d2h_bytes_per_step": W * H * 4,
                 "note": "pool purged before the timed steps; bricks streamed from pinned host "
-                        "memory; RGBA8 frame copied to host every step"},
+                        "memory; RGBA8 frame copied to host every step on a copy stream "
+                        "overlapping the next frame; wall clock over all steps"},
         "e2e_gpu_launches": launches_e2e,
         "clocks": clocks.summary(),
         "visible_bricks_mean": float(np.mean([s["n_visible"] for s in stats])),

@@ -504,8 +504,9 @@ struct RayState
     float dir[3];
     float tg, thi;
     float kf;            /* index of the next sample (exact in FP32 below 2^24) */
+    float kf_safe;       /* samples up to this index stay in the current brick */
     float4 dst;
-    uint32_t cur, entry; /* leaf cell of the last sample and its entry */
+    uint32_t entry;      /* leaf entry of the current brick (or empty cell) */
     const uint8_t* brick;
     float vs[3], off[3];
 };
@@ -529,19 +530,115 @@ __device__ __forceinline__ bool ray_begin(const RayGeom& g, float step, RayState
     }
     r.tg = g.tg;
     r.thi = g.thi;
-    r.cur = 0xFFFFFFFFu;
+    r.kf_safe = -1.0f;
     r.entry = kLeafEmpty;
     r.brick = nullptr;
     return true;
 }
 
+/* Sample position in leaf-cell units at ray parameter t: single-rounding
+ * FMAs in a fixed order (the CPU oracle evaluates the same fmaf chain). */
+__device__ __forceinline__ void sample_cell_coord(const RayView& V, const RayState& r, float t,
+                                                  float f[3])
+{
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        f[a] = fmaf(fmaf(r.dir[a], t, V.eye[a]), V.gscale[a], V.goff[a]);
+}
+
+/* The slow path of a sample (index r.kf, position f) that leaves the range
+ * known to lie in the current brick: finds its leaf cell (floor(f) in one
+ * conversion; 0 <= c < dims one unsigned compare, f is finite), the brick
+ * there, and how far the ray stays in that brick. False: the sample is
+ * outside the octree.
+ *
+ * The cell of a sample is monotone in its index along each axis (t, the
+ * position and f are monotone single-rounding functions of it, and floor is
+ * monotone), so if the sample at index k lies in the brick's cube of leaf
+ * cells, so does every sample between this one and k. k is the estimated
+ * last sample before the exit (or the one before it), checked with the
+ * exact per-sample arithmetic; samples up to r.kf_safe then skip the lookup
+ * and take the same brick the per-sample lookup would. */
+template <int FILTER>
+__device__ __forceinline__ bool locate(const RayView& V, RayState& r, float step, const float f[3])
+{
+    uint32_t c[3];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        c[a] = uint32_t(__float2int_rd(f[a]));
+        inside = inside && c[a] < V.dims[a];
+    }
+    r.kf_safe = r.kf; /* this sample only, unless shown otherwise below */
+    if (!inside)
+        return false;
+    uint32_t entry = __ldg(V.leaf + (c[2] * V.dims[1] + c[1]) * V.dims[0] + c[0]);
+    if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
+                                (entry >> kLeafSlotBits) > V.Lf))
+    {
+        atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
+        entry = kLeafEmpty;
+    }
+    r.entry = entry;
+    /* an empty cell spans one leaf cell; a brick at level L spans 2^(Lf-L) */
+    const uint32_t sh = entry == kLeafEmpty ? 0u : V.Lf - (entry >> kLeafSlotBits);
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        c[a] >>= sh; /* the brick's cube, in its own cells */
+    if (entry != kLeafEmpty)
+    {
+        const float half_texel = FILTER == LV_FILTER_TRILINEAR ? 0.5f : 0.0f;
+        r.brick = V.pool + uint64_t(entry & kLeafSlotMask) * kSlotUnit;
+        const float inv_side = __int_as_float(int(127u - sh) << 23); /* 2^-sh */
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            r.vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
+            r.off[a] = (__uint2float_rn(V.O[a]) - __uint2float_rn(c[a] * V.B[a])) -
+                       half_texel; /* exact */
+        }
+    }
+    /* estimated parameter where the ray leaves the cube */
+    float tx = 3.0e38f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+    {
+        const float d = r.dir[a];
+        if (d != 0.0f)
+        {
+            const uint32_t bound = d > 0.0f ? min((c[a] + 1u) << sh, V.dims[a]) : c[a] << sh;
+            tx = fminf(tx, __fdividef(__fdividef(__uint2float_rn(bound) - V.goff[a],
+                                                 V.gscale[a]) -
+                                          V.eye[a],
+                                      d));
+        }
+    }
+    float ke = fminf(floorf(__fdividef(tx - r.tg, step)), 16777215.0f);
+#pragma unroll 1
+    for (int attempt = 0; attempt < 2 && ke > r.kf; ++attempt, ke -= 1.0f)
+    {
+        float g[3];
+        sample_cell_coord(V, r, fmaf(ke, step, r.tg), g);
+        bool in = true;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+        {
+            const uint32_t ca = uint32_t(__float2int_rd(g[a]));
+            in = in && ca < V.dims[a] && (ca >> sh) == c[a];
+        }
+        if (in)
+        {
+            r.kf_safe = ke;
+            break;
+        }
+    }
+    return true;
+}
+
 /* Advances the ray to its next sample. Returns 0 once the ray has left its
  * segment, 1 for a sample without data (outside the octree or no brick
- * rendered there), 2 with the sample's voxels in T. Position, cell and slot
- * coordinate are single-rounding FMAs in a fixed order (the CPU oracle
- * evaluates the same fmaf chain); the cell is floor(f) in one conversion and
- * 0 <= c < dims one unsigned compare (f is finite: a ray with a non-finite
- * direction or bounds has no samples). */
+ * rendered there), 2 with the sample's voxels in T. */
 template <int DT, int FILTER, int EDGE>
 __device__ __forceinline__ int fetch_sample(const RayView& V, RayState& r, float step,
                                             Taps<FILTER>& T)
@@ -549,51 +646,15 @@ __device__ __forceinline__ int fetch_sample(const RayView& V, RayState& r, float
     const float t = fmaf(r.kf, step, r.tg);
     if (!(t < r.thi))
         return 0;
-    r.kf += 1.0f;
     float f[3];
-    int c[3];
-    bool inside = true;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
+    sample_cell_coord(V, r, t, f);
+    const bool known = r.kf <= r.kf_safe;
+    if (!known && !locate<FILTER>(V, r, step, f))
     {
-        const float p = fmaf(r.dir[a], t, V.eye[a]);
-        f[a] = fmaf(p, V.gscale[a], V.goff[a]);
-        c[a] = __float2int_rd(f[a]);
-        inside = inside && uint32_t(c[a]) < V.dims[a];
-    }
-    if (!inside)
+        r.kf += 1.0f;
         return 1;
-    const uint32_t lin =
-        (uint32_t(c[2]) * V.dims[1] + uint32_t(c[1])) * V.dims[0] + uint32_t(c[0]);
-    if (lin != r.cur)
-    {
-        r.cur = lin;
-        uint32_t entry = __ldg(V.leaf + lin);
-        if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
-                                    (entry >> kLeafSlotBits) > V.Lf))
-        {
-            atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
-            entry = kLeafEmpty;
-        }
-        r.entry = entry;
-        if (entry != kLeafEmpty)
-        {
-            const float half_texel = FILTER == LV_FILTER_TRILINEAR ? 0.5f : 0.0f;
-            const uint32_t L = entry >> kLeafSlotBits;
-            const uint32_t slot = entry & kLeafSlotMask;
-            const uint32_t sh = V.Lf - L;
-            r.brick = V.pool + uint64_t(slot) * kSlotUnit;
-            const float inv_side = __int_as_float(int(127u - sh) << 23); /* 2^-sh */
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-            {
-                r.vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
-                r.off[a] = (__uint2float_rn(V.O[a]) -
-                            __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a])) -
-                           half_texel; /* exact */
-            }
-        }
     }
+    r.kf += 1.0f;
     if (r.entry == kLeafEmpty)
         return 1;
     float sc[3];
@@ -634,51 +695,14 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     const float t = fmaf(r.kf, step, r.tg);
     if (!(t < r.thi))
         return false;
-    r.kf += 1.0f;
     float f[3];
-    int c[3];
-    bool inside = true;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
+    sample_cell_coord(V, r, t, f);
+    if (!(r.kf <= r.kf_safe) && !locate<FILTER>(V, r, step, f))
     {
-        const float p = fmaf(r.dir[a], t, V.eye[a]);
-        f[a] = fmaf(p, V.gscale[a], V.goff[a]);
-        c[a] = __float2int_rd(f[a]);
-        inside = inside && uint32_t(c[a]) < V.dims[a];
-    }
-    if (!inside)
+        r.kf += 1.0f;
         return true;
-    const uint32_t lin =
-        (uint32_t(c[2]) * V.dims[1] + uint32_t(c[1])) * V.dims[0] + uint32_t(c[0]);
-    if (lin != r.cur)
-    {
-        r.cur = lin;
-        uint32_t entry = __ldg(V.leaf + lin);
-        if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
-                                    (entry >> kLeafSlotBits) > V.Lf))
-        {
-            atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
-            entry = kLeafEmpty;
-        }
-        r.entry = entry;
-        if (entry != kLeafEmpty)
-        {
-            const float half_texel = FILTER == LV_FILTER_TRILINEAR ? 0.5f : 0.0f;
-            const uint32_t L = entry >> kLeafSlotBits;
-            const uint32_t slot = entry & kLeafSlotMask;
-            const uint32_t sh = V.Lf - L;
-            r.brick = V.pool + uint64_t(slot) * kSlotUnit;
-            const float inv_side = __int_as_float(int(127u - sh) << 23); /* 2^-sh */
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-            {
-                r.vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
-                r.off[a] = (__uint2float_rn(V.O[a]) -
-                            __uint2float_rn((uint32_t(c[a]) >> sh) * V.B[a])) -
-                           half_texel; /* exact */
-            }
-        }
     }
+    r.kf += 1.0f;
     if (r.entry == kLeafEmpty)
         return true;
     float sc[3];
