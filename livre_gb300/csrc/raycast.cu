@@ -508,7 +508,10 @@ struct RayState
     float4 dst;
     uint32_t entry;      /* leaf entry of the current brick (or empty cell) */
     const uint8_t* brick;
-    float vs[3], off[3];
+    /* slot coordinate of a sample of the brick: sc = fma(t, sa, sb), the
+     * composition of the position, cell and slot maps (a few ulp from the
+     * oracle's three-FMA chain; which brick a sample reads is exact) */
+    float sa[3], sb[3];
 };
 
 /* First sample on the global grid at or after tlo; false: no sample. */
@@ -525,8 +528,8 @@ __device__ __forceinline__ bool ray_begin(const RayGeom& g, float step, RayState
     for (int a = 0; a < 3; ++a)
     {
         r.dir[a] = g.dir[a];
-        r.vs[a] = 0.f;
-        r.off[a] = 0.f;
+        r.sa[a] = 0.f;
+        r.sb[a] = 0.f;
     }
     r.tg = g.tg;
     r.thi = g.thi;
@@ -594,9 +597,13 @@ __device__ __forceinline__ bool locate(const RayView& V, RayState& r, float step
 #pragma unroll
         for (int a = 0; a < 3; ++a)
         {
-            r.vs[a] = __uint2float_rn(V.B[a]) * inv_side; /* exact */
-            r.off[a] = (__uint2float_rn(V.O[a]) - __uint2float_rn(c[a] * V.B[a])) -
-                       half_texel; /* exact */
+            /* slot coordinate = f * vs + off (vs, off exact); composed with
+             * f = (eye + dir * t) * gscale + goff into one map of t */
+            const float vs = __uint2float_rn(V.B[a]) * inv_side;
+            const float off =
+                (__uint2float_rn(V.O[a]) - __uint2float_rn(c[a] * V.B[a])) - half_texel;
+            r.sa[a] = r.dir[a] * V.gscale[a] * vs;
+            r.sb[a] = fmaf(fmaf(V.eye[a], V.gscale[a], V.goff[a]), vs, off);
         }
     }
     /* estimated parameter where the ray leaves the cube */
@@ -646,13 +653,15 @@ __device__ __forceinline__ int fetch_sample(const RayView& V, RayState& r, float
     const float t = fmaf(r.kf, step, r.tg);
     if (!(t < r.thi))
         return 0;
-    float f[3];
-    sample_cell_coord(V, r, t, f);
-    const bool known = r.kf <= r.kf_safe;
-    if (!known && !locate<FILTER>(V, r, step, f))
+    if (!(r.kf <= r.kf_safe))
     {
-        r.kf += 1.0f;
-        return 1;
+        float f[3];
+        sample_cell_coord(V, r, t, f);
+        if (!locate<FILTER>(V, r, step, f))
+        {
+            r.kf += 1.0f;
+            return 1;
+        }
     }
     r.kf += 1.0f;
     if (r.entry == kLeafEmpty)
@@ -660,7 +669,7 @@ __device__ __forceinline__ int fetch_sample(const RayView& V, RayState& r, float
     float sc[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-        sc[a] = fmaf(f[a], r.vs[a], r.off[a]);
+        sc[a] = fmaf(t, r.sa[a], r.sb[a]);
     load_taps<DT, FILTER, EDGE>(V, r.brick, sc, T);
     return 2;
 }
@@ -695,12 +704,15 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     const float t = fmaf(r.kf, step, r.tg);
     if (!(t < r.thi))
         return false;
-    float f[3];
-    sample_cell_coord(V, r, t, f);
-    if (!(r.kf <= r.kf_safe) && !locate<FILTER>(V, r, step, f))
+    if (!(r.kf <= r.kf_safe))
     {
-        r.kf += 1.0f;
-        return true;
+        float f[3];
+        sample_cell_coord(V, r, t, f);
+        if (!locate<FILTER>(V, r, step, f))
+        {
+            r.kf += 1.0f;
+            return true;
+        }
     }
     r.kf += 1.0f;
     if (r.entry == kLeafEmpty)
@@ -708,7 +720,7 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     float sc[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
-        sc[a] = fmaf(f[a], r.vs[a], r.off[a]);
+        sc[a] = fmaf(t, r.sa[a], r.sb[a]);
     Taps<FILTER> T;
     load_taps<DT, FILTER, EDGE>(V, r.brick, sc, T);
     const float4 src = tf_lookup<TFS>(V, interp<FILTER>(T));
