@@ -407,14 +407,14 @@ lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
  * LV_ORDER_LONGEST_FIRST first estimates each tile's cost by the length of
  * its centre ray inside the volume and starts the longest tiles first, so
  * the frame does not end waiting on a few long rays started late.
- * lookahead (grid and tile queue): 1 loads the voxels of a ray's next sample
- * before compositing the current one (shorter latency per ray, more
+ * lookahead (all kinds but warp refill): 1 loads the voxels of a ray's next
+ * sample before compositing the current one (shorter latency per ray, more
  * registers per thread); 0 does not.
- * Default: {LV_LAUNCH_TILE_GRID, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 0}, the
- * fastest on a 2048^3 volume at 1920x1080 (0.46 ms per frame against 0.47 ms
- * for the 8 x 16 grid in raster order and 0.43-0.53 ms for the persistent
- * queue, whose time varies from run to run), and the friendliest to other
- * work on the device.
+ * Default: {LV_LAUNCH_TILE_GRID, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 1}, the
+ * fastest on a 2048^3 volume at 1920x1080: 0.356 ms of ray cast per frame,
+ * against 0.368 ms without look-ahead, 0.43 ms in raster order, 0.43 ms for
+ * warp tiles and 0.45 ms for the persistent tile queue; and the friendliest
+ * to other work on the device.
  * No reference counterpart (the reference rasterises one brick at a time,
  * RayCastRenderer.cpp:503-571). */
 enum
@@ -499,6 +499,9 @@ typedef struct lv_batch_config
     uint32_t order;          /* LV_ORDER_* (CTA tiles): longest first ranks the
                                 (view, tile) items of all views by the
                                 estimated samples of their centre ray */
+    uint32_t lookahead;      /* view kernels: 1 = one-sample look-ahead (the
+                                voxels of the next sample load while the
+                                current one composites), as lv_render_launch */
 } lv_batch_config;
 
 /* A batch renderer on ctx (its own stream, graphs and per-view buffers).

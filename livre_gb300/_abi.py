@@ -86,7 +86,8 @@ QUEUE_VIEW_KERNELS = 2
 class BatchConfig(C.Structure):
     _fields_ = [("tile_w", C.c_uint32), ("tile_h", C.c_uint32), ("ctas_per_sm", C.c_uint32),
                 ("tf_shared", C.c_uint32), ("use_graph", C.c_uint32), ("queue", C.c_uint32),
-                ("samples_per_check", C.c_uint32), ("order", C.c_uint32)]
+                ("samples_per_check", C.c_uint32), ("order", C.c_uint32),
+                ("lookahead", C.c_uint32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

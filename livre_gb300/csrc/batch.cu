@@ -56,7 +56,7 @@ struct lv_batch
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr, user_ready = nullptr;
     cudaEvent_t t_sel0 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
-    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_VIEW_KERNELS, 8, LV_ORDER_LONGEST_FIRST};
+    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_VIEW_KERNELS, 8, LV_ORDER_LONGEST_FIRST, 1};
     /* per-group longest-first order: hist (128 words) | keys | order, each
      * group at a fixed offset sized for order_cap items (grow-only) */
     lv::DeviceBuffer order_buf;
@@ -458,7 +458,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         /* lv_render's ray cast per view, views spread over the aux streams */
         const RayView* h_rays = reinterpret_cast<const RayView*>(b->h_params.as<uint8_t>() + PL.ray);
         const lv_render_launch L{LV_LAUNCH_TILE_GRID, b->cfg.tile_w, b->cfg.tile_h, 0,
-                                 b->cfg.order, 0};
+                                 b->cfg.order, b->cfg.lookahead};
         std::vector<uint64_t> offs(n + 1, 0);
         for (uint32_t i = 0; i < n; ++i)
             offs[i + 1] = offs[i] + ((tile_order_bytes(h_rays[i], L) + 255) & ~size_t(255));
@@ -682,6 +682,8 @@ extern "C" lv_status lv_batch_set_config(lv_batch* b, const lv_batch_config* cfg
         return fail(b->ctx, LV_EINVAL, "unknown queue kind");
     if (cfg->order != LV_ORDER_RASTER && cfg->order != LV_ORDER_LONGEST_FIRST)
         return fail(b->ctx, LV_EINVAL, "unknown tile order");
+    if (cfg->lookahead > 1 || (cfg->lookahead && cfg->queue != LV_QUEUE_VIEW_KERNELS))
+        return fail(b->ctx, LV_EINVAL, "look-ahead 0 or 1, view kernels only");
     std::lock_guard<std::mutex> lock(b->ctx->mutex);
     b->cfg = *cfg;
     return LV_OK;
@@ -886,8 +888,9 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
 {
     if (!b || !views || n == 0)
         return LV_EINVAL;
-    /* CTA tiles: 6 tile shapes x TF staging, resident grid; warp refill:
-     * 4 tile sizes x 3 refill intervals */
+    /* CTA tiles: 6 tile shapes x TF staging x order, resident grid; view
+     * kernels: 2 tile shapes x order x look-ahead; warp refill: 4 tile sizes
+     * x 3 refill intervals */
     static const uint32_t cta_shapes[][2] = {{8, 8}, {16, 8}, {8, 16}, {16, 16}, {32, 4}, {32, 8}};
     static const uint32_t warp_shapes[][2] = {{8, 4}, {8, 8}, {16, 8}, {16, 16}};
     static const uint32_t checks[] = {2, 8, 32};
@@ -905,22 +908,25 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
                 c.tf_shared = tfs;
                 c.samples_per_check = 8;
                 c.order = ord;
+                c.lookahead = 0;
                 cands.push_back(c);
             }
     static const uint32_t view_shapes[][2] = {{8, 8}, {8, 16}};
     for (const auto& sh : view_shapes)
         for (uint32_t ord = 0; ord < 2; ++ord)
-        {
-            lv_batch_config c = start;
-            c.queue = LV_QUEUE_VIEW_KERNELS;
-            c.tile_w = sh[0];
-            c.tile_h = sh[1];
-            c.ctas_per_sm = 0;
-            c.tf_shared = 0;
-            c.samples_per_check = 8;
-            c.order = ord;
-            cands.push_back(c);
-        }
+            for (uint32_t la = 0; la < 2; ++la)
+            {
+                lv_batch_config c = start;
+                c.queue = LV_QUEUE_VIEW_KERNELS;
+                c.tile_w = sh[0];
+                c.tile_h = sh[1];
+                c.ctas_per_sm = 0;
+                c.tf_shared = 0;
+                c.samples_per_check = 8;
+                c.order = ord;
+                c.lookahead = la;
+                cands.push_back(c);
+            }
     for (const auto& sh : warp_shapes)
         for (uint32_t k : checks)
         {
@@ -932,6 +938,7 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
             c.tf_shared = 0;
             c.samples_per_check = k;
             c.order = LV_ORDER_RASTER;
+            c.lookahead = 0;
             cands.push_back(c);
         }
     lv_batch_config best = start;

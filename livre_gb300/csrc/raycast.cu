@@ -1606,10 +1606,10 @@ lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launc
     return LV_OK;
 }
 
-/* The default launch (one CTA per tile, no look-ahead) for bricks of NX x NX
- * voxels in x and y, the pitches as immediates: 34, 66 and 130 are the
- * 32^3, 64^3 and 128^3 bricks with an overlap of 1. */
-template <int DT, int F, int NX>
+/* One CTA per tile for bricks of NX x NX voxels in x and y, the pitches as
+ * immediates: 34, 66 and 130 are the 32^3, 64^3 and 128^3 bricks with an
+ * overlap of 1. LA: one-sample look-ahead. */
+template <int DT, int F, int NX, int LA>
 lv_status tiles_nx_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                             cudaStream_t s, uint8_t* scratch)
 {
@@ -1622,8 +1622,8 @@ lv_status tiles_nx_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launc
     if (st != LV_OK)
         return st;
     const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
-    raycast_tiles_kernel<DT, F, NX, 0><<<tiles, L.tile_w * L.tile_h, 0, s>>>(V, L.tile_w,
-                                                                           L.tile_h, order);
+    raycast_tiles_kernel<DT, F, NX, LA><<<tiles, L.tile_w * L.tile_h, 0, s>>>(V, L.tile_w,
+                                                                            L.tile_h, order);
     LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;
 }
@@ -1633,14 +1633,15 @@ lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& 
                          cudaStream_t s, uint8_t* scratch)
 {
     if (EDGE == 0 && F == LV_FILTER_TRILINEAR && L.kind == LV_LAUNCH_TILE_GRID &&
-        !L.lookahead && V.N[0] == V.N[1])
+        V.N[0] == V.N[1] && (V.N[0] == 66 || V.N[0] == 34 || V.N[0] == 130))
     {
-        if (V.N[0] == 66)
-            return tiles_nx_dispatch<DT, F, 66>(ctx, V, L, s, scratch);
-        if (V.N[0] == 34)
-            return tiles_nx_dispatch<DT, F, 34>(ctx, V, L, s, scratch);
-        if (V.N[0] == 130)
-            return tiles_nx_dispatch<DT, F, 130>(ctx, V, L, s, scratch);
+        if (L.lookahead)
+            return V.N[0] == 66   ? tiles_nx_dispatch<DT, F, 66, 1>(ctx, V, L, s, scratch)
+                   : V.N[0] == 34 ? tiles_nx_dispatch<DT, F, 34, 1>(ctx, V, L, s, scratch)
+                                  : tiles_nx_dispatch<DT, F, 130, 1>(ctx, V, L, s, scratch);
+        return V.N[0] == 66   ? tiles_nx_dispatch<DT, F, 66, 0>(ctx, V, L, s, scratch)
+               : V.N[0] == 34 ? tiles_nx_dispatch<DT, F, 34, 0>(ctx, V, L, s, scratch)
+                              : tiles_nx_dispatch<DT, F, 130, 0>(ctx, V, L, s, scratch);
     }
     if (L.kind == LV_LAUNCH_WARP_REFILL)
         return refill_dispatch<DT, F, EDGE>(ctx, V, L, s);

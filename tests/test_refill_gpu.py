@@ -11,7 +11,7 @@ LAUNCHES = [(0, 8, 4, 0, 0, 0), (0, 16, 16, 0, 0, 1), (0, 32, 2, 0, 0, 0),
             (1, 8, 16, 0, 0, 1), (1, 16, 16, 0, 1, 0), (1, 8, 8, 0, 1, 1), (1, 32, 1, 0, 0, 0),
             (2, 8, 8, 8, 0, 0), (2, 8, 4, 1, 1, 0), (2, 16, 8, 2, 0, 0), (2, 16, 16, 32, 1, 0),
             (2, 32, 32, 64, 0, 0), (2, 32, 1, 5, 0, 0), (3, 8, 16, 0, 1, 0),
-            (3, 16, 16, 0, 0, 1), (3, 32, 1, 0, 1, 0)]
+            (3, 8, 16, 0, 1, 1), (3, 16, 16, 0, 0, 1), (3, 32, 1, 0, 1, 0), (4, 8, 4, 0, 1, 1)]
 
 
 def scenes(ctx, lv):
@@ -71,7 +71,7 @@ def test_render_launch_validation(gpu_ctx):
         with pytest.raises(lv.LivreError):
             gpu_ctx.set_render_launch(*bad)
     assert gpu_ctx.render_launch() == {"kind": 3, "tile_w": 8, "tile_h": 16,
-                                       "samples_per_check": 0, "order": 1, "lookahead": 0}
+                                       "samples_per_check": 0, "order": 1, "lookahead": 1}
 
 
 @pytest.mark.parametrize("cfg", [
@@ -83,6 +83,7 @@ def test_render_launch_validation(gpu_ctx):
     dict(queue=0, tile_w=8, tile_h=8, tf_shared=1, ctas_per_sm=3),
     dict(queue=0, tile_w=8, tile_h=16, tf_shared=1, order=0),
     dict(queue=2, tile_w=8, tile_h=16),
+    dict(queue=2, tile_w=8, tile_h=16, lookahead=0),
     dict(queue=2, tile_w=16, tile_h=16, order=0),
 ])
 def test_batch_queue_kinds_match_single_views(gpu_ctx, cfg):
