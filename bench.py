@@ -498,14 +498,13 @@ def gb300_arm(args, cfg):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    h2d, launches_e2e = 0, 0
+    tot0 = ctx.totals()
     t1 = time.perf_counter()
     for i in range(args.steps):
         b = i & 1
         if copied[b] is not None:
             copied[b].synchronize()  # the copy of frame i - 2 has landed
         ctx.render(vol, tf, descs[frame_of(i)], out)
-        st = ctx.last_stats()
         ctx.to_rgba8(out, out8s[b])
         ready = torch.cuda.Event()
         ready.record(stream)
@@ -514,10 +513,12 @@ def gb300_arm(args, cfg):
             host8s[b].copy_(out8s[b], non_blocking=True)
             copied[b] = torch.cuda.Event()
             copied[b].record(copy_stream)
-        h2d += st["bytes_uploaded"]
-        launches_e2e += st["n_launches"] + 1
     copy_stream.synchronize()
     e2e_total = time.perf_counter() - t1
+    tot1 = ctx.totals()
+    h2d = tot1["bytes_uploaded"] - tot0["bytes_uploaded"]
+    launches_e2e = tot1["launches"] - tot0["launches"] + args.steps  # + RGBA8 conversions
+    ctx.last_stats()  # raises if a frame reported a device error
 
     # ---- value: every brick of the orbit resident, L2 flushed between frames
     for k in my_frames:

@@ -447,6 +447,19 @@ typedef struct lv_render_launch
 lv_status lv_set_render_launch(lv_ctx* ctx, const lv_render_launch* cfg);
 lv_status lv_get_render_launch(lv_ctx* ctx, lv_render_launch* cfg);
 
+/* Running totals of lv_render on a context since its creation, kept on the
+ * host: reading them does not wait for the device (lv_last_stats does). A
+ * frame counts once lv_render has returned LV_OK; its bricks and bytes are
+ * the ones it streamed before its ray cast; launches as lv_frame_stats. */
+typedef struct lv_ctx_totals
+{
+    uint64_t frames;
+    uint64_t bricks_uploaded;
+    uint64_t bytes_uploaded;
+    uint64_t launches;
+} lv_ctx_totals;
+lv_status lv_get_totals(lv_ctx* ctx, lv_ctx_totals* out);
+
 /* Statistics of the last lv_render / lv_render_batch call (synchronises with
  * its stream). */
 lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out);

@@ -713,6 +713,13 @@ class Context:
         c = _abi.RenderLaunch(kind, tile_w, tile_h, samples_per_check, order, lookahead)
         check(lib().lv_set_render_launch(self.handle, C.byref(c)), self.handle)
 
+    def totals(self):
+        """Running totals of lv_render (frames, bricks and bytes streamed,
+        launches) without waiting for the device."""
+        t = _abi.CtxTotals()
+        check(lib().lv_get_totals(self.handle, C.byref(t)), self.handle)
+        return t.as_dict()
+
     def last_stats(self):
         s = _abi.FrameStats()
         check(lib().lv_last_stats(self.handle, C.byref(s)), self.handle)

@@ -73,6 +73,14 @@ class FrameStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class CtxTotals(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("bricks_uploaded", C.c_uint64),
+                ("bytes_uploaded", C.c_uint64), ("launches", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BatchView(C.Structure):
     _fields_ = [("volume", C.c_void_p), ("tf", C.c_void_p), ("desc", RenderDesc),
                 ("d_rgba", C.c_void_p)]
@@ -178,6 +186,7 @@ _SIGNATURES = {
     "lv_render": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, P(RenderDesc), C.c_void_p,
                             C.c_void_p]),
     "lv_last_stats": (C.c_int, [C.c_void_p, P(FrameStats)]),
+    "lv_get_totals": (C.c_int, [C.c_void_p, P(CtxTotals)]),
     "lv_batch_create": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
     "lv_batch_destroy": (None, [C.c_void_p]),
     "lv_batch_set_config": (C.c_int, [C.c_void_p, P(BatchConfig)]),

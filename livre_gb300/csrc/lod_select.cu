@@ -609,6 +609,11 @@ uint32_t fused_grid(lv_ctx* ctx)
 }
 } // namespace
 
+uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth)
+{
+    return n_views == 1 && fused_grid(ctx) ? 1u : depth + 2u;
+}
+
 lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                         uint32_t n_views, uint32_t max_depth,
                         cudaStream_t stream)

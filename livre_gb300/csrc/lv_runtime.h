@@ -124,6 +124,7 @@ struct lv_ctx
     lv_render_launch launch{LV_LAUNCH_TILE_GRID, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 1};
     /* host fetchers of callback sources (created on first use) */
     lv::HostPool* host_pool = nullptr;
+    lv_ctx_totals totals{}; /* since creation, host-side (lv_get_totals) */
     std::mutex mutex;
 };
 
@@ -162,6 +163,9 @@ lv_status make_lod_view(lv_ctx* ctx, const lv_volume_info& vol,
 lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                         uint32_t n_views, uint32_t max_depth,
                         cudaStream_t stream);
+
+/* Kernels run_selection launches for n views of an octree of `depth` levels. */
+uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth);
 
 /* Enqueues the selection kernels for n views whose constants are already
  * on the device (capturable: no host synchronisation). */
@@ -232,6 +236,10 @@ struct Renderer
     uint32_t pending_frame = 0;
     cudaEvent_t render_event = nullptr;
     cudaEvent_t upload_event = nullptr;
+    /* end of the last lv_render's work on its stream: lv_render returns
+     * before its ray cast ends, so the next frame (on any stream) and any
+     * brick streaming wait for it */
+    cudaEvent_t frame_done = nullptr;
     /* timing of the last frame: selection and ray cast */
     cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
     uint32_t launches = 0;
@@ -324,7 +332,6 @@ struct lv_volume
      * requests are never evicted (empty until a server uses the volume) */
     std::vector<uint16_t> pins;
     uint32_t time_step = 0;
-    bool streamed_last = false; /* the last synchronous frame streamed bricks */
     /* pinned staging ring for callback sources: 2 * fetch_threads buffers
      * (at least 4), one group fetching while the previous one copies */
     std::vector<lv::PinnedBuffer*> staging;

@@ -139,6 +139,7 @@ lv_status ensure_renderer(lv_ctx* ctx)
     cudaEventCreateWithFlags(&r->pending_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->render_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->upload_event, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->frame_done, cudaEventDisableTiming);
     cudaEventCreate(&r->t_sel0);
     cudaEventCreate(&r->t_sel1);
     cudaEventCreate(&r->t_ray0);
@@ -290,9 +291,12 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     bytes_loaded = 0;
     if (n == 0)
         return LV_OK;
-    /* new copies may overwrite evicted slots still read by queued work */
+    /* new copies may overwrite evicted slots still read by queued work: the
+     * caller's stream and the last lv_render frame (on any stream) */
     LV_CUDA(ctx, cudaEventRecord(R.render_event, render));
     LV_CUDA(ctx, cudaStreamWaitEvent(up, R.render_event, 0));
+    if (R.have_last)
+        LV_CUDA(ctx, cudaStreamWaitEvent(up, R.frame_done, 0));
     std::unordered_map<lv_volume*, std::vector<uint32_t>> stamps;
     std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>> updates;
     std::vector<uint64_t> gen_ids, gen_offsets;
@@ -630,6 +634,7 @@ extern "C" void lv_ctx_destroy(lv_ctx* ctx)
         cudaEventDestroy(ctx->renderer->pending_event);
         cudaEventDestroy(ctx->renderer->render_event);
         cudaEventDestroy(ctx->renderer->upload_event);
+        cudaEventDestroy(ctx->renderer->frame_done);
         cudaEventDestroy(ctx->renderer->t_sel0);
         cudaEventDestroy(ctx->renderer->t_sel1);
         cudaEventDestroy(ctx->renderer->t_ray0);
@@ -1090,6 +1095,10 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
 
     lv_frame_stats stats{};
     R.stats = stats;
+    /* the previous frame's buffers are reused: its work (maybe on another
+     * stream) comes first */
+    if (R.have_last)
+        LV_CUDA(ctx, cudaStreamWaitEvent(s, R.frame_done, 0));
     /* async: bricks missed by the previous frame are streamed now */
     if (!desc->synchronous)
     {
@@ -1147,14 +1156,15 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     LV.out_ids = R.visible.as<uint64_t>();
     LV.capacity = uint32_t(std::min<uint64_t>(R.visible_capacity, 0xFFFFFFFFu));
     LV.result = R.sel_result.as<uint32_t>();
-    /* kernels: roots + one per level + finish, resolve, prune (asynchronous
-     * mode only), leaf fill, ray cast (+ tile keys and order when longest
-     * first); the last three to six again on a synchronous miss */
+    /* kernels: the selection (one cooperative launch, or roots + one per
+     * level + finish), resolve, prune (asynchronous mode only), leaf fill,
+     * ray cast (+ tile keys and order when longest first); a synchronous
+     * frame that streams misses resolves once more */
     const lv_render_launch& RL = ctx->launch;
     const uint32_t tail_launches =
         3u + (desc->synchronous ? 0u : 1u) +
         (RL.kind != LV_LAUNCH_GRID && RL.order == LV_ORDER_LONGEST_FIRST ? 2u : 0u);
-    R.launches = info.depth + 2u + tail_launches;
+    R.launches = selection_launches(ctx, 1, info.depth) + tail_launches;
     LV_CUDA(ctx, cudaEventRecord(R.t_sel0, s));
     st = run_selection(ctx, &LV, 1, info.depth, s);
     if (st != LV_OK)
@@ -1200,9 +1210,10 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                        R.counters.as<uint32_t>(), V);
     if (st != LV_OK)
         return st;
-    /* residency pass, leaf grid and ray cast, enqueued without a host round
-     * trip; the synchronous mode checks for misses once the frame is done
-     * and, only if some brick was missing, streams it and renders again */
+    /* residency pass, leaf grid and ray cast. The synchronous mode reads the
+     * residency pass's miss count back before the rest (one host round trip
+     * early in the frame), streams the misses, and returns without waiting
+     * for the ray cast. */
     auto timed_stream = [&](const uint64_t* ids, uint32_t n, uint32_t protect,
                             uint32_t& loaded, uint64_t& bytes) -> lv_status {
         const auto t0 = std::chrono::steady_clock::now();
@@ -1212,13 +1223,13 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                                  .count();
         return r;
     };
-    auto frame_tail = [&]() -> lv_status {
+    auto resolve = [&]() -> lv_status {
         LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
-        lv_status t = launch_resolve(ctx, RV, s);
-        if (t != LV_OK)
-            return t;
+        return launch_resolve(ctx, RV, s);
+    };
+    auto after_resolve = [&]() -> lv_status {
         LV_CUDA(ctx, cudaMemsetAsync(R.leaf.ptr, 0xFF, cells * sizeof(uint32_t), s));
-        t = launch_leaf_fill(ctx, RV, s);
+        lv_status t = launch_leaf_fill(ctx, RV, s);
         if (t != LV_OK)
             return t;
         LV_CUDA(ctx, cudaEventRecord(R.t_ray0, s));
@@ -1227,6 +1238,10 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             return t;
         LV_CUDA(ctx, cudaEventRecord(R.t_ray1, s));
         return LV_OK;
+    };
+    auto frame_tail = [&]() -> lv_status {
+        const lv_status t = resolve();
+        return t != LV_OK ? t : after_resolve();
     };
     /* A visible set larger than the brick pool renders in passes of at most
      * a pool's worth of bricks, front to back by brick distance
@@ -1331,7 +1346,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         agg.n_passes = passes;
         R.pass_stats = agg;
         R.passes = passes;
-        R.launches += passes * (1u + tail_launches);
+        R.launches = selection_launches(ctx, 1, info.depth) + passes * (1u + tail_launches);
         return LV_OK;
     };
     R.passes = 0;
@@ -1354,14 +1369,11 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                 return st;
         }
     }
-    if (!multi && desc->synchronous && vol->streamed_last)
+    if (!multi && desc->synchronous)
     {
-        /* this volume's last frame streamed bricks: find this frame's misses
-         * and stream them before the ray cast, instead of ray casting, then
-         * streaming and ray casting again */
+        /* find this frame's misses and stream them before the ray cast */
         uint32_t* hc = R.h_counters.as<uint32_t>();
-        LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
-        st = launch_resolve(ctx, RV, s);
+        st = resolve();
         if (st != LV_OK)
             return st;
         LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
@@ -1381,41 +1393,18 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             R.stats.bytes_uploaded += bytes;
             if (st != LV_OK && st != LV_EAGAIN)
                 return st;
+            /* resolve again with the streamed bricks; what still misses
+             * (pool too small) is not rendered */
+            st = frame_tail();
+            R.launches += 1;
         }
-        R.launches += 1;
+        else
+            st = after_resolve();
     }
-    if (!multi)
+    else if (!multi)
         st = frame_tail();
     if (st != LV_OK)
         return st;
-    if (desc->synchronous && !multi)
-    {
-        uint32_t* hc = R.h_counters.as<uint32_t>();
-        LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
-                                     cudaMemcpyDeviceToHost, s));
-        LV_CUDA(ctx, cudaStreamSynchronize(s));
-        const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
-        if (missing)
-        {
-            LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
-                                         sizeof(uint64_t) * missing,
-                                         cudaMemcpyDeviceToHost, s));
-            LV_CUDA(ctx, cudaStreamSynchronize(s));
-            uint32_t loaded = 0;
-            uint64_t bytes = 0;
-            st = timed_stream(R.h_missing.as<uint64_t>(), missing, frame, loaded, bytes);
-            R.stats.n_uploaded += loaded;
-            R.stats.bytes_uploaded += bytes;
-            if (st != LV_OK && st != LV_EAGAIN)
-                return st;
-            /* render again with the streamed bricks; what still misses
-             * (pool too small) is not rendered */
-            st = frame_tail();
-            if (st != LV_OK)
-                return st;
-            R.launches += tail_launches;
-        }
-    }
 
     /* 5. copy back counters (+ misses in async mode) */
     uint32_t* hc = R.h_counters.as<uint32_t>();
@@ -1434,10 +1423,22 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         R.pending_max = desc->max_uploads;
         R.pending_frame = frame;
     }
-    if (desc->synchronous)
-        vol->streamed_last = R.stats.n_uploaded > 0;
+    LV_CUDA(ctx, cudaEventRecord(R.frame_done, s));
     R.last_stream = s;
     R.have_last = true;
+    ++ctx->totals.frames;
+    ctx->totals.bricks_uploaded += R.stats.n_uploaded;
+    ctx->totals.bytes_uploaded += R.stats.bytes_uploaded;
+    ctx->totals.launches += R.launches;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_get_totals(lv_ctx* ctx, lv_ctx_totals* out)
+{
+    if (!ctx || !out)
+        return LV_EINVAL;
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    *out = ctx->totals;
     return LV_OK;
 }
 
