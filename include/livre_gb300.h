@@ -352,7 +352,8 @@ typedef struct lv_render_desc
     uint32_t step_policy;
     float early_exit;          /* 0.999 in fragRayCast.glsl:12 */
     uint32_t filter;
-    float data_range[2];       /* dataSourceRange; hi <= lo: dtype range */
+    float data_range[2];       /* dataSourceRange, used when hi > 0 and hi > lo,
+                                  else the voxel type's range */
     uint32_t synchronous;      /* 1: stream every missing brick first
                                   (RenderPipeline::renderSync); 0: render the
                                   nearest resident ancestors and stream up to

@@ -368,7 +368,13 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n, uint3
         if (st != LV_OK)
             return st;
         tfn_max = std::max(tfn_max, bv.tf->n);
-        groups[kernel_variant(V.dtype, V.filter, V.edge)].views.push_back(i);
+        const int variant = kernel_variant(V.dtype, V.filter, V.edge);
+        if (variant < kGroups)
+            groups[variant].views.push_back(i);
+        else if (b->cfg.queue != LV_QUEUE_VIEW_KERNELS)
+            return fail(ctx, LV_EINVAL,
+                        "the persistent batch kernels render uint8 and uint16 volumes; other "
+                        "voxel types need the view-kernel queue");
     }
     /* views [n, n_run) pad the launch to a power of two so a few captured
      * graphs serve every batch size: no roots, no visible nodes, no tiles */

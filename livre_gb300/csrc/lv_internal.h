@@ -60,6 +60,11 @@ struct LodView
     uint32_t* result;     /* LV_SELECT_RESULT_WORDS */
 };
 
+/* Voxel-type template argument of the ray-cast kernels for the types other
+ * than uint8 and uint16 (int8, int16, uint32, int32, float), read through a
+ * run-time switch on RayView::dtype. */
+constexpr int kDtAny = -1;
+
 /* Per-view constants of the ray cast. */
 struct RayView
 {
@@ -75,6 +80,7 @@ struct RayView
     uint32_t Lf;      /* finest level = depth - 1 */
     uint32_t N[3], B[3], O[3];
     uint32_t dtype;   /* lv_dtype */
+    uint32_t bpv;     /* bytes per voxel */
     uint32_t filter;
     uint32_t edge;    /* 1: some overlap is 0, clamp every trilinear tap */
     float dmul, dadd; /* density = value * dmul + dadd */

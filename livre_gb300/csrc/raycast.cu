@@ -288,12 +288,26 @@ __device__ __forceinline__ unsigned long long globaltimer()
     return t;
 }
 
+/* One voxel as a float (the GL shader's conversion of an unsigned, signed or
+ * float texel, fragRayCast.glsl:179-197; RayCastRenderer.cpp:236-277). DT is
+ * the voxel type, or kDtAny for a type chosen at run time by `dt`. */
 template <int DT>
-__device__ __forceinline__ float ldv(const uint8_t* p)
+__device__ __forceinline__ float ldv(const uint8_t* p, uint32_t dt)
 {
     if (DT == LV_DT_UINT16)
         return float(__ldg(reinterpret_cast<const uint16_t*>(p)));
-    return float(__ldg(p));
+    if (DT == LV_DT_UINT8)
+        return float(__ldg(p));
+    switch (dt)
+    {
+    case LV_DT_INT8: return float(__ldg(reinterpret_cast<const signed char*>(p)));
+    case LV_DT_INT16: return float(__ldg(reinterpret_cast<const short*>(p)));
+    case LV_DT_UINT32: return __uint2float_rn(__ldg(reinterpret_cast<const unsigned int*>(p)));
+    case LV_DT_INT32: return __int2float_rn(__ldg(reinterpret_cast<const int*>(p)));
+    case LV_DT_FLOAT: return __ldg(reinterpret_cast<const float*>(p));
+    case LV_DT_UINT16: return float(__ldg(reinterpret_cast<const uint16_t*>(p)));
+    default: return float(__ldg(p));
+    }
 }
 
 /* The voxels a sample reads and its interpolation weights; loaded one
@@ -317,7 +331,8 @@ template <int DT, int FILTER, int EDGE>
 __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick,
                                           const float s[3], Taps<FILTER>& T)
 {
-    constexpr int bpv = DT == LV_DT_UINT16 ? 2 : 1;
+    const int bpv = DT == LV_DT_UINT16 ? 2 : DT == LV_DT_UINT8 ? 1 : int(V.bpv);
+    const uint32_t dt = V.dtype;
     constexpr int NX = EDGE > 1 ? EDGE : 0;
     const int n0 = NX ? NX : int(V.N[0]), n1 = NX ? NX : int(V.N[1]), n2 = int(V.N[2]);
     if (FILTER == LV_FILTER_NEAREST)
@@ -325,7 +340,7 @@ __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick
         const int x = min(max(int(floorf(s[0])), 0), n0 - 1);
         const int y = min(max(int(floorf(s[1])), 0), n1 - 1);
         const int z = min(max(int(floorf(s[2])), 0), n2 - 1);
-        T.c[0] = ldv<DT>(brick + ((z * n1 + y) * n0 + x) * bpv);
+        T.c[0] = ldv<DT>(brick + ((z * n1 + y) * n0 + x) * bpv, dt);
         return;
     }
     const float fx0 = floorf(s[0]), fy0 = floorf(s[1]), fz0 = floorf(s[2]);
@@ -340,14 +355,14 @@ __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick
         const int z0 = min(max(iz, 0), n2 - 1), z1 = min(max(iz + 1, 0), n2 - 1);
         const int r00 = (z0 * n1 + y0) * n0, r01 = (z0 * n1 + y1) * n0;
         const int r10 = (z1 * n1 + y0) * n0, r11 = (z1 * n1 + y1) * n0;
-        T.c[0] = ldv<DT>(brick + (r00 + x0) * bpv);
-        T.c[1] = ldv<DT>(brick + (r00 + x1) * bpv);
-        T.c[2] = ldv<DT>(brick + (r01 + x0) * bpv);
-        T.c[3] = ldv<DT>(brick + (r01 + x1) * bpv);
-        T.c[4] = ldv<DT>(brick + (r10 + x0) * bpv);
-        T.c[5] = ldv<DT>(brick + (r10 + x1) * bpv);
-        T.c[6] = ldv<DT>(brick + (r11 + x0) * bpv);
-        T.c[7] = ldv<DT>(brick + (r11 + x1) * bpv);
+        T.c[0] = ldv<DT>(brick + (r00 + x0) * bpv, dt);
+        T.c[1] = ldv<DT>(brick + (r00 + x1) * bpv, dt);
+        T.c[2] = ldv<DT>(brick + (r01 + x0) * bpv, dt);
+        T.c[3] = ldv<DT>(brick + (r01 + x1) * bpv, dt);
+        T.c[4] = ldv<DT>(brick + (r10 + x0) * bpv, dt);
+        T.c[5] = ldv<DT>(brick + (r10 + x1) * bpv, dt);
+        T.c[6] = ldv<DT>(brick + (r11 + x0) * bpv, dt);
+        T.c[7] = ldv<DT>(brick + (r11 + x1) * bpv, dt);
     }
     else
     {
@@ -361,14 +376,14 @@ __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick
         const uint8_t* p01 = p00 + dy;
         const uint8_t* p10 = p00 + dz;
         const uint8_t* p11 = p10 + dy;
-        T.c[0] = ldv<DT>(p00);
-        T.c[1] = ldv<DT>(p00 + bpv);
-        T.c[2] = ldv<DT>(p01);
-        T.c[3] = ldv<DT>(p01 + bpv);
-        T.c[4] = ldv<DT>(p10);
-        T.c[5] = ldv<DT>(p10 + bpv);
-        T.c[6] = ldv<DT>(p11);
-        T.c[7] = ldv<DT>(p11 + bpv);
+        T.c[0] = ldv<DT>(p00, dt);
+        T.c[1] = ldv<DT>(p00 + bpv, dt);
+        T.c[2] = ldv<DT>(p01, dt);
+        T.c[3] = ldv<DT>(p01 + bpv, dt);
+        T.c[4] = ldv<DT>(p10, dt);
+        T.c[5] = ldv<DT>(p10 + bpv, dt);
+        T.c[6] = ldv<DT>(p11, dt);
+        T.c[7] = ldv<DT>(p11 + bpv, dt);
     }
 }
 
@@ -1539,6 +1554,45 @@ lv_status refill_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch&
     return LV_OK;
 }
 
+/* One CTA per tile (LV_LAUNCH_TILE_GRID). */
+template <int DT, int F, int EDGE, int LA>
+lv_status tiles_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                         cudaStream_t s, uint8_t* scratch)
+{
+    lv_status st = LV_OK;
+    if (!scratch)
+        scratch = render_order_scratch(ctx, V, L, st);
+    if (st != LV_OK)
+        return st;
+    const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+    if (st != LV_OK)
+        return st;
+    const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
+    raycast_tiles_kernel<DT, F, EDGE, LA><<<tiles, L.tile_w * L.tile_h, 0, s>>>(V, L.tile_w,
+                                                                            L.tile_h, order);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
+/* The voxel types other than uint8 / uint16 (kDtAny kernels, the voxel type a
+ * run-time switch) always use one CTA per tile, with the launch's tile shape
+ * (8 x 16 when it is not a CTA's), order and look-ahead. */
+template <int F, int EDGE>
+lv_status any_type_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                            cudaStream_t s, uint8_t* scratch)
+{
+    lv_render_launch T = L;
+    T.kind = LV_LAUNCH_TILE_GRID;
+    const uint32_t px = T.tile_w * T.tile_h;
+    if (px == 0 || px > 256 || px % 32 != 0)
+    {
+        T.tile_w = 8;
+        T.tile_h = 16;
+    }
+    return T.lookahead ? tiles_dispatch<kDtAny, F, EDGE, 1>(ctx, V, T, s, scratch)
+                       : tiles_dispatch<kDtAny, F, EDGE, 0>(ctx, V, T, s, scratch);
+}
+
 template <int DT, int F, int EDGE, int LA>
 lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                             cudaStream_t s, uint8_t* scratch)
@@ -1563,22 +1617,7 @@ lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launc
         return LV_OK;
     }
     if (L.kind == LV_LAUNCH_TILE_GRID)
-    {
-        lv_status st = LV_OK;
-        if (!scratch)
-            scratch = render_order_scratch(ctx, V, L, st);
-        if (st != LV_OK)
-            return st;
-        const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
-        if (st != LV_OK)
-            return st;
-        const uint32_t tiles =
-            ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
-        raycast_tiles_kernel<DT, F, EDGE, LA><<<tiles, L.tile_w * L.tile_h, 0, s>>>(
-            V, L.tile_w, L.tile_h, order);
-        LV_CUDA(ctx, cudaGetLastError());
-        return LV_OK;
-    }
+        return tiles_dispatch<DT, F, EDGE, LA>(ctx, V, L, s, scratch);
     if (L.kind == LV_LAUNCH_TILE_QUEUE)
     {
         lv_status st = LV_OK;
@@ -1690,16 +1729,20 @@ size_t tile_order_bytes(const RayView& V, const lv_render_launch& L)
     return order_bytes_of(V, L);
 }
 
+/* 0..7: uint8 / uint16 x filter x edge; 8..11: the other voxel types x
+ * filter x edge */
 int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge)
 {
-    return (dtype == LV_DT_UINT16 ? 4 : 0) + (filter == LV_FILTER_TRILINEAR ? 2 : 0) +
-           (edge ? 1 : 0);
+    const int fe = (filter == LV_FILTER_TRILINEAR ? 2 : 0) + (edge ? 1 : 0);
+    if (dtype != LV_DT_UINT8 && dtype != LV_DT_UINT16)
+        return 8 + fe;
+    return (dtype == LV_DT_UINT16 ? 4 : 0) + fe;
 }
 
 lv_status launch_raycast(lv_ctx* ctx, const RayView& V, cudaStream_t s)
 {
-    if (V.dtype != LV_DT_UINT8 && V.dtype != LV_DT_UINT16)
-        return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
+    if (V.dtype > LV_DT_INT32)
+        return fail(ctx, LV_EINVAL, "unknown voxel type");
     /* the ray-cast kernels derive the samples per ray themselves */
     return launch_view_raycast(ctx, V, ctx->launch, nullptr, s);
 }
@@ -1709,6 +1752,10 @@ lv_status launch_view_raycast(lv_ctx* ctx, const RayView& V, const lv_render_lau
 {
     switch (kernel_variant(V.dtype, V.filter, V.edge))
     {
+    case 8: return any_type_dispatch<0, 0>(ctx, V, L, s, order_scratch);
+    case 9: return any_type_dispatch<0, 1>(ctx, V, L, s, order_scratch);
+    case 10: return any_type_dispatch<1, 0>(ctx, V, L, s, order_scratch);
+    case 11: return any_type_dispatch<1, 1>(ctx, V, L, s, order_scratch);
     case 0: return plain_dispatch<LV_DT_UINT8, 0, 0>(ctx, V, L, s, order_scratch);
     case 1: return plain_dispatch<LV_DT_UINT8, 0, 1>(ctx, V, L, s, order_scratch);
     case 2: return plain_dispatch<LV_DT_UINT8, 1, 0>(ctx, V, L, s, order_scratch);

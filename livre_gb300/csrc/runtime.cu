@@ -92,20 +92,20 @@ uint32_t bytes_per_voxel(uint32_t dt)
     }
 }
 
-/* dataSourceRange of RayCastRenderer::onFrameStart (RayCastRenderer.cpp:
- * 236-285): the integer type's range. */
+/* dataSourceRange of a voxel type: its numeric_limits min and max
+ * (RayCastRenderer.cpp:236-277; for float, the smallest positive normal and
+ * the largest finite value, as the reference has it). */
 void type_range(uint32_t dt, float& lo, float& hi)
 {
     switch (dt)
     {
-    case LV_DT_UINT16:
-        lo = 0.0f;
-        hi = 65535.0f;
-        break;
-    default:
-        lo = 0.0f;
-        hi = 255.0f;
-        break;
+    case LV_DT_UINT16: lo = 0.0f; hi = 65535.0f; break;
+    case LV_DT_UINT32: lo = 0.0f; hi = 4294967295.0f; break;
+    case LV_DT_INT8: lo = -128.0f; hi = 127.0f; break;
+    case LV_DT_INT16: lo = -32768.0f; hi = 32767.0f; break;
+    case LV_DT_INT32: lo = -2147483648.0f; hi = 2147483647.0f; break;
+    case LV_DT_FLOAT: lo = 1.17549435e-38f; hi = 3.40282347e+38f; break;
+    default: lo = 0.0f; hi = 255.0f; break;
     }
 }
 
@@ -499,8 +499,8 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
                         uint32_t* leaf, uint32_t* counters, RayView& V)
 {
     const lv_volume_info& info = vol->info;
-    if (info.dtype != LV_DT_UINT8 && info.dtype != LV_DT_UINT16)
-        return fail(ctx, LV_EINVAL, "ray cast supports uint8 and uint16 volumes");
+    if (info.dtype > LV_DT_INT32)
+        return fail(ctx, LV_EINVAL, "unknown voxel type");
     std::memset(&V, 0, sizeof(V));
     float lim[6], planes[6][4], eye[3], dir[3];
     bool ok = false;
@@ -534,9 +534,12 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     std::memcpy(V.clip, lod.clip_planes, sizeof(V.clip));
     V.Lf = Lf;
     V.dtype = info.dtype;
+    V.bpv = bytes_per_voxel(info.dtype);
     V.filter = desc.filter == LV_FILTER_TRILINEAR ? LV_FILTER_TRILINEAR : LV_FILTER_NEAREST;
+    /* the transfer function's range when valid, else the type's
+     * (RayCastRenderer.cpp:279-284) */
     float lo = desc.data_range[0], hi = desc.data_range[1];
-    if (!(hi > lo))
+    if (!(hi > 0.0f && hi - lo > 0.0f))
         type_range(info.dtype, lo, hi);
     V.dmul = 1.0f / (hi - lo);
     V.dadd = -lo / (hi - lo);

@@ -345,11 +345,20 @@ struct RenderSet
         x = std::min(std::max(x, 0), int(N[0]) - 1);
         y = std::min(std::max(y, 0), int(N[1]) - 1);
         z = std::min(std::max(z, 0), int(N[2]) - 1);
-        const size_t i = (size_t(z) * N[1] + size_t(y)) * N[0] + size_t(x);
-        if (dtype == 2)
-            return double(reinterpret_cast<const uint16_t*>(bricks)
-                              [brick * brickVoxels + i]);
-        return double(bricks[brick * brickVoxels + i]);
+        const size_t k = brick * brickVoxels +
+                         (size_t(z) * N[1] + size_t(y)) * N[0] + size_t(x);
+        /* lv_dtype codes: 0 float, 1 uint8, 2 uint16, 3 uint32, 4 int8,
+         * 5 int16, 6 int32 (the voxel value as the GL shader's texel) */
+        switch (dtype)
+        {
+        case 0: return double(reinterpret_cast<const float*>(bricks)[k]);
+        case 2: return double(reinterpret_cast<const uint16_t*>(bricks)[k]);
+        case 3: return double(reinterpret_cast<const uint32_t*>(bricks)[k]);
+        case 4: return double(reinterpret_cast<const int8_t*>(bricks)[k]);
+        case 5: return double(reinterpret_cast<const int16_t*>(bricks)[k]);
+        case 6: return double(reinterpret_cast<const int32_t*>(bricks)[k]);
+        default: return double(bricks[k]);
+        }
     }
 
     /* Per-ray mode: s = FP32 slot coordinate (nearest: the local position;

@@ -147,7 +147,8 @@ typedef struct
 /* Renders the set of bricks `node_ids` (the rendering set: a partition of
  * the visible region; when an id and one of its ancestors are both present
  * the ancestor wins, as RenderingSetGeneratorFilter.cpp:51-79 does).
- * bricks: n_nodes bricks of max_block^3 voxels (x fastest), dtype 1=u8 2=u16.
+ * bricks: n_nodes bricks of max_block^3 voxels (x fastest), dtype an lv_dtype
+ * code (0 float, 1 uint8, 2 uint16, 3 uint32, 4 int8, 5 int16, 6 int32).
  * out_rgba: width*height*4 doubles, row y=0 is the bottom row.
  * n_threads <= 0 uses every hardware thread. */
 int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
