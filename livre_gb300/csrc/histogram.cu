@@ -36,7 +36,7 @@ template <int DT>
 __global__ void __launch_bounds__(256)
     histogram_kernel(const uint8_t* __restrict__ pool, const HistJob* __restrict__ jobs,
                      uint32_t N0, uint32_t N1, uint32_t N2, uint32_t O0, uint32_t O1,
-                     uint32_t O2, uint32_t n_bins, float lo, float scale_bins,
+                     uint32_t O2, uint32_t dt, uint32_t n_bins, float lo, float scale_bins,
                      unsigned long long* __restrict__ per_brick,
                      unsigned long long* __restrict__ acc)
 {
@@ -55,8 +55,21 @@ __global__ void __launch_bounds__(256)
         float v;
         if (DT == LV_DT_UINT16)
             v = float(reinterpret_cast<const uint16_t*>(brick)[idx]);
-        else
+        else if (DT == LV_DT_UINT8)
             v = float(brick[idx]);
+        else /* kDtAny: the voxel type `dt` */
+            switch (dt)
+            {
+            case LV_DT_INT8: v = float(reinterpret_cast<const int8_t*>(brick)[idx]); break;
+            case LV_DT_INT16: v = float(reinterpret_cast<const int16_t*>(brick)[idx]); break;
+            case LV_DT_UINT32:
+                v = __uint2float_rn(reinterpret_cast<const uint32_t*>(brick)[idx]);
+                break;
+            case LV_DT_INT32:
+                v = __int2float_rn(reinterpret_cast<const int32_t*>(brick)[idx]);
+                break;
+            default: v = reinterpret_cast<const float*>(brick)[idx]; break;
+            }
         const float f = floorf((v - lo) * scale_bins);
         const int bin = int(fminf(fmaxf(f, 0.0f), float(n_bins - 1)));
         atomicAdd(&bins[bin], 1u);
@@ -81,8 +94,6 @@ extern "C" lv_status lv_histogram(lv_volume* vol, const uint64_t* ids, uint32_t 
         !(range_hi > range_lo))
         return LV_EINVAL;
     lv_ctx* ctx = vol->ctx;
-    if (vol->info.dtype != LV_DT_UINT8 && vol->info.dtype != LV_DT_UINT16)
-        return fail(ctx, LV_EINVAL, "histograms support uint8 and uint16 volumes");
     std::lock_guard<std::mutex> lock(ctx->mutex);
     LV_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->upload_stream;
@@ -122,18 +133,14 @@ extern "C" lv_status lv_histogram(lv_volume* vol, const uint64_t* ids, uint32_t 
     const float scale_bins = float(n_bins - 1) / (range_hi - range_lo);
     const size_t smem = sizeof(uint32_t) * n_bins;
     const auto& I = vol->info;
-    if (I.dtype == LV_DT_UINT16)
-        histogram_kernel<LV_DT_UINT16><<<n, 256, smem, s>>>(
-            ctx->pool->arena.as<uint8_t>(), djobs.as<HistJob>(), I.max_block[0], I.max_block[1],
-            I.max_block[2], I.overlap[0], I.overlap[1], I.overlap[2], n_bins, range_lo,
-            scale_bins, per_brick ? dout.as<unsigned long long>() : nullptr,
-            dacc.as<unsigned long long>());
-    else
-        histogram_kernel<LV_DT_UINT8><<<n, 256, smem, s>>>(
-            ctx->pool->arena.as<uint8_t>(), djobs.as<HistJob>(), I.max_block[0], I.max_block[1],
-            I.max_block[2], I.overlap[0], I.overlap[1], I.overlap[2], n_bins, range_lo,
-            scale_bins, per_brick ? dout.as<unsigned long long>() : nullptr,
-            dacc.as<unsigned long long>());
+    auto kernel = I.dtype == LV_DT_UINT16  ? histogram_kernel<LV_DT_UINT16>
+                  : I.dtype == LV_DT_UINT8 ? histogram_kernel<LV_DT_UINT8>
+                                           : histogram_kernel<kDtAny>;
+    kernel<<<n, 256, smem, s>>>(ctx->pool->arena.as<uint8_t>(), djobs.as<HistJob>(),
+                                I.max_block[0], I.max_block[1], I.max_block[2], I.overlap[0],
+                                I.overlap[1], I.overlap[2], I.dtype, n_bins, range_lo, scale_bins,
+                                per_brick ? dout.as<unsigned long long>() : nullptr,
+                                dacc.as<unsigned long long>());
     LV_CUDA(ctx, cudaGetLastError());
     LV_CUDA(ctx, cudaMemcpyAsync(accumulated, dacc.ptr, sizeof(uint64_t) * n_bins,
                                  cudaMemcpyDeviceToHost, s));

@@ -126,3 +126,28 @@ def test_batches_of_other_voxel_types(gpu_ctx, oracle):
     batch.close()
     vol.close()
     tf.close()
+
+
+@pytest.mark.parametrize("dtype,ntype,vmap,rng", TYPES)
+def test_histograms_of_other_voxel_types(gpu_ctx, oracle, dtype, ntype, vmap, rng):
+    """lv_histogram bins every voxel type with the same rule as uint8/uint16:
+    floor((v - lo) * (n - 1) / (hi - lo)) clamped, counts weighted by the
+    finest voxels one voxel stands for, the overlap skipped."""
+    import livre_gb300 as lv
+    vi, ovol, vol, bricks = typed_volume(gpu_ctx, oracle, lv, dtype, ntype, vmap)
+    lo, hi = rng or (-128.0, 127.0)
+    n_bins = 100
+    ids = [lv.NodeId(0, (0, 0, 0)).id, lv.NodeId(1, (1, 0, 1)).id, lv.NodeId(2, (3, 2, 0)).id]
+    acc, per = vol.histogram(ids, n_bins, (lo, hi), per_brick=True)
+    scale_bins = np.float32(n_bins - 1) / (np.float32(hi) - np.float32(lo))
+    want_acc = np.zeros(n_bins, np.uint64)
+    for k, i in enumerate(ids):
+        b = bricks[i].reshape(34, 34, 34)[1:33, 1:33, 1:33].astype(np.float32)
+        f = np.floor((b - np.float32(lo)) * np.float32(scale_bins))
+        bins = np.clip(f, 0, n_bins - 1).astype(np.int64)
+        scale = (2 ** (vi.depth - 1 - (i & 0xF))) ** 3
+        h = np.bincount(bins.ravel(), minlength=n_bins).astype(np.uint64) * np.uint64(scale)
+        assert (per[k] == h).all(), k
+        want_acc += h
+    assert (acc == want_acc).all()
+    vol.close()
