@@ -371,6 +371,11 @@ def served_mode(ctx, args, dev, seed=11):
            "pool_gib": args.pool_gib or 96, "rates": []}
     for rate in args.serve_rates:
         reqs = [make_request() for _ in range(max(64, int(rate * args.serve_seconds)))]
+        # every brick the stream needs made resident first, so neither mode
+        # pays (or is spared) streaming the other mode already did
+        for v, t, d in reqs:
+            ctx.render(v, t, d, take(d.width, d.height))
+        ctx.last_stats()
         served = run(0, rate, reqs)
         plain = run(1, rate, reqs)
         out["rates"].append({"served": served, "plain": plain})
