@@ -359,6 +359,12 @@ typedef struct lv_render_desc
                                   nearest resident ancestors and stream up to
                                   max_uploads misses (renderAsync) */
     uint32_t max_uploads;      /* async mode only; reference: 1 per frame */
+    uint32_t rect[4];          /* {x, y, w, h}: render only these pixels of the
+                                  width x height frame (a sort-first tile,
+                                  Channel.cpp:234-281), writing them at their
+                                  place in d_rgba and no others; w = 0 or
+                                  h = 0: the whole frame. The visible set,
+                                  samples and pixels are the whole frame's. */
 } lv_render_desc;
 
 typedef struct lv_frame_stats

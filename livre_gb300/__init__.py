@@ -670,7 +670,9 @@ class Context:
     def render_desc(self, mv, proj, width, height, sse=1.0, min_lod=0, max_lod=100,
                     samples_per_ray=0, step_policy=STEP_HALF_VOXEL, early_exit=0.999,
                     filt=FILTER_TRILINEAR, data_range=(0.0, 0.0), synchronous=True,
-                    max_uploads=1, time_step=0, clip_planes=None, rng=(0.0, 1.0)):
+                    max_uploads=1, time_step=0, clip_planes=None, rng=(0.0, 1.0), rect=None):
+        """rect = (x, y, w, h): render only those pixels of the frame (a
+        sort-first tile); None renders the whole frame."""
         d = _abi.RenderDesc()
         d.camera = make_camera(mv, proj)
         d.width, d.height = width, height
@@ -679,6 +681,9 @@ class Context:
             samples_per_ray, step_policy, early_exit, filt)
         d.data_range[0], d.data_range[1] = data_range
         d.synchronous, d.max_uploads = int(bool(synchronous)), max_uploads
+        if rect is not None:
+            for i in range(4):
+                d.rect[i] = int(rect[i])
         return d
 
     def render(self, volume, tf, desc, out=None, stream=None):

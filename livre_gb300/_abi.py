@@ -56,7 +56,8 @@ class RenderDesc(C.Structure):
                 ("lod", LodParams), ("samples_per_ray", C.c_uint32),
                 ("step_policy", C.c_uint32), ("early_exit", C.c_float),
                 ("filter", C.c_uint32), ("data_range", C.c_float * 2),
-                ("synchronous", C.c_uint32), ("max_uploads", C.c_uint32)]
+                ("synchronous", C.c_uint32), ("max_uploads", C.c_uint32),
+                ("rect", C.c_uint32 * 4)]
 
 
 class FrameStats(C.Structure):

@@ -92,7 +92,9 @@ struct RayView
     uint32_t max_base;    /* last trilinear base voxel of a brick:
                              (N2-2)*N1*N0 + (N1-2)*N0 + N0-2 */
     float early;
-    uint32_t W, H;
+    uint32_t W, H;          /* pixels rendered: the rect (tiles cover these) */
+    uint32_t x0, y0;        /* the rect's corner in the frame */
+    uint32_t FW, FH;        /* the frame (ray directions, output rows) */
     uint32_t samples_fixed; /* 0 = policy */
     uint32_t step_policy;
     uint32_t max_voxel_dim;

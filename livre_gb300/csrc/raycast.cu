@@ -433,17 +433,26 @@ struct RayGeom
     bool hit;
 };
 
-/* Ray through the centre of pixel (px, py); FP32 IEEE ops in fixed order. */
+/* Pixel (px, py) of the rendered rect as an index into the frame. */
+__device__ __forceinline__ uint64_t frame_index(const RayView& V, uint32_t px, uint32_t py)
+{
+    return uint64_t(py + V.y0) * V.FW + (px + V.x0);
+}
+
+/* Ray through the centre of pixel (px, py) of the rendered rect (frame pixel
+ * (x0 + px, y0 + py)); FP32 IEEE ops in fixed order. */
 __device__ __forceinline__ RayGeom ray_setup(const RayView& V, uint32_t px,
                                              uint32_t py)
 {
     RayGeom g;
-    const float nx = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(__uint2float_rn(px), 0.5f), 2.0f),
-                                         __uint2float_rn(V.W)),
-                               1.0f);
-    const float ny = __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(__uint2float_rn(py), 0.5f), 2.0f),
-                                         __uint2float_rn(V.H)),
-                               1.0f);
+    const float nx =
+        __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(__uint2float_rn(px + V.x0), 0.5f), 2.0f),
+                            __uint2float_rn(V.FW)),
+                  1.0f);
+    const float ny =
+        __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(__uint2float_rn(py + V.y0), 0.5f), 2.0f),
+                            __uint2float_rn(V.FH)),
+                  1.0f);
     float e[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -755,7 +764,7 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
  * the same render texture), else transparent black. */
 __device__ __forceinline__ float4 initial_dst(const RayView& V, uint32_t px, uint32_t py)
 {
-    return V.accumulate ? V.out[uint64_t(py) * V.W + px] : make_float4(0.f, 0.f, 0.f, 0.f);
+    return V.accumulate ? V.out[frame_index(V, px, py)] : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 /* The whole ray. LOOKAHEAD = 1 loads the voxels of sample k + 1 before
@@ -808,7 +817,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const RayView V)
         const RayGeom g = ray_setup(V, px, py);
         const float4 r =
             march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
-        V.out[uint64_t(py) * V.W + px] = r;
+        V.out[frame_index(V, px, py)] = r;
     }
     /* warp-aggregated 64-bit sample count */
     unsigned long long s = nsamp;
@@ -892,7 +901,7 @@ __global__ void __launch_bounds__(256)
         {
             const RayGeom g = ray_setup(sV, px, py);
             const float4 r = march<DT, FILTER, TF_SHARED, EDGE>(sV, g, step, ac, nsamp);
-            sV.out[uint64_t(py) * sV.W + px] = r;
+            sV.out[frame_index(sV, px, py)] = r;
         }
         unsigned long long sum = nsamp;
 #pragma unroll
@@ -1020,7 +1029,7 @@ __global__ void __launch_bounds__(256)
         if (px < V.W && py < V.H)
         {
             const RayGeom g = ray_setup(V, px, py);
-            V.out[uint64_t(py) * V.W + px] =
+            V.out[frame_index(V, px, py)] =
                 march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
         }
     }
@@ -1049,7 +1058,7 @@ __global__ void __launch_bounds__(256)
     if (px < V.W && py < V.H)
     {
         const RayGeom g = ray_setup(V, px, py);
-        V.out[uint64_t(py) * V.W + px] =
+        V.out[frame_index(V, px, py)] =
             march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
     }
     unsigned long long sum = nsamp;
@@ -1088,7 +1097,7 @@ __global__ void __launch_bounds__(128)
         if (px < V.W && py < V.H)
         {
             const RayGeom g = ray_setup(V, px, py);
-            V.out[uint64_t(py) * V.W + px] =
+            V.out[frame_index(V, px, py)] =
                 march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
         }
         __syncwarp();
@@ -1314,7 +1323,7 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
                     active = ray_begin(g, K.step, r) && !(init.w > V.early);
                     r.dst = init;
                     if (!active)
-                        V.out[uint64_t(py) * V.W + px] = init;
+                        V.out[frame_index(V, px, py)] = init;
                 }
             }
         }
@@ -1339,7 +1348,7 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
                 if (!ray_step<DT, FILTER, 0, EDGE>(V, r, K.step, K.ac, nsamp))
                 {
                     active = false;
-                    V.out[uint64_t(py) * V.W + px] = r.dst;
+                    V.out[frame_index(V, px, py)] = r.dst;
                     break;
                 }
     }

@@ -544,8 +544,23 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     V.dmul = 1.0f / (hi - lo);
     V.dadd = -lo / (hi - lo);
     V.early = desc.early_exit;
-    V.W = desc.width;
-    V.H = desc.height;
+    V.FW = desc.width;
+    V.FH = desc.height;
+    if (desc.rect[2] && desc.rect[3])
+    {
+        if (uint64_t(desc.rect[0]) + desc.rect[2] > desc.width ||
+            uint64_t(desc.rect[1]) + desc.rect[3] > desc.height)
+            return fail(ctx, LV_EINVAL, "render rect outside the frame");
+        V.x0 = desc.rect[0];
+        V.y0 = desc.rect[1];
+        V.W = desc.rect[2];
+        V.H = desc.rect[3];
+    }
+    else
+    {
+        V.W = desc.width;
+        V.H = desc.height;
+    }
     V.samples_fixed = desc.samples_per_ray;
     V.step_policy = desc.step_policy;
     V.max_voxel_dim = std::max(info.voxels[0], std::max(info.voxels[1], info.voxels[2]));

@@ -420,7 +420,8 @@ void loop_batched(lv_server* S)
             for (size_t i = 0; i < S->queue.size() && cand.size() < S->cfg.max_batch; ++i)
             {
                 const lv_render_desc& d = S->queue[i]->r.desc;
-                const uint64_t p = uint64_t(d.width) * d.height;
+                const uint64_t p = d.rect[2] && d.rect[3] ? uint64_t(d.rect[2]) * d.rect[3]
+                                                          : uint64_t(d.width) * d.height;
                 if (!cand.empty() && S->cfg.max_pixels && pixels + p > S->cfg.max_pixels)
                     break;
                 pixels += p;
