@@ -240,6 +240,8 @@ struct Renderer
      * before its ray cast ends, so the next frame (on any stream) and any
      * brick streaming wait for it */
     cudaEvent_t frame_done = nullptr;
+    /* the residency pass's counters have reached the host */
+    cudaEvent_t resolve_done = nullptr;
     /* timing of the last frame: selection and ray cast */
     cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
     uint32_t launches = 0;

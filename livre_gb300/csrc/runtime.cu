@@ -140,6 +140,7 @@ lv_status ensure_renderer(lv_ctx* ctx)
     cudaEventCreateWithFlags(&r->render_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->upload_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->frame_done, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->resolve_done, cudaEventDisableTiming);
     cudaEventCreate(&r->t_sel0);
     cudaEventCreate(&r->t_sel1);
     cudaEventCreate(&r->t_ray0);
@@ -653,6 +654,7 @@ extern "C" void lv_ctx_destroy(lv_ctx* ctx)
         cudaEventDestroy(ctx->renderer->render_event);
         cudaEventDestroy(ctx->renderer->upload_event);
         cudaEventDestroy(ctx->renderer->frame_done);
+        cudaEventDestroy(ctx->renderer->resolve_done);
         cudaEventDestroy(ctx->renderer->t_sel0);
         cudaEventDestroy(ctx->renderer->t_sel1);
         cudaEventDestroy(ctx->renderer->t_ray0);
@@ -1229,9 +1231,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     if (st != LV_OK)
         return st;
     /* residency pass, leaf grid and ray cast. The synchronous mode reads the
-     * residency pass's miss count back before the rest (one host round trip
-     * early in the frame), streams the misses, and returns without waiting
-     * for the ray cast. */
+     * residency pass's miss count back while the rest runs, streams any
+     * misses and renders again, and returns without waiting for the ray
+     * cast. */
     auto timed_stream = [&](const uint64_t* ids, uint32_t n, uint32_t protect,
                             uint32_t& loaded, uint64_t& bytes) -> lv_status {
         const auto t0 = std::chrono::steady_clock::now();
@@ -1389,14 +1391,21 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     }
     if (!multi && desc->synchronous)
     {
-        /* find this frame's misses and stream them before the ray cast */
+        /* The residency pass's miss count goes to the host while the rest of
+         * the frame is already queued behind it; the host waits for the
+         * count only. A frame that missed bricks streams them and renders
+         * again (the first ray cast lacked them). */
         uint32_t* hc = R.h_counters.as<uint32_t>();
         st = resolve();
         if (st != LV_OK)
             return st;
         LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
                                      cudaMemcpyDeviceToHost, s));
-        LV_CUDA(ctx, cudaStreamSynchronize(s));
+        LV_CUDA(ctx, cudaEventRecord(R.resolve_done, s));
+        st = after_resolve();
+        if (st != LV_OK)
+            return st;
+        LV_CUDA(ctx, cudaEventSynchronize(R.resolve_done));
         const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
         if (missing)
         {
@@ -1414,10 +1423,8 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             /* resolve again with the streamed bricks; what still misses
              * (pool too small) is not rendered */
             st = frame_tail();
-            R.launches += 1;
+            R.launches += tail_launches;
         }
-        else
-            st = after_resolve();
     }
     else if (!multi)
         st = frame_tail();
