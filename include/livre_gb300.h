@@ -521,7 +521,11 @@ typedef struct lv_batch_config
                                 estimated samples of their centre ray */
     uint32_t lookahead;      /* view kernels: 1 = one-sample look-ahead (the
                                 voxels of the next sample load while the
-                                current one composites), as lv_render_launch */
+                                current one composites), as lv_render_launch.
+                                Default 0: on the mixed 64-view batch, 97 ms
+                                without against 108 ms with it (many view
+                                kernels share the SMs, and the look-ahead's
+                                registers cost resident warps) */
 } lv_batch_config;
 
 /* A batch renderer on ctx (its own stream, graphs and per-view buffers).

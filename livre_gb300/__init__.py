@@ -775,13 +775,13 @@ class Batch:
                    queue=_abi.QUEUE_CTA_TILES, samples_per_check=8, order=None,
                    lookahead=None):
         """order: ORDER_LONGEST_FIRST (default for CTA tiles) or ORDER_RASTER
-        (the only order of warp refill); lookahead (view kernels only):
-        default 1 for view kernels, else 0."""
+        (the only order of warp refill); lookahead (view kernels only, 0 or
+        1): default 0."""
         if order is None:
             order = (_abi.ORDER_RASTER if queue == _abi.QUEUE_WARP_REFILL
                      else _abi.ORDER_LONGEST_FIRST)
         if lookahead is None:
-            lookahead = 1 if queue == _abi.QUEUE_VIEW_KERNELS else 0
+            lookahead = 0
         c = _abi.BatchConfig(tile_w, tile_h, ctas_per_sm, tf_shared, use_graph, queue,
                              samples_per_check, order, lookahead)
         check(lib().lv_batch_set_config(self.handle, C.byref(c)), self.ctx.handle)

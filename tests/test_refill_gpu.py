@@ -83,7 +83,7 @@ def test_render_launch_validation(gpu_ctx):
     dict(queue=0, tile_w=8, tile_h=8, tf_shared=1, ctas_per_sm=3),
     dict(queue=0, tile_w=8, tile_h=16, tf_shared=1, order=0),
     dict(queue=2, tile_w=8, tile_h=16),
-    dict(queue=2, tile_w=8, tile_h=16, lookahead=0),
+    dict(queue=2, tile_w=8, tile_h=16, lookahead=1),
     dict(queue=2, tile_w=16, tile_h=16, order=0),
 ])
 def test_batch_queue_kinds_match_single_views(gpu_ctx, cfg):
