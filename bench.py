@@ -441,6 +441,8 @@ def outofcore_mode(local, args, dev):
                                        * vi.brick_bytes / 1e9),
         "samples_per_s": float(sum(r[1]["n_samples"] for r in timed) / (wall.sum() / 1e3)),
         "raycast_ms_mean": float(np.mean([r[1]["raycast_ms"] for r in timed])),
+        "select_ms_mean": float(np.mean([r[1]["select_ms"] for r in timed])),
+        "stream_ms_mean": float(np.mean([r[1]["stream_ms"] for r in timed])),
     }
     vol.close()
     tf.close()

@@ -166,12 +166,62 @@ __host__ __device__ __forceinline__ float fbm_at(const uint16_t* P, const lv_fbm
     return fbm<O>(P, f, x, y, z);
 }
 
-/* One brick per blockIdx.y; voxels strided over blockIdx.x and threads. */
+/* The gradient of corner hash h at a point, split into its x part and the
+ * rest: grad(h, x, y, z) = add(sx * x, c) when the gradient has an x
+ * component (h < 8, 12, 14; sx = +-1, c the signed other component), else
+ * the constant c = grad(h, x, y, z) itself. add(a, b) = add(b, a) exactly
+ * and +-1 * x is exact, so this is the same single rounding as grad<O>. */
+struct CornerGrad
+{
+    float sx, c;
+    bool has_x;
+};
+
+__device__ __forceinline__ CornerGrad corner_grad(uint32_t h, float y, float z)
+{
+    h &= 15u;
+    CornerGrad g;
+    if (h < 8u)
+    {
+        g.has_x = true;
+        g.sx = (h & 1u) ? -1.0f : 1.0f;
+        const float v = h < 4u ? y : z;
+        g.c = (h & 2u) ? -v : v;
+    }
+    else if (h == 12u || h == 14u)
+    {
+        g.has_x = true;
+        g.sx = (h & 2u) ? -1.0f : 1.0f;
+        g.c = (h & 1u) ? -y : y;
+    }
+    else
+    {
+        g.has_x = false;
+        g.sx = 0.0f;
+        g.c = DeviceOps::add((h & 1u) ? -y : y, (h & 2u) ? -z : z);
+    }
+    return g;
+}
+
+__device__ __forceinline__ float corner_value(const CornerGrad& g, float x)
+{
+    return g.has_x ? DeviceOps::add(DeviceOps::mul(g.sx, x), g.c) : g.c;
+}
+
+/* One brick per blockIdx.y; each thread takes runs of R consecutive voxels
+ * of a row (x), strided over blockIdx.x and the threads. Along a run only x
+ * changes, so per octave the y and z lattice cells, fractions and fades are
+ * computed once, and the eight corner hashes and the y / z parts of their
+ * gradients only when the x cell changes; every voxel still gets the values
+ * of fbm_at's operations (same roundings, same order), so the bytes equal the
+ * host generator's. */
+template <int R>
 __global__ void __launch_bounds__(256)
     fbm_brick_kernel(lv_volume_info info, lv_fbm_params f, const uint16_t* __restrict__ perm,
                      const uint64_t* __restrict__ ids, const uint64_t* __restrict__ offsets,
                      uint8_t* __restrict__ out, uint64_t brick_bytes)
 {
+    using O = DeviceOps;
     __shared__ uint16_t P[512];
     for (uint32_t i = threadIdx.x; i < 512; i += blockDim.x)
         P[i] = perm[i];
@@ -179,17 +229,89 @@ __global__ void __launch_bounds__(256)
     const uint64_t id = ids[blockIdx.y];
     const FbmBrick b = brick_consts(info, f, id);
     uint8_t* dst = out + (offsets ? offsets[blockIdx.y] : uint64_t(blockIdx.y) * brick_bytes);
-    const uint32_t n = b.N[0] * b.N[1] * b.N[2];
+    const uint32_t runs_x = (b.N[0] + R - 1) / R;
+    const uint32_t n_runs = runs_x * b.N[1] * b.N[2];
     const bool u16 = info.dtype == LV_DT_UINT16;
     const float full = u16 ? 65535.0f : 255.0f;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    auto clampi = [](int32_t g, int32_t hi) { return g < 0 ? 0 : (g > hi ? hi : g); };
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_runs;
+         w += gridDim.x * blockDim.x)
     {
-        const uint32_t i = v % b.N[0], j = (v / b.N[0]) % b.N[1], k = v / (b.N[0] * b.N[1]);
-        const uint32_t q = quantise<DeviceOps>(fbm_at<DeviceOps>(P, f, b, i, j, k), full);
-        if (u16)
-            reinterpret_cast<uint16_t*>(dst)[v] = uint16_t(q);
-        else
-            dst[v] = uint8_t(q);
+        const uint32_t rx = w % runs_x, j = (w / runs_x) % b.N[1], k = w / (runs_x * b.N[1]);
+        const uint32_t i0 = rx * R;
+        const uint32_t cnt = min(uint32_t(R), b.N[0] - i0);
+        const int32_t gj = clampi(b.base[1] + int32_t(j), b.last[1]);
+        const int32_t gk = clampi(b.base[2] + int32_t(k), b.last[2]);
+        const float y = O::mul(O::add(float(gj), 0.5f), b.scale);
+        const float z = O::mul(O::add(float(gk), 0.5f), b.scale);
+        float xs[R], sum[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+        {
+            const int32_t gi = clampi(b.base[0] + int32_t(i0 + r), b.last[0]);
+            xs[r] = O::mul(O::add(float(gi), 0.5f), b.scale);
+            sum[r] = 0.0f;
+        }
+        float amp = 1.0f, freq = 1.0f;
+        for (uint32_t o = 0; o < f.octaves; ++o)
+        {
+            const float yv = O::mul(y, freq), zv = O::mul(z, freq);
+            const float fy = floorf(yv), fz = floorf(zv);
+            const uint32_t Y = uint32_t(int32_t(fy)) & 255u, Z = uint32_t(int32_t(fz)) & 255u;
+            const float yf = O::sub(yv, fy), zf = O::sub(zv, fz);
+            const float v = fade<O>(yf), wz = fade<O>(zf);
+            const float y1 = O::sub(yf, 1.0f), z1 = O::sub(zf, 1.0f);
+            uint32_t prevX = 0xFFFFFFFFu;
+            /* corners (dx, dy, dz): g0 (0,0,0) g1 (1,0,0) g2 (0,1,0) g3 (1,1,0)
+             * g4 (0,0,1) g5 (1,0,1) g6 (0,1,1) g7 (1,1,1) */
+            CornerGrad g0{}, g1{}, g2{}, g3{}, g4{}, g5{}, g6{}, g7{};
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+            {
+                if (uint32_t(r) < cnt)
+                {
+                    const float xv = O::mul(xs[r], freq);
+                    const float fx = floorf(xv);
+                    const uint32_t X = uint32_t(int32_t(fx)) & 255u;
+                    if (X != prevX)
+                    {
+                        prevX = X;
+                        const uint32_t A = P[X] + Y, AA = P[A] + Z, AB = P[A + 1] + Z;
+                        const uint32_t B = P[X + 1] + Y, BA = P[B] + Z, BB = P[B + 1] + Z;
+                        g0 = corner_grad(P[AA], yf, zf);
+                        g1 = corner_grad(P[BA], yf, zf);
+                        g2 = corner_grad(P[AB], y1, zf);
+                        g3 = corner_grad(P[BB], y1, zf);
+                        g4 = corner_grad(P[AA + 1], yf, z1);
+                        g5 = corner_grad(P[BA + 1], yf, z1);
+                        g6 = corner_grad(P[AB + 1], y1, z1);
+                        g7 = corner_grad(P[BB + 1], y1, z1);
+                    }
+                    const float xf = O::sub(xv, fx);
+                    const float u = fade<O>(xf);
+                    const float x1 = O::sub(xf, 1.0f);
+                    const float l00 = lerp<O>(u, corner_value(g0, xf), corner_value(g1, x1));
+                    const float l10 = lerp<O>(u, corner_value(g2, xf), corner_value(g3, x1));
+                    const float l01 = lerp<O>(u, corner_value(g4, xf), corner_value(g5, x1));
+                    const float l11 = lerp<O>(u, corner_value(g6, xf), corner_value(g7, x1));
+                    const float n = lerp<O>(wz, lerp<O>(v, l00, l10), lerp<O>(v, l01, l11));
+                    sum[r] = O::add(sum[r], O::mul(amp, n));
+                }
+            }
+            amp = O::mul(amp, f.gain);
+            freq = O::mul(freq, f.lacunarity);
+        }
+        const uint64_t row = (uint64_t(k) * b.N[1] + j) * b.N[0] + i0;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+            if (uint32_t(r) < cnt)
+            {
+                const uint32_t q = quantise<O>(sum[r], full);
+                if (u16)
+                    reinterpret_cast<uint16_t*>(dst)[row + r] = uint16_t(q);
+                else
+                    dst[row + r] = uint8_t(q);
+            }
     }
 }
 
@@ -288,9 +410,11 @@ lv_status launch_fbm_bricks(lv_ctx* ctx, const lv_volume_info& info, const lv_fb
     for (uint32_t first = 0; first < n; first += 65535u)
     {
         const uint32_t cnt = std::min(65535u, n - first);
-        const uint32_t voxels = info.max_block[0] * info.max_block[1] * info.max_block[2];
-        const dim3 grid(std::min(64u, (voxels + 255u) / 256u), cnt);
-        fbm_brick_kernel<<<grid, 256, 0, s>>>(info, f, d_perm, d_ids + first,
+        constexpr int R = 8;
+        const uint32_t runs =
+            (info.max_block[0] + R - 1) / R * info.max_block[1] * info.max_block[2];
+        const dim3 grid(std::min(64u, (runs + 255u) / 256u), cnt);
+        fbm_brick_kernel<R><<<grid, 256, 0, s>>>(info, f, d_perm, d_ids + first,
                                                d_offsets ? d_offsets + first : nullptr,
                                                d_offsets ? out : out + first * brick_bytes,
                                                brick_bytes);

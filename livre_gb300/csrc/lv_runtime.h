@@ -334,6 +334,9 @@ struct lv_volume
      * requests are never evicted (empty until a server uses the volume) */
     std::vector<uint16_t> pins;
     uint32_t time_step = 0;
+    /* the last synchronous frame streamed bricks: the next one likely will
+     * too, so it waits for its miss count before queueing the ray cast */
+    bool streamed_last = false;
     /* pinned staging ring for callback sources: 2 * fetch_threads buffers
      * (at least 4), one group fetching while the previous one copies */
     std::vector<lv::PinnedBuffer*> staging;

@@ -1394,7 +1394,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         /* The residency pass's miss count goes to the host while the rest of
          * the frame is already queued behind it; the host waits for the
          * count only. A frame that missed bricks streams them and renders
-         * again (the first ray cast lacked them). */
+         * again (the first ray cast lacked them), unless its volume streamed
+         * in the previous frame too: then the ray cast is queued only after
+         * the count is known. */
         uint32_t* hc = R.h_counters.as<uint32_t>();
         st = resolve();
         if (st != LV_OK)
@@ -1402,12 +1404,20 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
                                      cudaMemcpyDeviceToHost, s));
         LV_CUDA(ctx, cudaEventRecord(R.resolve_done, s));
-        st = after_resolve();
-        if (st != LV_OK)
-            return st;
+        /* a volume that streamed last frame likely misses again: then the
+         * ray cast waits for the streaming instead of running twice */
+        const bool queued = !vol->streamed_last;
+        if (queued)
+        {
+            st = after_resolve();
+            if (st != LV_OK)
+                return st;
+        }
         LV_CUDA(ctx, cudaEventSynchronize(R.resolve_done));
         const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
-        if (missing)
+        if (!missing && !queued)
+            st = after_resolve();
+        else if (missing)
         {
             LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
                                          sizeof(uint64_t) * missing,
@@ -1423,8 +1433,12 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             /* resolve again with the streamed bricks; what still misses
              * (pool too small) is not rendered */
             st = frame_tail();
-            R.launches += tail_launches;
+            if (queued)
+                R.launches += tail_launches;
+            else
+                R.launches += 1; /* one more residency pass */
         }
+        vol->streamed_last = R.stats.n_uploaded > 0;
     }
     else if (!multi)
         st = frame_tail();
