@@ -237,7 +237,9 @@ __global__ void __launch_bounds__(256)
     for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_runs;
          w += gridDim.x * blockDim.x)
     {
-        const uint32_t rx = w % runs_x, j = (w / runs_x) % b.N[1], k = w / (runs_x * b.N[1]);
+        /* neighbouring lanes take the same x run of neighbouring rows, so a
+         * warp's lanes change x cell at the same voxel (no divergence) */
+        const uint32_t j = w % b.N[1], rx = (w / b.N[1]) % runs_x, k = w / (runs_x * b.N[1]);
         const uint32_t i0 = rx * R;
         const uint32_t cnt = min(uint32_t(R), b.N[0] - i0);
         const int32_t gj = clampi(b.base[1] + int32_t(j), b.last[1]);
