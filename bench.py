@@ -47,7 +47,7 @@ CONFIGS = {
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=64)
+    p.add_argument("--steps", type=int, default=512)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="plain2048", choices=sorted(CONFIGS))
@@ -242,7 +242,7 @@ def batched_mode(ctx, args, dev, seed=7):
     ctx.last_stats()
     # plain: one lv_render per view
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * len(items))]
-    reps = max(2, args.steps // 16)
+    reps = min(4, max(2, args.steps // 16))
     plain_ms = []
     for r in range(reps + 1):
         for i, (v, t, d, o) in enumerate(items):
