@@ -45,3 +45,54 @@ def test_plugin_volume_renders_like_the_oracle(gpu_ctx, oracle, checker_plugin, 
             assert err <= TOL, (k, err)
     tf.close()
     v.close()
+
+
+def test_cpp_host_renders_a_plugin_volume(gpu_ctx, checker_plugin, tmp_path):
+    """A C++ program drives the C ABI alone (plugins, URI, lv_render, PNG), in
+    its own process; its frame equals the frame rendered here, byte for byte."""
+    import os
+    import shutil
+    import subprocess
+    import livre_gb300 as lv
+    from livre_gb300 import _abi
+    from test_png import read_png
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    if shutil.which("g++") is None or not os.path.isdir(os.path.join(cuda, "include")):
+        pytest.skip("needs g++ and the CUDA headers")
+    libdir = os.path.dirname(_abi.LIB_PATH)
+    here = os.path.dirname(os.path.abspath(__file__))
+    exe = str(tmp_path / "render_check")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror",
+                        "-I", os.path.join(os.path.dirname(here), "include"),
+                        "-I", os.path.join(cuda, "include"),
+                        os.path.join(here, "plugins", "render_check.cpp"), "-o", exe,
+                        "-L", libdir, "-llivre_gb300", "-Wl,-rpath," + libdir,
+                        "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                        "-Wl,-rpath," + os.path.join(cuda, "lib64")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    W, H = 96, 72
+    v = gpu_ctx.open_volume(CHECKER)
+    mv, proj = lv.orbit_camera(2, 8, v.info.world_size, W, H, radius_scale=1.3)
+    tf_rgba = lv.gaussian_peaks_tf(256, seed=5)
+    view = tmp_path / "view.bin"
+    # the camera as lv_render_desc holds it (lv.make_camera's layout)
+    np.concatenate([np.asarray(mv, np.float32).reshape(16),
+                    np.asarray(proj, np.float32).reshape(16),
+                    tf_rgba.ravel()]).astype(np.float32).tofile(view)
+    png = tmp_path / "frame.png"
+    plugins_dir = str(checker_plugin[0])
+    r = subprocess.run([exe, plugins_dir, CHECKER, str(view), str(W), str(H), str(png)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("visible ")
+    tf = gpu_ctx.transfer_function(tf_rgba)
+    img = gpu_ctx.render(v, tf, gpu_ctx.render_desc(mv, proj, W, H, sse=1.0,
+                                                    early_exit=0.999))
+    mine = gpu_ctx.to_rgba8(img).cpu().numpy()
+    theirs = read_png(png.read_bytes())[::-1]  # the file is top row first
+    assert theirs.shape == (H, W, 4)
+    assert (theirs[..., 3] > 0).any()
+    np.testing.assert_array_equal(theirs, mine)
+    tf.close()
+    v.close()
