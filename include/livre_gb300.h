@@ -651,7 +651,8 @@ lv_status lv_frame_to_rgba8(lv_ctx* ctx, const float* d_rgba, uint32_t width,
 lv_status lv_frame_encode_png(const uint8_t* rgba8, uint32_t width, uint32_t height,
                               uint8_t* out, size_t capacity, size_t* size);
 /* An RGBA32F device frame converted like lv_frame_to_rgba8 and written to
- * `path` as PNG. Synchronous. */
+ * `path` as PNG. Synchronous: waits for the device (work queued on any
+ * stream, such as the frame's own ray cast) first. */
 lv_status lv_frame_write_png(lv_ctx* ctx, const float* d_rgba, uint32_t width,
                              uint32_t height, const char* path);
 

@@ -129,6 +129,9 @@ extern "C" lv_status lv_frame_write_png(lv_ctx* ctx, const float* d_rgba, uint32
     const size_t n = size_t(width) * height;
     lv::DeviceBuffer d8;
     LV_CUDA(ctx, cudaSetDevice(ctx->device));
+    /* the frame may still be rendering on any stream (lv_render returns with
+     * its ray cast queued; batches render on their own streams) */
+    LV_CUDA(ctx, cudaDeviceSynchronize());
     LV_CUDA(ctx, d8.reserve(n * 4));
     lv_status st = lv_frame_to_rgba8(ctx, d_rgba, width, height, d8.as<uint8_t>(), nullptr);
     if (st != LV_OK)
