@@ -55,6 +55,9 @@ def parse():
     p.add_argument("--cpu-rows", type=int, default=12)
     p.add_argument("--pool-gib", type=int, default=None,
                    help="brick pool size (default: the config's)")
+    p.add_argument("--ooc-voxels", type=int, default=8192,
+                   help="out-of-core volume edge (a smaller one for ncu captures)")
+    p.add_argument("--ooc-pool-gib", type=int, default=64)
     p.add_argument("--ooc-frames", type=int, default=16,
                    help="frames of the 128-frame out-of-core fly-through to render")
     p.add_argument("--modes", default="plain,batched,served,outofcore",
@@ -408,8 +411,8 @@ def outofcore_mode(local, args, dev):
     import torch
     import livre_gb300 as lv
     W, H, n_path = 1920, 1080, 128
-    ctx = lv.Context(local, pool_bytes=64 << 30)
-    vi = lv.VolumeInformation(8192, 128, 1, dtype=lv.DT_UINT16)
+    ctx = lv.Context(local, pool_bytes=args.ooc_pool_gib << 30)
+    vi = lv.VolumeInformation(args.ooc_voxels, 128, 1, dtype=lv.DT_UINT16)
     vol = ctx.fbm_volume(vi, 3, octaves=6, frequency=8.0, placement=lv.FBM_DEVICE)
     tf = ctx.transfer_function(lv.gaussian_peaks_tf(4096, seed=12))
     out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
@@ -425,12 +428,14 @@ def outofcore_mode(local, args, dev):
         rows.append((time.perf_counter() - t0, st))
     timed = rows[1:]  # frame 0 fills the empty pool
     wall = np.array([r[0] for r in timed]) * 1e3
+    n = args.ooc_voxels
     res = {
-        "workload": "outofcore_8192c_u16_128b_1080p_flythrough128",
-        "volume": "8192^3 u16 fBm (6 octaves), 128^3 bricks + overlap 1, 1 TiB logical",
+        "workload": "outofcore_%dc_u16_128b_1080p_flythrough128" % n,
+        "volume": "%d^3 u16 fBm (6 octaves), 128^3 bricks + overlap 1, %.0f GiB logical"
+                  % (n, 2.0 * n ** 3 / 2 ** 30),
         "generator": "device fBm, bit-identical to the host generator a data-source "
                      "plugin runs (host generation: ~0.3 s per brick on 16 cores)",
-        "pool_gib": 64, "frames": frames, "timed_frames": len(timed),
+        "pool_gib": args.ooc_pool_gib, "frames": frames, "timed_frames": len(timed),
         "frames_per_s": float(len(timed) / (wall.sum() / 1e3)),
         "p50_ms": float(np.percentile(wall, 50)), "p99_ms": float(np.percentile(wall, 99)),
         "first_frame_ms": rows[0][0] * 1e3,
