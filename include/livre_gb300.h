@@ -467,6 +467,15 @@ typedef struct lv_ctx_totals
 } lv_ctx_totals;
 lv_status lv_get_totals(lv_ctx* ctx, lv_ctx_totals* out);
 
+/* The histogram a view's frame feeds the transfer-function editor
+ * (HistogramFilter::execute, livre/lib/pipeline/HistogramFilter.cpp:77-149):
+ * lv_histogram of the bricks of the last lv_render frame whose world-box
+ * centre projects into the rect it rendered (the frame's borders pushed out
+ * to infinity, edges half-open), so the histograms of the sort-first tiles
+ * of a frame add up to the whole frame's. Waits for the frame. */
+lv_status lv_frame_histogram(lv_ctx* ctx, uint32_t n_bins, float range_lo, float range_hi,
+                             uint64_t* accumulated);
+
 /* Statistics of the last lv_render / lv_render_batch call (synchronises with
  * its stream). */
 lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out);

@@ -718,6 +718,15 @@ class Context:
         c = _abi.RenderLaunch(kind, tile_w, tile_h, samples_per_check, order, lookahead)
         check(lib().lv_set_render_launch(self.handle, C.byref(c)), self.handle)
 
+    def frame_histogram(self, n_bins=256, data_range=(0.0, 255.0)):
+        """Histogram of the last frame's bricks whose centre projects into the
+        rendered rect (HistogramFilter's per-view histogram)."""
+        acc = np.zeros(n_bins, np.uint64)
+        check(lib().lv_frame_histogram(self.handle, n_bins, float(data_range[0]),
+                                       float(data_range[1]),
+                                       acc.ctypes.data_as(C.POINTER(C.c_uint64))), self.handle)
+        return acc
+
     def totals(self):
         """Running totals of lv_render (frames, bricks and bytes streamed,
         launches) without waiting for the device."""

@@ -188,6 +188,8 @@ _SIGNATURES = {
                             C.c_void_p]),
     "lv_last_stats": (C.c_int, [C.c_void_p, P(FrameStats)]),
     "lv_get_totals": (C.c_int, [C.c_void_p, P(CtxTotals)]),
+    "lv_frame_histogram": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float, C.c_float,
+                                     P(C.c_uint64)]),
     "lv_batch_create": (C.c_int, [C.c_void_p, P(C.c_void_p)]),
     "lv_batch_destroy": (None, [C.c_void_p]),
     "lv_batch_set_config": (C.c_int, [C.c_void_p, P(BatchConfig)]),

@@ -229,6 +229,9 @@ struct Renderer
     lv_frame_stats stats{};
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
+    /* the last frame's volume (null once destroyed) and description */
+    lv_volume* last_vol = nullptr;
+    lv_render_desc last_desc{};
     /* async mode: misses of the previous frame, copied back */
     cudaEvent_t pending_event = nullptr;
     lv_volume* pending_vol = nullptr;

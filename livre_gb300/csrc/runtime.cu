@@ -21,6 +21,7 @@
 #include <chrono>
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <list>
 #include <map>
 #include <functional>
@@ -901,6 +902,8 @@ extern "C" void lv_volume_destroy(lv_volume* v)
         drop_volume_residency(ctx, v);
         if (ctx->renderer && ctx->renderer->pending_vol == v)
             ctx->renderer->pending_vol = nullptr;
+        if (ctx->renderer && ctx->renderer->last_vol == v)
+            ctx->renderer->last_vol = nullptr;
     }
     if (v->user_free)
         v->user_free(v->user);
@@ -1465,6 +1468,8 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     LV_CUDA(ctx, cudaEventRecord(R.frame_done, s));
     R.last_stream = s;
     R.have_last = true;
+    R.last_vol = vol;
+    R.last_desc = *desc;
     ++ctx->totals.frames;
     ctx->totals.bricks_uploaded += R.stats.n_uploaded;
     ctx->totals.bytes_uploaded += R.stats.bytes_uploaded;
@@ -1479,6 +1484,72 @@ extern "C" lv_status lv_get_totals(lv_ctx* ctx, lv_ctx_totals* out)
     std::lock_guard<std::mutex> lock(ctx->mutex);
     *out = ctx->totals;
     return LV_OK;
+}
+
+extern "C" lv_status lv_frame_histogram(lv_ctx* ctx, uint32_t n_bins, float range_lo,
+                                       float range_hi, uint64_t* accumulated)
+{
+    if (!ctx || !accumulated)
+        return LV_EINVAL;
+    std::vector<uint64_t> ids;
+    lv_volume* vol = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mutex);
+        if (!ctx->renderer || !ctx->renderer->have_last || !ctx->renderer->last_vol)
+            return fail(ctx, LV_EINVAL, "no frame rendered (or its volume is gone)");
+        Renderer& R = *ctx->renderer;
+        LV_CUDA(ctx, cudaSetDevice(ctx->device));
+        LV_CUDA(ctx, cudaStreamSynchronize(R.last_stream));
+        vol = R.last_vol;
+        const lv_render_desc& d = R.last_desc;
+        /* the frame's bricks: every pass's of a multi-pass frame, else the
+         * rendering set (entries dropped for an ancestor are invalid ids) */
+        std::vector<uint64_t> set;
+        if (R.passes)
+        {
+            const uint64_t* hp = R.h_pass.as<uint64_t>();
+            set.assign(hp, hp + R.h_counters.as<uint32_t>()[FC_WORDS + LV_SEL_WRITTEN]);
+        }
+        else
+        {
+            const uint32_t n = std::min<uint32_t>(R.h_counters.as<uint32_t>()[FC_RENDERED],
+                                                  uint32_t(R.visible_capacity));
+            set.resize(n);
+            if (n)
+                LV_CUDA(ctx, cudaMemcpy(set.data(), R.render_ids.ptr, sizeof(uint64_t) * n,
+                                        cudaMemcpyDeviceToHost));
+        }
+        /* HistogramFilter::isCenterInViewport (HistogramFilter.cpp:44-76): a
+         * brick counts when its centre projects into the rendered rect, the
+         * frame's own borders pushed out to infinity; half-open, so a centre
+         * on an edge two rects share counts in one of them */
+        const bool whole = !(d.rect[2] && d.rect[3]);
+        const uint32_t x0 = whole ? 0 : d.rect[0], y0 = whole ? 0 : d.rect[1];
+        const uint32_t w = whole ? d.width : d.rect[2], h = whole ? d.height : d.rect[3];
+        const float inf = std::numeric_limits<float>::infinity();
+        const float xlo = x0 == 0 ? -inf : 2.0f * float(x0) / float(d.width) - 1.0f;
+        const float xhi = x0 + w == d.width ? inf : 2.0f * float(x0 + w) / float(d.width) - 1.0f;
+        const float ylo = y0 == 0 ? -inf : 2.0f * float(y0) / float(d.height) - 1.0f;
+        const float yhi = y0 + h == d.height ? inf : 2.0f * float(y0 + h) / float(d.height) - 1.0f;
+        const float* mv = d.camera.modelview;
+        const float* pj = d.camera.projection;
+        for (uint64_t id : set)
+        {
+            if (id == kInvalidNode)
+                continue;
+            float c[3], e[4], q[4];
+            node_centre(vol->info, id, c);
+            for (int r = 0; r < 4; ++r)
+                e[r] = mv[r] * c[0] + mv[4 + r] * c[1] + mv[8 + r] * c[2] + mv[12 + r];
+            for (int r = 0; r < 4; ++r)
+                q[r] = pj[r] * e[0] + pj[4 + r] * e[1] + pj[8 + r] * e[2] + pj[12 + r] * e[3];
+            const float nx = q[0] / q[3], ny = q[1] / q[3];
+            if (nx >= xlo && nx < xhi && ny >= ylo && ny < yhi)
+                ids.push_back(id);
+        }
+    }
+    return lv_histogram(vol, ids.data(), uint32_t(ids.size()), n_bins, range_lo, range_hi,
+                        nullptr, accumulated);
 }
 
 extern "C" lv_status lv_last_stats(lv_ctx* ctx, lv_frame_stats* out)

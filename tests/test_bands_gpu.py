@@ -93,3 +93,32 @@ def test_batched_bands(gpu_ctx, queue):
     batch.close()
     vol.close()
     tf.close()
+
+
+def test_band_histograms_add_up_to_the_frame(gpu_ctx, oracle):
+    """HistogramFilter's per-view histogram: every brick of the frame counts
+    once over the whole frame, and the bands' histograms add up to it."""
+    import numpy as np
+    import livre_gb300 as lv
+    from livre_gb300 import replicas
+    vi, vol, tf, mv, proj = scene(gpu_ctx, lv)
+    W, H = 77, 53
+    gpu_ctx.render(vol, tf, gpu_ctx.render_desc(mv, proj, W, H, sse=1.0))
+    whole = gpu_ctx.frame_histogram(64, (0.0, 255.0))
+    ovol = oracle.volume(128, 32, 1)
+    ids, _ = oracle.select_visible(ovol, mv, proj, H, 1.0)
+    np.testing.assert_array_equal(whole, vol.histogram([int(i) for i in ids], 64, (0.0, 255.0)))
+    for world in (2, 3, 4):
+        total = np.zeros(64, np.uint64)
+        nonempty = 0
+        for r in range(world):
+            y0, rows = replicas.band(H, r, world)
+            gpu_ctx.render(vol, tf, gpu_ctx.render_desc(mv, proj, W, H, sse=1.0,
+                                                         rect=(0, y0, W, rows)))
+            part = gpu_ctx.frame_histogram(64, (0.0, 255.0))
+            nonempty += int(part.sum() > 0)
+            total += part
+        np.testing.assert_array_equal(total, whole)
+        assert nonempty >= 2  # the bricks split between bands
+    vol.close()
+    tf.close()
