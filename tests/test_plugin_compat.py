@@ -113,3 +113,37 @@ def test_unregistered_source_is_not_found(native):
     assert L.lv_unregister_source(hp, op) == _abi.LV_OK
     assert L.lv_unregister_source(hp, op) == _abi.LV_ENOTFOUND
     assert L.lv_register_source(None, op, None, None) == _abi.LV_EINVAL
+
+
+def test_host_datasource_built_in_sources(native, tmp_path):
+    """lv_source_open without a device: mem:// bricks (the known answer of
+    MemoryDataSource::computeData) and a raw:// file read back as written."""
+    import math
+    import livre_gb300 as lv
+    with lv.DataSource("mem://?datatype=uint16#256,256,256,32") as src:
+        assert src.info.depth == 4 and src.info.max_block == (40, 40, 40)
+        n = lv.NodeId(2, (1, 2, 3), 9)
+        b = n.id.to_bytes(8, "little")
+        want = int(float((b[0] ^ b[1] ^ b[2] ^ b[3]) + 16) + 127.0 * math.sin((9 + 1) / 200.0))
+        assert (src.get_data(n).view(np.uint16) == want).all()
+    data = (np.arange(12 * 10 * 8, dtype=np.uint32) * 7919 % 65536).astype(np.uint16)
+    path = tmp_path / "ramp.raw"
+    data.tofile(path)
+    with lv.DataSource("raw://%s#12,10,8,uint16" % path) as src:
+        assert src.info.voxels == (12, 10, 8) and src.info.depth == 1
+        assert (src.get_data(lv.NodeId(0, (0, 0, 0))).view(np.uint16) == data).all()
+    with lv.DataSource(str(tmp_path / "ramp.raw") + "#12,10,8,uint16") as src:
+        assert src.info.voxels == (12, 10, 8)  # no scheme: a .raw path
+
+
+def test_source_errors(native, tmp_path):
+    import livre_gb300 as lv
+    with pytest.raises(lv.LivreError):
+        lv.DataSource("nosuchscheme://volume")
+    with pytest.raises(lv.LivreError):
+        lv.DataSource("raw://%s#4,4,4" % (tmp_path / "missing.raw"))
+    with pytest.raises(lv.LivreError):
+        lv.DataSource("mem://?datatype=complex64")
+    with pytest.raises(lv.LivreError):
+        lv.load_plugins(str(tmp_path), pattern="(unbalanced")
+    assert lv.load_plugins(str(tmp_path / "does-not-exist")) == 0
