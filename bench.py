@@ -449,6 +449,17 @@ def outofcore_mode(local, args, dev):
         "select_ms_mean": float(np.mean([r[1]["select_ms"] for r in timed])),
         "stream_ms_mean": float(np.mean([r[1]["stream_ms"] for r in timed])),
     }
+    if not args.no_cpu_baseline:
+        # the CPU restatement of the reference's LOD selection (one thread, as
+        # on the reference's render thread) on frame 1's camera
+        from oracle import pyoracle as O
+        ovol = O.volume(args.ooc_voxels, 128, 1)
+        mv, proj = fly_through(1, n_path, W, H)
+        t0 = time.perf_counter()
+        ids, visited = O.select_visible(ovol, mv, proj, H, 1.0)
+        res["cpu_lod_select_ms"] = 1e3 * (time.perf_counter() - t0)
+        res["cpu_lod_visited"] = int(visited)
+        res["gpu_lod_visible_equal"] = int(len(ids)) == int(rows[1][1]["n_visible"])
     vol.close()
     tf.close()
     ctx.close()
@@ -620,7 +631,7 @@ def gb300_arm(args, cfg):
     if world == 1 and not args.no_cpu_baseline:
         sec, t_lod, t_rows = cpu_frame_estimate(cfg, k=0, rows=args.cpu_rows)
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "frames/s", "cores": os.cpu_count(),
-                                "kind": "port",
+                                "kind": "port", "lod_select_ms": 1e3 * t_lod,
                                 "sample": "frame 0: FP32 LOD selection (1 thread, %.3f s) + FP64 "
                                           "ray cast of %d evenly spaced rows on all threads "
                                           "(%.2f s), extrapolated to %d rows"
