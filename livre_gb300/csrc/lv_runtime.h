@@ -164,6 +164,14 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                         uint32_t n_views, uint32_t max_depth,
                         cudaStream_t stream);
 
+/* The launch the ray cast of V really uses under L (other voxel types than
+ * uint8 / uint16 always use one CTA per tile). */
+lv_render_launch effective_launch(const RayView& V, const lv_render_launch& L);
+/* lv_render's tile order for V under L, computed on `side` into the
+ * renderer's tile scratch (null for raster order or the per-pixel grid). */
+lv_status prepare_frame_order(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                              cudaStream_t side, const uint32_t*& order);
+
 /* Kernels run_selection launches for n views of an octree of `depth` levels. */
 uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth);
 
@@ -245,6 +253,13 @@ struct Renderer
     cudaEvent_t frame_done = nullptr;
     /* the residency pass's counters have reached the host */
     cudaEvent_t resolve_done = nullptr;
+    /* work a frame needs from the camera alone (the tile order, clearing
+     * the leaf grid) runs on `side` while the selection runs: `fork` is
+     * recorded before the selection, `join` after the side work */
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    const uint32_t* pre_order = nullptr; /* this frame's tile order (or null) */
+    bool leaf_cleared = false;           /* the side stream cleared the leaf grid */
     /* timing of the last frame: selection and ray cast */
     cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
     uint32_t launches = 0;

@@ -1542,15 +1542,62 @@ uint8_t* render_order_scratch(lv_ctx* ctx, const RayView& V, const lv_render_lau
     return buf.as<uint8_t>();
 }
 
+} // namespace
+
+lv_render_launch effective_launch(const RayView& V, const lv_render_launch& L)
+{
+    if (V.dtype == LV_DT_UINT8 || V.dtype == LV_DT_UINT16)
+        return L;
+    lv_render_launch T = L;
+    T.kind = LV_LAUNCH_TILE_GRID;
+    const uint32_t px = T.tile_w * T.tile_h;
+    if (px == 0 || px > 256 || px % 32 != 0)
+    {
+        T.tile_w = 8;
+        T.tile_h = 16;
+    }
+    return T;
+}
+
+lv_status prepare_frame_order(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                              cudaStream_t side, const uint32_t*& order)
+{
+    order = nullptr;
+    const lv_render_launch T = effective_launch(V, L);
+    if (T.kind == LV_LAUNCH_GRID || T.order != LV_ORDER_LONGEST_FIRST)
+        return LV_OK;
+    lv_status st = LV_OK;
+    uint8_t* scratch = render_order_scratch(ctx, V, T, st);
+    if (st != LV_OK)
+        return st;
+    order = tile_order(ctx, V, T, scratch, side, st);
+    return st;
+}
+
+namespace
+{
+/* The tile order of a launch: the one lv_render computed ahead for this
+ * frame on its side stream (scratch == nullptr: lv_render's own scratch),
+ * else computed now on `s` (null for raster order). */
+const uint32_t* frame_order(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
+                            uint8_t* scratch, cudaStream_t s, lv_status& st)
+{
+    st = LV_OK;
+    if (!scratch && ctx->renderer->pre_order)
+        return ctx->renderer->pre_order;
+    if (!scratch)
+        scratch = render_order_scratch(ctx, V, L, st);
+    if (st != LV_OK)
+        return nullptr;
+    return tile_order(ctx, V, L, scratch, s, st);
+}
+
 template <int DT, int F, int EDGE>
 lv_status refill_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                           cudaStream_t s)
 {
     lv_status st = LV_OK;
-    uint8_t* scratch = render_order_scratch(ctx, V, L, st);
-    if (st != LV_OK)
-        return st;
-    const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+    const uint32_t* order = frame_order(ctx, V, L, nullptr, s, st);
     if (st != LV_OK)
         return st;
     auto k = raycast_refill_kernel<DT, F, EDGE>;
@@ -1569,11 +1616,7 @@ lv_status tiles_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& 
                          cudaStream_t s, uint8_t* scratch)
 {
     lv_status st = LV_OK;
-    if (!scratch)
-        scratch = render_order_scratch(ctx, V, L, st);
-    if (st != LV_OK)
-        return st;
-    const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+    const uint32_t* order = frame_order(ctx, V, L, scratch, s, st);
     if (st != LV_OK)
         return st;
     const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);
@@ -1590,14 +1633,7 @@ template <int F, int EDGE>
 lv_status any_type_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& L,
                             cudaStream_t s, uint8_t* scratch)
 {
-    lv_render_launch T = L;
-    T.kind = LV_LAUNCH_TILE_GRID;
-    const uint32_t px = T.tile_w * T.tile_h;
-    if (px == 0 || px > 256 || px % 32 != 0)
-    {
-        T.tile_w = 8;
-        T.tile_h = 16;
-    }
+    const lv_render_launch T = effective_launch(V, L);
     return T.lookahead ? tiles_dispatch<kDtAny, F, EDGE, 1>(ctx, V, T, s, scratch)
                        : tiles_dispatch<kDtAny, F, EDGE, 0>(ctx, V, T, s, scratch);
 }
@@ -1609,11 +1645,7 @@ lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launc
     if (L.kind == LV_LAUNCH_WARP_TILES)
     {
         lv_status st = LV_OK;
-        if (!scratch)
-            scratch = render_order_scratch(ctx, V, L, st);
-        if (st != LV_OK)
-            return st;
-        const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+        const uint32_t* order = frame_order(ctx, V, L, scratch, s, st);
         if (st != LV_OK)
             return st;
         auto k = raycast_warp_tiles_kernel<DT, F, EDGE, LA>;
@@ -1630,11 +1662,7 @@ lv_status plain_dispatch_la(lv_ctx* ctx, const RayView& V, const lv_render_launc
     if (L.kind == LV_LAUNCH_TILE_QUEUE)
     {
         lv_status st = LV_OK;
-        if (!scratch)
-            scratch = render_order_scratch(ctx, V, L, st);
-        if (st != LV_OK)
-            return st;
-        const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+        const uint32_t* order = frame_order(ctx, V, L, scratch, s, st);
         if (st != LV_OK)
             return st;
         auto k = raycast_queue_kernel<DT, F, EDGE, LA>;
@@ -1662,11 +1690,7 @@ lv_status tiles_nx_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launc
                             cudaStream_t s, uint8_t* scratch)
 {
     lv_status st = LV_OK;
-    if (!scratch)
-        scratch = render_order_scratch(ctx, V, L, st);
-    if (st != LV_OK)
-        return st;
-    const uint32_t* order = tile_order(ctx, V, L, scratch, s, st);
+    const uint32_t* order = frame_order(ctx, V, L, scratch, s, st);
     if (st != LV_OK)
         return st;
     const uint32_t tiles = ((V.W + L.tile_w - 1) / L.tile_w) * ((V.H + L.tile_h - 1) / L.tile_h);

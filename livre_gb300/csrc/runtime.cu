@@ -142,6 +142,9 @@ lv_status ensure_renderer(lv_ctx* ctx)
     cudaEventCreateWithFlags(&r->upload_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->frame_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->resolve_done, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->join, cudaEventDisableTiming);
+    cudaStreamCreateWithFlags(&r->side, cudaStreamNonBlocking);
     cudaEventCreate(&r->t_sel0);
     cudaEventCreate(&r->t_sel1);
     cudaEventCreate(&r->t_ray0);
@@ -656,6 +659,9 @@ extern "C" void lv_ctx_destroy(lv_ctx* ctx)
         cudaEventDestroy(ctx->renderer->upload_event);
         cudaEventDestroy(ctx->renderer->frame_done);
         cudaEventDestroy(ctx->renderer->resolve_done);
+        cudaEventDestroy(ctx->renderer->fork);
+        cudaEventDestroy(ctx->renderer->join);
+        cudaStreamDestroy(ctx->renderer->side);
         cudaEventDestroy(ctx->renderer->t_sel0);
         cudaEventDestroy(ctx->renderer->t_sel1);
         cudaEventDestroy(ctx->renderer->t_ray0);
@@ -1122,6 +1128,15 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
      * stream) comes first */
     if (R.have_last)
         LV_CUDA(ctx, cudaStreamWaitEvent(s, R.frame_done, 0));
+    /* the side stream's work for this frame may start from here */
+    LV_CUDA(ctx, cudaEventRecord(R.fork, s));
+    R.pre_order = nullptr;
+    R.leaf_cleared = false;
+    struct ClearOrder
+    {
+        Renderer& r;
+        ~ClearOrder() { r.pre_order = nullptr; }
+    } clear_order{R};
     /* async: bricks missed by the previous frame are streamed now */
     if (!desc->synchronous)
     {
@@ -1233,6 +1248,15 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                        R.counters.as<uint32_t>(), V);
     if (st != LV_OK)
         return st;
+    /* from the camera alone, beside the selection: the longest-first tile
+     * order and the cleared leaf grid; the leaf fill waits for both */
+    LV_CUDA(ctx, cudaStreamWaitEvent(R.side, R.fork, 0));
+    LV_CUDA(ctx, cudaMemsetAsync(R.leaf.ptr, 0xFF, cells * sizeof(uint32_t), R.side));
+    st = prepare_frame_order(ctx, V, ctx->launch, R.side, R.pre_order);
+    if (st != LV_OK)
+        return st;
+    LV_CUDA(ctx, cudaEventRecord(R.join, R.side));
+    R.leaf_cleared = true;
     /* residency pass, leaf grid and ray cast. The synchronous mode reads the
      * residency pass's miss count back while the rest runs, streams any
      * misses and renders again, and returns without waiting for the ray
@@ -1251,7 +1275,15 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         return launch_resolve(ctx, RV, s);
     };
     auto after_resolve = [&]() -> lv_status {
-        LV_CUDA(ctx, cudaMemsetAsync(R.leaf.ptr, 0xFF, cells * sizeof(uint32_t), s));
+        /* the first leaf fill of the frame waits for the side stream; a later
+         * one (a frame rendered again, a later pass) clears the grid itself */
+        if (R.leaf_cleared)
+        {
+            LV_CUDA(ctx, cudaStreamWaitEvent(s, R.join, 0));
+            R.leaf_cleared = false;
+        }
+        else
+            LV_CUDA(ctx, cudaMemsetAsync(R.leaf.ptr, 0xFF, cells * sizeof(uint32_t), s));
         lv_status t = launch_leaf_fill(ctx, RV, s);
         if (t != LV_OK)
             return t;
