@@ -41,7 +41,9 @@ struct Group
     std::vector<uint32_t> views;
     uint32_t items = 0; /* work items (tiles) of the group's views */
 };
-constexpr int kGroups = 8;
+constexpr int kGroups = lv::kBatchGroups;
+/* streams the per-view kernels of a batch spread over */
+constexpr uint32_t kViewStreams = 8;
 
 /* byte offsets of one view's device regions */
 struct ViewSlots
@@ -63,10 +65,10 @@ struct lv_batch
     uint32_t order_cap = 0;
     /* one stream per non-first group: the groups' persistent launches run
      * side by side, so one group's last tiles overlap the next group */
-    cudaStream_t aux[8] = {};
-    cudaStream_t aux_low[8] = {}; /* lowest priority: a batch overlapping another */
+    cudaStream_t aux[kGroups] = {};
+    cudaStream_t aux_low[kGroups] = {}; /* lowest priority: a batch overlapping another */
     bool low_priority = false;
-    cudaEvent_t fork = nullptr, join[8] = {};
+    cudaEvent_t fork = nullptr, join[kGroups] = {};
     /* per-view kernels: tile-order scratch and ray-cast timing */
     lv::DeviceBuffer view_scratch;
     cudaEvent_t t_vk0 = nullptr, t_vk1 = nullptr;
@@ -126,7 +128,7 @@ struct lv_batch
             cudaEventDestroy(t_vk0);
         if (t_vk1)
             cudaEventDestroy(t_vk1);
-        for (int g = 0; g < 8; ++g)
+        for (int g = 0; g < kGroups; ++g)
         {
             if (join[g])
                 cudaEventDestroy(join[g]);
@@ -368,7 +370,7 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n, uint3
         if (st != LV_OK)
             return st;
         tfn_max = std::max(tfn_max, bv.tf->n);
-        const int variant = kernel_variant(V.dtype, V.filter, V.edge);
+        const int variant = batch_group(V);
         if (variant < kGroups)
             groups[variant].views.push_back(i);
         else if (b->cfg.queue != LV_QUEUE_VIEW_KERNELS)
@@ -482,7 +484,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         }
         LV_CUDA(ctx, cudaEventRecord(b->t_vk0, s));
         LV_CUDA(ctx, cudaEventRecord(b->fork, s));
-        const uint32_t n_streams = std::min<uint32_t>(n, kGroups);
+        const uint32_t n_streams = std::min<uint32_t>(n, kViewStreams);
         for (uint32_t k = 0; k < n_streams; ++k)
             LV_CUDA(ctx, cudaStreamWaitEvent(aux[k], b->fork, 0));
         for (uint32_t i = 0; i < n; ++i)

@@ -285,6 +285,12 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
                         uint32_t* leaf, uint32_t* counters, RayView& V);
 /* Index of the ray-cast kernel instantiation for a view. */
 int kernel_variant(uint32_t dtype, uint32_t filter, uint32_t edge);
+/* Kernel groups of a batch's persistent queues: kernel_variant's 0..7, and
+ * 8..13 for trilinear uint8 / uint16 bricks of pitch 34, 66 or 130 (the
+ * pitch as immediates); >= kBatchGroups: a voxel type only the per-view
+ * kernels render. */
+constexpr int kBatchGroups = 14;
+int batch_group(const RayView& V);
 /* Per-view completion of a batch of per-view kernels (LV_QUEUE_VIEW_KERNELS):
  * called on a CUDA host-function thread once view `view`'s image is written,
  * with its counter words (FrameCounter words, then the selection result).

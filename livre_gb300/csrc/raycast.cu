@@ -529,6 +529,7 @@ struct RayState
     float tg, thi;
     float kf;            /* index of the next sample (exact in FP32 below 2^24) */
     float kf_safe;       /* samples up to this index stay in the current brick */
+    uint32_t err;        /* FC_ERROR value to report when the ray ends (0: none) */
     float4 dst;
     uint32_t entry;      /* leaf entry of the current brick (or empty cell) */
     const uint8_t* brick;
@@ -558,6 +559,7 @@ __device__ __forceinline__ bool ray_begin(const RayGeom& g, float step, RayState
     r.tg = g.tg;
     r.thi = g.thi;
     r.kf_safe = -1.0f;
+    r.err = 0u;
     r.entry = kLeafEmpty;
     r.brick = nullptr;
     return true;
@@ -604,7 +606,9 @@ __device__ __forceinline__ bool locate(const RayView& V, RayState& r, float step
     if (entry != kLeafEmpty && ((entry & kLeafSlotMask) + V.brick_units > V.pool_units ||
                                 (entry >> kLeafSlotBits) > V.Lf))
     {
-        atomicExch(&V.counters[FC_ERROR], 3u); /* entry outside the pool */
+        /* entry outside the pool: reported when the ray ends, so that the
+         * sample loop stores nothing to memory */
+        r.err = 3u;
         entry = kLeafEmpty;
     }
     r.entry = entry;
@@ -759,6 +763,13 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     return !(r.dst.w > V.early);
 }
 
+/* A ray has ended: report an index check it failed. */
+__device__ __forceinline__ void flush_error(const RayView& V, const RayState& r)
+{
+    if (r.err)
+        atomicExch(&V.counters[FC_ERROR], r.err);
+}
+
 /* Colour a ray starts from: the frame so far in a later pass of a
  * multi-pass frame (RenderPipeline.cpp:92-158 composites every pass into
  * the same render texture), else transparent black. */
@@ -786,6 +797,7 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
         while (ray_step<DT, FILTER, TFS, EDGE>(V, r, step, ac, nsamp))
         {
         }
+        flush_error(V, r);
         return r.dst;
     }
     Taps<FILTER> T0;
@@ -799,6 +811,7 @@ __device__ float4 march(const RayView& V, const RayGeom& g, float step,
         s0 = s1;
         T0 = T1;
     }
+    flush_error(V, r);
     return r.dst;
 }
 
@@ -1349,6 +1362,7 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
                 {
                     active = false;
                     V.out[frame_index(V, px, py)] = r.dst;
+                    flush_error(V, r);
                     break;
                 }
     }
@@ -1722,13 +1736,20 @@ lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& 
     return plain_dispatch_la<DT, F, EDGE, 0>(ctx, V, L, s, scratch);
 }
 
-/* combination index: dtype (u8 0 / u16 1), filter, edge */
+/* combination index (batch_group): 0..7 dtype (u8 0 / u16 1), filter,
+ * edge; 8..13 trilinear bricks of pitch 34 / 66 / 130 (u8, then u16) */
 template <int TFS>
 lv_status persistent_by_index(int idx, lv_ctx* ctx, const RayView* d, const TileQueue& Q,
                               uint32_t ctas, size_t smem, cudaStream_t s)
 {
     switch (idx)
     {
+    case 8: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 34>(ctx, d, Q, ctas, smem, s);
+    case 9: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 66>(ctx, d, Q, ctas, smem, s);
+    case 10: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 130>(ctx, d, Q, ctas, smem, s);
+    case 11: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 34>(ctx, d, Q, ctas, smem, s);
+    case 12: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 66>(ctx, d, Q, ctas, smem, s);
+    case 13: return persistent_dispatch<LV_DT_UINT16, 1, TFS, 130>(ctx, d, Q, ctas, smem, s);
     case 0: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 0>(ctx, d, Q, ctas, smem, s);
     case 1: return persistent_dispatch<LV_DT_UINT8, 0, TFS, 1>(ctx, d, Q, ctas, smem, s);
     case 2: return persistent_dispatch<LV_DT_UINT8, 1, TFS, 0>(ctx, d, Q, ctas, smem, s);
@@ -1743,6 +1764,11 @@ lv_status persistent_by_index(int idx, lv_ctx* ctx, const RayView* d, const Tile
 lv_status refill_views_by_index(int idx, lv_ctx* ctx, const RayView* d, const TileQueue& Q,
                                 uint32_t ctas, uint32_t checks, cudaStream_t s)
 {
+    /* the fixed-pitch groups take the general trilinear kernels */
+    if (idx >= 8 && idx <= 10)
+        idx = 2;
+    else if (idx >= 11 && idx <= 13)
+        idx = 6;
     switch (idx)
     {
     case 0: return refill_views_dispatch<LV_DT_UINT8, 0, 0>(ctx, d, Q, ctas, checks, s);
@@ -1760,6 +1786,17 @@ lv_status refill_views_by_index(int idx, lv_ctx* ctx, const RayView* d, const Ti
 size_t tile_order_bytes(const RayView& V, const lv_render_launch& L)
 {
     return order_bytes_of(V, L);
+}
+
+int batch_group(const RayView& V)
+{
+    const int v = kernel_variant(V.dtype, V.filter, V.edge);
+    if (v >= 8 || V.filter != LV_FILTER_TRILINEAR || V.edge != 0 || V.N[0] != V.N[1])
+        return v < 8 ? v : kBatchGroups + v;
+    const int pitch = V.N[0] == 34 ? 0 : V.N[0] == 66 ? 1 : V.N[0] == 130 ? 2 : -1;
+    if (pitch < 0)
+        return v;
+    return 8 + (V.dtype == LV_DT_UINT16 ? 3 : 0) + pitch;
 }
 
 /* 0..7: uint8 / uint16 x filter x edge; 8..11: the other voxel types x
