@@ -71,9 +71,9 @@ def parse():
 
 
 # DRAM bytes (read + write) of one ray-cast launch of the 2048^3 / 1080p
-# orbit, measured by ncu on a GB300 (18.63 MB read, 0.13 MB written: the
+# orbit, measured by ncu on a GB300 (18.64 MB read, 0.08 MB written: the
 # visible bricks once; the 8-byte-per-sample gather is served by L1/L2).
-RAYCAST_DRAM_BYTES_PER_LAUNCH = 18.76e6
+RAYCAST_DRAM_BYTES_PER_LAUNCH = 18.72e6
 
 
 def transfer_function(cfg):
