@@ -609,19 +609,19 @@ uint32_t fused_grid(lv_ctx* ctx)
 }
 } // namespace
 
-uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth)
+uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth, bool allow_fused)
 {
-    return n_views == 1 && fused_grid(ctx) ? 1u : depth + 2u;
+    return allow_fused && n_views == 1 && fused_grid(ctx) ? 1u : depth + 2u;
 }
 
 lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                         uint32_t n_views, uint32_t max_depth,
-                        cudaStream_t stream)
+                        cudaStream_t stream, bool allow_fused)
 {
     SelectScratch& S = ctx->sel;
     if (S.frontier_capacity == 0)
         return fail(ctx, LV_EINVAL, "selection scratch not reserved");
-    const uint32_t grid = n_views == 1 ? fused_grid(ctx) : 0u;
+    const uint32_t grid = allow_fused && n_views == 1 ? fused_grid(ctx) : 0u;
     if (grid)
     {
         /* one view: one cooperative launch, its constants a kernel parameter */

@@ -58,10 +58,12 @@ struct DeviceBuffer
     }
 };
 
-/* Owning page-locked host buffer that only grows. */
+/* Owning page-locked host buffer that only grows. It is mapped into the
+ * device's address space: kernels may write it through `dev`. */
 struct PinnedBuffer
 {
     void* ptr = nullptr;
+    void* dev = nullptr;
     size_t bytes = 0;
     PinnedBuffer() = default;
     PinnedBuffer(const PinnedBuffer&) = delete;
@@ -72,6 +74,7 @@ struct PinnedBuffer
         if (ptr)
             cudaFreeHost(ptr);
         ptr = nullptr;
+        dev = nullptr;
         bytes = 0;
     }
     cudaError_t reserve(size_t n)
@@ -79,12 +82,20 @@ struct PinnedBuffer
         if (n <= bytes)
             return cudaSuccess;
         release();
-        cudaError_t e = cudaHostAlloc(&ptr, n < 256 ? 256 : n, cudaHostAllocDefault);
-        if (e == cudaSuccess)
-            bytes = n < 256 ? 256 : n;
-        else
+        cudaError_t e = cudaHostAlloc(&ptr, n < 256 ? 256 : n, cudaHostAllocMapped);
+        if (e != cudaSuccess)
+        {
             ptr = nullptr;
-        return e;
+            return e;
+        }
+        e = cudaHostGetDevicePointer(&dev, ptr, 0);
+        if (e != cudaSuccess)
+        {
+            release();
+            return e;
+        }
+        bytes = n < 256 ? 256 : n;
+        return cudaSuccess;
     }
     template <class T>
     T* as() const
@@ -162,7 +173,7 @@ lv_status make_lod_view(lv_ctx* ctx, const lv_volume_info& vol,
  * The device frontier holds at most `frontier_capacity` nodes per level. */
 lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
                         uint32_t n_views, uint32_t max_depth,
-                        cudaStream_t stream);
+                        cudaStream_t stream, bool allow_fused = true);
 
 /* The launch the ray cast of V really uses under L (other voxel types than
  * uint8 / uint16 always use one CTA per tile). */
@@ -173,7 +184,8 @@ lv_status prepare_frame_order(lv_ctx* ctx, const RayView& V, const lv_render_lau
                               cudaStream_t side, const uint32_t*& order);
 
 /* Kernels run_selection launches for n views of an octree of `depth` levels. */
-uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth);
+uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth,
+                            bool allow_fused = true);
 
 /* Enqueues the selection kernels for n views whose constants are already
  * on the device (capturable: no host synchronisation). */
@@ -260,6 +272,13 @@ struct Renderer
     cudaEvent_t fork = nullptr, join = nullptr;
     const uint32_t* pre_order = nullptr; /* this frame's tile order (or null) */
     bool leaf_cleared = false;           /* the side stream cleared the leaf grid */
+    /* the selection runs on its own high-priority stream once the previous
+     * frame's residency pass has read the visible list (`visible_free`), so
+     * a frame queued while the previous one still ray casts selects beside
+     * it; `sel_done` orders the rest of the frame after it */
+    cudaStream_t sel_stream = nullptr;
+    cudaEvent_t sel_done = nullptr, visible_free = nullptr;
+    bool visible_free_recorded = false;
     /* timing of the last frame: selection and ray cast */
     cudaEvent_t t_sel0 = nullptr, t_sel1 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
     uint32_t launches = 0;

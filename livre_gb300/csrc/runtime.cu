@@ -57,6 +57,27 @@ __global__ void scatter_kernel(int32_t* __restrict__ table,
         table[pairs[2 * i]] = int32_t(pairs[2 * i + 1]);
 }
 
+/* Copies a few result words into mapped page-locked host memory. A frame's
+ * counters reach the host this way rather than by a copy-engine transfer: a
+ * small copy queued behind a large one (the application's copy of the last
+ * frame, say) would hold up the stream, and with it the frame's ray cast,
+ * until the large one ends. */
+__global__ void words_to_host_kernel(const uint32_t* __restrict__ src, uint32_t* dst, uint32_t n)
+{
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        dst[i] = src[i];
+    __threadfence_system();
+}
+
+lv_status words_to_host(lv_ctx* ctx, const void* d_src, const PinnedBuffer& host,
+                        size_t word_offset, uint32_t n, cudaStream_t s)
+{
+    words_to_host_kernel<<<1, 32, 0, s>>>(static_cast<const uint32_t*>(d_src),
+                                          static_cast<uint32_t*>(host.dev) + word_offset, n);
+    LV_CUDA(ctx, cudaGetLastError());
+    return LV_OK;
+}
+
 __global__ void fill_i32_kernel(int32_t* p, uint64_t n, int32_t v)
 {
     for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
@@ -145,6 +166,13 @@ lv_status ensure_renderer(lv_ctx* ctx)
     cudaEventCreateWithFlags(&r->fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->join, cudaEventDisableTiming);
     cudaStreamCreateWithFlags(&r->side, cudaStreamNonBlocking);
+    {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        cudaStreamCreateWithPriority(&r->sel_stream, cudaStreamNonBlocking, greatest);
+    }
+    cudaEventCreateWithFlags(&r->sel_done, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->visible_free, cudaEventDisableTiming);
     cudaEventCreate(&r->t_sel0);
     cudaEventCreate(&r->t_sel1);
     cudaEventCreate(&r->t_ray0);
@@ -662,6 +690,9 @@ extern "C" void lv_ctx_destroy(lv_ctx* ctx)
         cudaEventDestroy(ctx->renderer->fork);
         cudaEventDestroy(ctx->renderer->join);
         cudaStreamDestroy(ctx->renderer->side);
+        cudaStreamDestroy(ctx->renderer->sel_stream);
+        cudaEventDestroy(ctx->renderer->sel_done);
+        cudaEventDestroy(ctx->renderer->visible_free);
         cudaEventDestroy(ctx->renderer->t_sel0);
         cudaEventDestroy(ctx->renderer->t_sel1);
         cudaEventDestroy(ctx->renderer->t_ray0);
@@ -1195,26 +1226,52 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     LV.capacity = uint32_t(std::min<uint64_t>(R.visible_capacity, 0xFFFFFFFFu));
     LV.result = R.sel_result.as<uint32_t>();
     /* kernels: the selection (one cooperative launch, or roots + one per
-     * level + finish), resolve, prune (asynchronous mode only), leaf fill,
-     * ray cast (+ tile keys and order when longest first); a synchronous
-     * frame that streams misses resolves once more */
+     * level + finish) and the copy of its result words to the host; then
+     * resolve, the copy of its counters (synchronous mode) or prune
+     * (asynchronous mode), leaf fill, ray cast (+ tile keys and order when
+     * longest first) and the final copy of the counters. A synchronous frame
+     * that streams misses resolves once more, and leaf fills and ray casts
+     * again if its first ray cast was already queued. */
     const lv_render_launch& RL = ctx->launch;
-    const uint32_t tail_launches =
-        3u + (desc->synchronous ? 0u : 1u) +
-        (RL.kind != LV_LAUNCH_GRID && RL.order == LV_ORDER_LONGEST_FIRST ? 2u : 0u);
-    R.launches = selection_launches(ctx, 1, info.depth) + tail_launches;
-    LV_CUDA(ctx, cudaEventRecord(R.t_sel0, s));
-    st = run_selection(ctx, &LV, 1, info.depth, s);
+    const uint32_t order_launches =
+        RL.kind != LV_LAUNCH_GRID && RL.order == LV_ORDER_LONGEST_FIRST ? 2u : 0u;
+    const uint32_t tail_launches = 3u + 1u + order_launches + 1u;
+    /* the selection waits only for the previous frame's residency pass; while
+     * that frame may still ray cast, the one-launch cooperative form (whose
+     * CTAs must all be resident at once) gives way to the per-level form */
+    cudaStream_t ss = R.sel_stream;
+    bool overlap = false;
+    if (R.have_last)
+    {
+        const cudaError_t q = cudaEventQuery(R.frame_done);
+        overlap = q == cudaErrorNotReady;
+        if (q != cudaSuccess)
+            cudaGetLastError(); /* not ready is no error */
+    }
+    /* a frame queued behind one still in flight selects once that frame's
+     * residency pass is done; otherwise in stream order */
+    overlap = overlap && R.visible_free_recorded;
+    LV_CUDA(ctx, cudaStreamWaitEvent(ss, overlap ? R.visible_free : R.fork, 0));
+    R.launches = selection_launches(ctx, 1, info.depth, !overlap) + 1u + tail_launches;
+    LV_CUDA(ctx, cudaEventRecord(R.t_sel0, ss));
+    st = run_selection(ctx, &LV, 1, info.depth, ss, !overlap);
     if (st != LV_OK)
         return st;
-    LV_CUDA(ctx, cudaEventRecord(R.t_sel1, s));
+    LV_CUDA(ctx, cudaEventRecord(R.t_sel1, ss));
     if (!(lod.range[0] == 0.0f && lod.range[1] == 1.0f))
     {
         st = range_slice(ctx, info, lod.range, R.visible.as<uint64_t>(),
-                         R.sel_result.as<uint32_t>(), s);
+                         R.sel_result.as<uint32_t>(), ss);
         if (st != LV_OK)
             return st;
     }
+    /* the frame's selection words for lv_last_stats, copied now: the next
+     * frame's selection may overwrite them before this frame ends */
+    st = words_to_host(ctx, R.sel_result.ptr, R.h_counters, FC_WORDS, LV_SELECT_RESULT_WORDS, ss);
+    if (st != LV_OK)
+        return st;
+    LV_CUDA(ctx, cudaEventRecord(R.sel_done, ss));
+    LV_CUDA(ctx, cudaStreamWaitEvent(s, R.sel_done, 0));
 
     /* 2. residency */
     ResolveView RV;
@@ -1272,7 +1329,13 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     };
     auto resolve = [&]() -> lv_status {
         LV_CUDA(ctx, cudaMemsetAsync(R.counters.ptr, 0, sizeof(uint32_t) * FC_WORDS, s));
-        return launch_resolve(ctx, RV, s);
+        const lv_status t = launch_resolve(ctx, RV, s);
+        if (t != LV_OK)
+            return t;
+        /* the next frame's selection may overwrite the visible list now */
+        LV_CUDA(ctx, cudaEventRecord(R.visible_free, s));
+        R.visible_free_recorded = true;
+        return LV_OK;
     };
     auto after_resolve = [&]() -> lv_status {
         /* the first leaf fill of the frame waits for the side stream; a later
@@ -1401,7 +1464,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         agg.n_passes = passes;
         R.pass_stats = agg;
         R.passes = passes;
-        R.launches = selection_launches(ctx, 1, info.depth) + passes * (1u + tail_launches);
+        /* per pass: a residency pass, then resolve, leaf fill and ray cast */
+        R.launches = selection_launches(ctx, 1, info.depth, !overlap) + 1u + order_launches +
+                     passes * 4u;
         return LV_OK;
     };
     R.passes = 0;
@@ -1436,8 +1501,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         st = resolve();
         if (st != LV_OK)
             return st;
-        LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
-                                     cudaMemcpyDeviceToHost, s));
+        st = words_to_host(ctx, R.counters.ptr, R.h_counters, 0, FC_WORDS, s);
+        if (st != LV_OK)
+            return st;
         LV_CUDA(ctx, cudaEventRecord(R.resolve_done, s));
         /* a volume that streamed last frame likely misses again: then the
          * ray cast waits for the streaming instead of running twice */
@@ -1469,7 +1535,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
              * (pool too small) is not rendered */
             st = frame_tail();
             if (queued)
-                R.launches += tail_launches;
+                R.launches += 3u;
             else
                 R.launches += 1; /* one more residency pass */
         }
@@ -1480,13 +1546,14 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     if (st != LV_OK)
         return st;
 
-    /* 5. copy back counters (+ misses in async mode) */
-    uint32_t* hc = R.h_counters.as<uint32_t>();
-    LV_CUDA(ctx, cudaMemcpyAsync(hc, R.counters.ptr, sizeof(uint32_t) * FC_WORDS,
-                                 cudaMemcpyDeviceToHost, s));
-    LV_CUDA(ctx, cudaMemcpyAsync(hc + FC_WORDS, R.sel_result.ptr,
-                                 sizeof(uint32_t) * LV_SELECT_RESULT_WORDS,
-                                 cudaMemcpyDeviceToHost, s));
+    /* 5. copy back counters (+ misses in async mode); the selection words
+     * were copied after the selection */
+    if (!multi)
+    {
+        st = words_to_host(ctx, R.counters.ptr, R.h_counters, 0, FC_WORDS, s);
+        if (st != LV_OK)
+            return st;
+    }
     if (!desc->synchronous)
     {
         LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
