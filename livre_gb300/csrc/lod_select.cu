@@ -213,12 +213,14 @@ __device__ __forceinline__ void level_items(const LodView* __restrict__ views,
                                             uint64_t* __restrict__ out_ids,
                                             uint32_t* __restrict__ out_view,
                                             uint32_t* __restrict__ out_count, uint32_t capacity,
-                                            uint32_t* __restrict__ overflow)
+                                            uint32_t* __restrict__ overflow,
+                                            bool block_only = false)
 {
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t lt = lanemask_lt();
-    for (uint32_t base = blockIdx.x * blockDim.x; base < n;
-         base += gridDim.x * blockDim.x)
+    const uint32_t first = block_only ? 0u : blockIdx.x * blockDim.x;
+    const uint32_t stride = block_only ? blockDim.x : gridDim.x * blockDim.x;
+    for (uint32_t base = first; base < n; base += stride)
     {
         const uint32_t i = base + threadIdx.x;
         const bool active = i < n;
@@ -319,6 +321,7 @@ __global__ void lod_finish_kernel(const LodView* __restrict__ views,
  * bar[2] an error flag set when a wait gives up (kSpinLimit polls); the
  * words are zeroed before the launch, with the level counters. */
 constexpr uint32_t kSpinLimit = 1u << 22; /* ~0.3 s of 64 ns sleeps */
+constexpr uint32_t kSoloItems = 1024;     /* frontier one CTA visits alone */
 
 __device__ __forceinline__ void grid_barrier(uint32_t* bar)
 {
@@ -360,25 +363,55 @@ __global__ void __launch_bounds__(256)
 {
     uint32_t* overflow = counts + kMaxLevels + 1;
     uint32_t* bar = counts + kMaxLevels + 2;
+    uint32_t* solo_end = counts + kMaxLevels + 5;
     const LodView* views = &V;
     const uint32_t rx = V.root_blocks[0], ry = V.root_blocks[1], rz = V.root_blocks[2];
-    const uint32_t n_roots = rx * ry * rz;
+    const uint32_t n_roots = min(rx * ry * rz, capacity);
+    /* Levels whose frontier is small are visited by CTA 0 alone, separated
+     * by block barriers; the other CTAs wait at one grid barrier until the
+     * frontier outgrows a CTA (or the selection ends). */
+    const bool solo = n_roots <= kSoloItems;
     if (blockIdx.x == 0)
     {
         if (threadIdx.x == 0)
-            counts[0] = min(n_roots, capacity);
+            counts[0] = n_roots;
         if (threadIdx.x < LV_SELECT_RESULT_WORDS)
             V.result[threadIdx.x] = 0u;
     }
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < min(n_roots, capacity);
-         i += gridDim.x * blockDim.x)
+    if (!solo || blockIdx.x == 0)
+        for (uint32_t i = (solo ? 0u : blockIdx.x * blockDim.x) + threadIdx.x; i < n_roots;
+             i += solo ? blockDim.x : gridDim.x * blockDim.x)
+        {
+            const uint32_t x = i / (ry * rz), y = (i / rz) % ry, z = i % rz;
+            ids0[i] = nid_make(0, x, y, z, V.time_step);
+            view0[i] = 0u;
+        }
+    uint32_t l = 0;
+    if (solo)
     {
-        const uint32_t x = i / (ry * rz), y = (i / rz) % ry, z = i % rz;
-        ids0[i] = nid_make(0, x, y, z, V.time_step);
-        view0[i] = 0u;
+        if (blockIdx.x == 0)
+        {
+            __syncthreads();
+            for (; l < max_depth; ++l)
+            {
+                const uint32_t n = min(__ldcg(counts + l), capacity);
+                if (n == 0 || n > kSoloItems)
+                    break; /* the same value in every thread: read after the barrier */
+                const bool even = (l & 1u) == 0;
+                level_items<true>(views, even ? ids0 : ids1, even ? view0 : view1, n,
+                                  even ? ids1 : ids0, even ? view1 : view0, counts + l + 1,
+                                  capacity, overflow, true);
+                __syncthreads();
+            }
+            if (threadIdx.x == 0)
+                *solo_end = l;
+        }
+        grid_barrier(bar);
+        l = __ldcg(solo_end);
     }
-    grid_barrier(bar);
-    for (uint32_t l = 0; l < max_depth; ++l)
+    else
+        grid_barrier(bar);
+    for (; l < max_depth; ++l)
     {
         const uint32_t n = min(__ldcg(counts + l), capacity);
         if (n == 0 || __ldcg(bar + 2))
