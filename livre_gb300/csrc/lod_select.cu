@@ -642,6 +642,22 @@ uint32_t fused_grid(lv_ctx* ctx)
 }
 } // namespace
 
+lv_status scratch_acquire(lv_ctx* ctx, SelectScratch& S, cudaStream_t s)
+{
+    if (S.free_recorded)
+        LV_CUDA(ctx, cudaStreamWaitEvent(s, S.free_event, 0));
+    return LV_OK;
+}
+
+lv_status scratch_release(lv_ctx* ctx, SelectScratch& S, cudaStream_t s)
+{
+    if (!S.free_event)
+        LV_CUDA(ctx, cudaEventCreateWithFlags(&S.free_event, cudaEventDisableTiming));
+    LV_CUDA(ctx, cudaEventRecord(S.free_event, s));
+    S.free_recorded = true;
+    return LV_OK;
+}
+
 uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth, bool allow_fused)
 {
     return allow_fused && n_views == 1 && fused_grid(ctx) ? 1u : depth + 2u;
@@ -737,6 +753,8 @@ lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaSt
     if (S.frontier_capacity >= cap)
         return LV_OK;
     LV_CUDA(ctx, cudaStreamSynchronize(s));
+    if (S.free_recorded) /* the last user may have run on another stream */
+        LV_CUDA(ctx, cudaEventSynchronize(S.free_event));
     for (int i = 0; i < 2; ++i)
     {
         LV_CUDA(ctx, S.ids[i].reserve(sizeof(uint64_t) * cap));
@@ -803,13 +821,22 @@ extern "C" lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
     st = reserve_frontier(ctx, ctx->sel, max_frontier(*vol), s);
     if (st != LV_OK)
         return st;
+    /* the scratch is the renderer's too, whose selection runs on a stream of
+     * its own */
+    st = scratch_acquire(ctx, ctx->sel, s);
+    if (st != LV_OK)
+        return st;
     st = run_selection(ctx, &V, 1, vol->depth, s);
     if (st != LV_OK)
         return st;
     const bool full = params->range[0] == 0.0f && params->range[1] == 1.0f;
     if (!full)
-        return range_slice(ctx, *vol, params->range, d_out_ids, d_result, s);
-    return LV_OK;
+    {
+        st = range_slice(ctx, *vol, params->range, d_out_ids, d_result, s);
+        if (st != LV_OK)
+            return st;
+    }
+    return scratch_release(ctx, ctx->sel, s);
 }
 
 /* ------------------------------------------------------------------------

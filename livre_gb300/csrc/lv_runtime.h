@@ -115,7 +115,24 @@ struct SelectScratch
     PinnedBuffer staging; /* host copy of the LodView array */
     uint32_t frontier_capacity = 0;
     uint32_t generation = 0; /* bumped whenever the queues are reallocated */
+    /* recorded after the last selection that used these queues, on whatever
+     * stream it ran: the next user, on any stream, waits for it */
+    cudaEvent_t free_event = nullptr;
+    bool free_recorded = false;
+    SelectScratch() = default;
+    SelectScratch(const SelectScratch&) = delete;
+    SelectScratch& operator=(const SelectScratch&) = delete;
+    ~SelectScratch()
+    {
+        if (free_event)
+            cudaEventDestroy(free_event);
+    }
 };
+
+/* Orders a selection on stream s after the previous user of the scratch
+ * (scratch_acquire), and the next user after it (scratch_release). */
+lv_status scratch_acquire(lv_ctx* ctx, SelectScratch& S, cudaStream_t s);
+lv_status scratch_release(lv_ctx* ctx, SelectScratch& S, cudaStream_t s);
 
 struct Pool;
 struct Renderer;

@@ -1252,6 +1252,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
      * residency pass is done; otherwise in stream order */
     overlap = overlap && R.visible_free_recorded;
     LV_CUDA(ctx, cudaStreamWaitEvent(ss, overlap ? R.visible_free : R.fork, 0));
+    st = scratch_acquire(ctx, ctx->sel, ss); /* after any lv_select_visible */
+    if (st != LV_OK)
+        return st;
     R.launches = selection_launches(ctx, 1, info.depth, !overlap) + 1u + tail_launches;
     LV_CUDA(ctx, cudaEventRecord(R.t_sel0, ss));
     st = run_selection(ctx, &LV, 1, info.depth, ss, !overlap);
@@ -1267,6 +1270,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     }
     /* the frame's selection words for lv_last_stats, copied now: the next
      * frame's selection may overwrite them before this frame ends */
+    st = scratch_release(ctx, ctx->sel, ss);
+    if (st != LV_OK)
+        return st;
     st = words_to_host(ctx, R.sel_result.ptr, R.h_counters, FC_WORDS, LV_SELECT_RESULT_WORDS, ss);
     if (st != LV_OK)
         return st;

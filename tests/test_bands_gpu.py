@@ -149,3 +149,45 @@ def test_frames_on_different_streams_stay_ordered(gpu_ctx):
         assert torch.equal(o, a)
     vol.close()
     tf.close()
+
+
+def test_selections_between_queued_frames(gpu_ctx):
+    """lv_render's selection and lv_select_visible share the context's
+    frontier queues and run on different streams; frames queued back to back
+    with selections of another view issued between them (on a third stream,
+    no host wait) give the frames and visible sets each gives alone."""
+    import torch
+    import livre_gb300 as lv
+    vi, vol, tf, mv, proj = scene(gpu_ctx, lv)
+    W, H = 77, 53
+    cams = [lv.orbit_camera(k, 8, vi.world_size, W, H, radius_scale=1.1 + 0.1 * k)
+            for k in range(6)]
+    descs = [gpu_ctx.render_desc(m, p, W, H, sse=1.0) for m, p in cams]
+    alone = [gpu_ctx.render(vol, tf, d).clone() for d in descs]
+    sel_cams = [lv.orbit_camera(k, 8, vi.world_size, W, H, radius_scale=2.0) for k in (1, 4)]
+    sel_alone = [sorted(gpu_ctx.select_visible(vi, m, p, H, 0.5)[0].tolist()) for m, p in sel_cams]
+    torch.cuda.synchronize()
+    other = torch.cuda.Stream()
+    outs = [torch.empty((H, W, 4), dtype=torch.float32, device="cuda") for _ in descs]
+    # the selections' buffers, made before any frame is queued (a buffer
+    # zeroed on the rendering stream would be zeroed after the frames)
+    bufs = [(torch.empty(vi.node_count(), dtype=torch.int64, device="cuda"),
+             torch.zeros(lv._abi.SELECT_RESULT_WORDS, dtype=torch.int32, device="cuda"))
+            for _ in descs]
+    torch.cuda.synchronize()
+    pending = []
+    for k, (d, o) in enumerate(zip(descs, outs)):
+        gpu_ctx.render(vol, tf, d, o)
+        m, p = sel_cams[k % 2]
+        ids, res = bufs[k]
+        pending.append((k % 2, gpu_ctx.select_visible(vi, m, p, H, 0.5, out=ids, result=res,
+                                                      stream=other, sync=False)))
+    torch.cuda.synchronize()
+    for o, a in zip(outs, alone):
+        assert torch.equal(o, a)
+    for j, (ids, res) in pending:
+        n = int(res.cpu().numpy().view("uint32")[lv._abi.SEL_WRITTEN])
+        got = sorted(ids[:n].cpu().numpy().view("uint64").tolist())
+        assert got == sel_alone[j]
+    vol.close()
+    tf.close()
