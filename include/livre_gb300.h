@@ -398,7 +398,11 @@ typedef struct lv_frame_stats
  * reference's RGBA32F render texture holds it). Replaces
  * RenderPipeline::render (livre/lib/pipeline/RenderPipeline.cpp:268-278) with
  * Renderer::render (livre/core/render/Renderer.cpp:33-47) and the
- * RayCastRenderer shaders. Returns once the frame is enqueued on `stream`. */
+ * RayCastRenderer shaders. Returns once the frame is enqueued on `stream`:
+ * the writes to d_rgba are ordered on `stream` after the caller's earlier
+ * work there. The selection, which reads and writes only the context's own
+ * buffers, runs on an internal stream; when the previous frame is still in
+ * flight it may start before the caller's work queued since that frame. */
 lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                     const lv_render_desc* desc, float* d_rgba, void* stream);
 
