@@ -687,8 +687,15 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
         uint32_t* view1 = S.view[1].as<uint32_t>();
         void* args[] = {&V, &max_depth, &ids0, &view0, &ids1, &view1, &counts,
                         const_cast<uint32_t*>(&cap)};
+        /* no level holds more nodes than the octree's widest one: a CTA more
+         * than it needs would only add an arrival to each grid barrier */
+        uint64_t widest = uint64_t(V.root_blocks[0]) * V.root_blocks[1] * V.root_blocks[2];
+        for (uint32_t l = 1; l < max_depth && widest < (uint64_t(1) << 40); ++l)
+            widest <<= 3;
+        const uint32_t used =
+            uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(grid, (widest + 255) / 256)));
         LV_CUDA(ctx, cudaLaunchCooperativeKernel(reinterpret_cast<void*>(lod_fused_kernel),
-                                                 dim3(grid), dim3(256), args, 0, stream));
+                                                 dim3(used), dim3(256), args, 0, stream));
         return LV_OK;
     }
     LV_CUDA(ctx, S.staging.reserve(sizeof(LodView) * n_views));
