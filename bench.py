@@ -433,6 +433,29 @@ def outofcore_mode(local, args, dev):
         st = ctx.last_stats()  # synchronises
         rows.append((time.perf_counter() - t0, st))
     timed = rows[1:]  # frame 0 fills the empty pool
+    # the same frames again from a purged pool, back to back with no wait
+    # between frames: each frame's misses stream beside the previous
+    # frame's ray cast
+    ctx.purge()
+    mv, proj = fly_through(0, n_path, W, H)
+    d0 = ctx.render_desc(mv, proj, W, H, sse=1.0, step_policy=lv.STEP_REFERENCE,
+                         early_exit=0.999)
+    ctx.render(vol, tf, d0, out)
+    ctx.last_stats()
+    descs = []
+    for k in range(1, frames):
+        mv, proj = fly_through(k, n_path, W, H)
+        descs.append(ctx.render_desc(mv, proj, W, H, sse=1.0, step_policy=lv.STEP_REFERENCE,
+                                     early_exit=0.999))
+    tot0 = ctx.totals()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for d in descs:
+        ctx.render(vol, tf, d, out)
+    ctx.last_stats()  # waits for the last frame; raises on a device error
+    torch.cuda.synchronize()
+    pipe_s = time.perf_counter() - t0
+    tot1 = ctx.totals()
     wall = np.array([r[0] for r in timed]) * 1e3
     n = args.ooc_voxels
     res = {
@@ -454,6 +477,10 @@ def outofcore_mode(local, args, dev):
         "raycast_ms_mean": float(np.mean([r[1]["raycast_ms"] for r in timed])),
         "select_ms_mean": float(np.mean([r[1]["select_ms"] for r in timed])),
         "stream_ms_mean": float(np.mean([r[1]["stream_ms"] for r in timed])),
+        # frames 1.. back to back (no host wait between frames), from a purged pool
+        "back_to_back_frames_per_s": len(descs) / pipe_s,
+        "back_to_back_streamed_bricks_per_frame":
+            (tot1["bricks_uploaded"] - tot0["bricks_uploaded"]) / len(descs),
     }
     if not args.no_cpu_baseline:
         # the CPU restatement of the reference's LOD selection (one thread, as

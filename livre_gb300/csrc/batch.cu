@@ -711,6 +711,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     if (!b || (n && !views))
         return fail(b ? b->ctx : nullptr, LV_EINVAL, "null argument");
     lv_ctx* ctx = b->ctx;
+    ++ctx->foreign_pool_use; /* its kernels read pool slots after it returns */
     for (uint32_t i = 0; i < n; ++i)
         if (!views[i].volume || !views[i].tf || !views[i].d_rgba || views[i].volume->ctx != ctx ||
             views[i].tf->ctx != ctx || !views[i].desc.width || !views[i].desc.height)

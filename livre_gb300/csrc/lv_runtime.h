@@ -6,6 +6,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdio>
 #include <cstring>
 #include <list>
@@ -153,6 +155,9 @@ struct lv_ctx
     /* host fetchers of callback sources (created on first use) */
     lv::HostPool* host_pool = nullptr;
     lv_ctx_totals totals{}; /* since creation, host-side (lv_get_totals) */
+    /* bumped by every pool user other than lv_render (batches, the server)
+     * whose work may still read pool slots when it returns */
+    std::atomic<uint64_t> foreign_pool_use{0};
     std::mutex mutex;
 };
 
@@ -241,6 +246,7 @@ struct Resident
     uint64_t node_idx;
     uint32_t unit;
     uint32_t units;
+    uint64_t load; /* the stream_bricks call that placed it (Pool::loads) */
 };
 
 struct Pool
@@ -250,6 +256,7 @@ struct Pool
     uint64_t bump = 0;
     std::map<uint32_t, std::vector<uint32_t>> free_by_units;
     std::list<Resident> lru; /* front = oldest load */
+    uint64_t loads = 0;      /* stream_bricks calls so far */
     uint64_t resident_bytes = 0;
     /* per slot size: resident bricks and those pinned by server requests */
     std::map<uint32_t, uint64_t> resident_count, pinned_count;
@@ -304,16 +311,28 @@ struct Renderer
     DeviceBuffer pass_count; /* visible ids of the current pass */
     uint32_t passes = 0;     /* passes of the last frame (0: one-pass frame) */
     lv_frame_stats pass_stats{}; /* summed over the passes */
+    /* a frame queued while the previous one still ray casts looks its
+     * visible bricks up beside it and streams the missing ones then */
+    DeviceBuffer probe, probe_count; /* missing visible ids, their count */
+    PinnedBuffer h_probe;
+    uint64_t foreign_seen = 0; /* lv_ctx::foreign_pool_use after the last frame */
+    /* device-generated bricks: ids and slot offsets */
+    DeviceBuffer gen;
+    PinnedBuffer h_gen;
 };
 
 
 
 /* Streams bricks `ids` of `vol` into the pool (allocate / evict bricks whose
  * node stamp is below protect_frame, fetch, copy on the upload stream,
- * publish page-table entries); `render` waits for the copies. */
+ * publish page-table entries); `render` waits for the copies. The copies
+ * wait for the work queued on `render` and for the last lv_render frame,
+ * unless `beside_frame`: the caller then guarantees that protect_frame
+ * spares every brick that queued work reads. */
 lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                         uint32_t n, uint32_t protect_frame, cudaStream_t render,
-                        uint32_t& n_loaded, uint64_t& bytes_loaded);
+                        uint32_t& n_loaded, uint64_t& bytes_loaded,
+                        bool beside_frame = false);
 lv_status ensure_renderer(lv_ctx* ctx);
 /* Ray-cast constants of one view (shared by the plain and batched paths). */
 lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,

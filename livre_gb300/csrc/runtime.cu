@@ -78,6 +78,33 @@ lv_status words_to_host(lv_ctx* ctx, const void* d_src, const PinnedBuffer& host
     return LV_OK;
 }
 
+/* The visible nodes of a frame queued while the previous frame still ray
+ * casts: the ones not resident are collected (to stream beside that ray
+ * cast), the resident ones stamped with the frame so that eviction spares
+ * them. */
+__global__ void probe_kernel(const __grid_constant__ ResolveView RV, uint64_t* __restrict__ out,
+                             uint32_t* __restrict__ out_count, uint32_t capacity)
+{
+    const uint32_t n = *RV.n_visible_ptr;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    {
+        const uint64_t id = RV.visible[i];
+        if (nid_level(id) >= RV.depth)
+            continue;
+        const uint64_t idx = node_index(RV.level_offset, RV.root_blocks, id);
+        if (idx >= RV.n_nodes)
+            continue;
+        if (RV.node_table[idx] >= 0)
+            RV.node_stamp[idx] = RV.frame;
+        else
+        {
+            const uint32_t k = atomicAdd(out_count, 1u);
+            if (k < capacity)
+                out[k] = id;
+        }
+    }
+}
+
 __global__ void fill_i32_kernel(int32_t* p, uint64_t n, int32_t v)
 {
     for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
@@ -196,7 +223,7 @@ lv_status reserve_selection(lv_ctx* ctx, const lv_volume_info& info,
 bool pool_alloc(lv_ctx* ctx, uint32_t units, uint32_t protect_frame,
                 std::unordered_map<lv_volume*, std::vector<uint32_t>>& stamps,
                 std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>>& updates,
-                uint32_t& out_unit)
+                uint32_t& out_unit, cudaStream_t stamp_stream)
 {
     Pool& P = *ctx->pool;
     auto& fl = P.free_by_units[units];
@@ -214,7 +241,9 @@ bool pool_alloc(lv_ctx* ctx, uint32_t units, uint32_t protect_frame,
     }
     for (auto it = P.lru.begin(); it != P.lru.end(); ++it)
     {
-        if (it->units != units)
+        /* a brick placed by this very call is not stamped yet, and evicting
+         * it would leave the call's page-table updates naming one node twice */
+        if (it->units != units || it->load == P.loads)
             continue;
         lv_volume* v = it->vol;
         if (protect_frame == 0xFFFFFFFFu)
@@ -234,8 +263,17 @@ bool pool_alloc(lv_ctx* ctx, uint32_t units, uint32_t protect_frame,
         if (st == stamps.end())
         {
             std::vector<uint32_t> h(v->n_nodes);
-            if (cudaMemcpy(h.data(), v->node_stamp.ptr, sizeof(uint32_t) * v->n_nodes,
-                           cudaMemcpyDeviceToHost) != cudaSuccess)
+            /* on a stream of the library's own when a frame may still run on
+             * the caller's (the legacy default stream would wait for it) */
+            if (stamp_stream)
+            {
+                if (cudaMemcpyAsync(h.data(), v->node_stamp.ptr, sizeof(uint32_t) * v->n_nodes,
+                                    cudaMemcpyDeviceToHost, stamp_stream) != cudaSuccess ||
+                    cudaStreamSynchronize(stamp_stream) != cudaSuccess)
+                    return false;
+            }
+            else if (cudaMemcpy(h.data(), v->node_stamp.ptr, sizeof(uint32_t) * v->n_nodes,
+                                cudaMemcpyDeviceToHost) != cudaSuccess)
                 return false;
             st = stamps.emplace(v, std::move(h)).first;
         }
@@ -262,12 +300,18 @@ lv_status apply_updates(
     if (updates.empty())
         return LV_OK;
     Renderer& R = *ctx->renderer;
-    std::map<lv_volume*, std::vector<int64_t>> per;
+    /* one pair per node, its last value: the scatter writes the pairs in no
+     * particular order */
+    std::map<lv_volume*, std::map<uint64_t, int32_t>> last;
     for (auto& u : updates)
-    {
-        per[u.first].push_back(int64_t(u.second.first));
-        per[u.first].push_back(int64_t(u.second.second));
-    }
+        last[u.first][u.second.first] = u.second.second;
+    std::map<lv_volume*, std::vector<int64_t>> per;
+    for (auto& kv : last)
+        for (auto& e : kv.second)
+        {
+            per[kv.first].push_back(int64_t(e.first));
+            per[kv.first].push_back(int64_t(e.second));
+        }
     size_t total = 0;
     for (auto& kv : per)
         total += kv.second.size();
@@ -315,7 +359,7 @@ HostPool* host_pool(lv_ctx* ctx)
  * fetch_threads host threads at once, while the previous group copies. */
 lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                         uint32_t n, uint32_t protect_frame, cudaStream_t render,
-                        uint32_t& n_loaded, uint64_t& bytes_loaded)
+                        uint32_t& n_loaded, uint64_t& bytes_loaded, bool beside_frame)
 {
     Renderer& R = *ctx->renderer;
     Pool& P = *ctx->pool;
@@ -324,12 +368,17 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     bytes_loaded = 0;
     if (n == 0)
         return LV_OK;
+    ++P.loads;
     /* new copies may overwrite evicted slots still read by queued work: the
      * caller's stream and the last lv_render frame (on any stream) */
-    LV_CUDA(ctx, cudaEventRecord(R.render_event, render));
-    LV_CUDA(ctx, cudaStreamWaitEvent(up, R.render_event, 0));
-    if (R.have_last)
-        LV_CUDA(ctx, cudaStreamWaitEvent(up, R.frame_done, 0));
+    if (!beside_frame)
+    {
+        LV_CUDA(ctx, cudaEventRecord(R.render_event, render));
+        LV_CUDA(ctx, cudaStreamWaitEvent(up, R.render_event, 0));
+        if (R.have_last)
+            LV_CUDA(ctx, cudaStreamWaitEvent(up, R.frame_done, 0));
+    }
+    const cudaStream_t stamp_stream = beside_frame ? R.sel_stream : nullptr;
     std::unordered_map<lv_volume*, std::vector<uint32_t>> stamps;
     std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>> updates;
     std::vector<uint64_t> gen_ids, gen_offsets;
@@ -339,7 +388,7 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     const auto place = [&](uint64_t idx, uint32_t unit) {
         vol->host_table[idx] = int32_t(unit);
         updates.push_back({vol, {idx, int32_t(unit)}});
-        P.lru.push_back(Resident{vol, idx, unit, vol->slot_units});
+        P.lru.push_back(Resident{vol, idx, unit, vol->slot_units, P.loads});
         P.resident_bytes += uint64_t(vol->slot_units) * kSlotUnit;
         ++P.resident_count[vol->slot_units];
         ++n_loaded;
@@ -385,7 +434,8 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                 if (rc[j] != 0)
                     continue;
                 uint32_t unit = 0;
-                if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit))
+                if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit,
+                                stamp_stream))
                 {
                     st = fail(ctx, LV_EAGAIN, "brick pool full of bricks in use");
                     break;
@@ -411,7 +461,8 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
             if (idx >= vol->n_nodes || vol->host_table[idx] >= 0)
                 continue;
             uint32_t unit = 0;
-            if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit))
+            if (!pool_alloc(ctx, vol->slot_units, protect_frame, stamps, updates, unit,
+                                stamp_stream))
             {
                 st = fail(ctx, LV_EAGAIN, "brick pool full of bricks in use");
                 break;
@@ -432,9 +483,12 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
         }
     if (!gen_ids.empty())
     {
-        DeviceBuffer dids;
+        /* grow-only buffers: freeing device memory would wait for the whole
+         * device, a frame still ray casting included */
+        DeviceBuffer& dids = R.gen;
+        PinnedBuffer& h = R.h_gen;
+        LV_CUDA(ctx, cudaStreamSynchronize(up)); /* the last generation read them */
         LV_CUDA(ctx, dids.reserve(sizeof(uint64_t) * 2 * gen_ids.size()));
-        PinnedBuffer h;
         LV_CUDA(ctx, h.reserve(sizeof(uint64_t) * 2 * gen_ids.size()));
         std::memcpy(h.ptr, gen_ids.data(), sizeof(uint64_t) * gen_ids.size());
         std::memcpy(h.as<uint64_t>() + gen_ids.size(), gen_offsets.data(),
@@ -451,8 +505,6 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                                      dids.as<uint64_t>() + gen_ids.size(), up);
         if (g != LV_OK)
             return g;
-        /* temporaries die at scope exit */
-        LV_CUDA(ctx, cudaStreamSynchronize(up));
     }
     lv_status u = apply_updates(ctx, updates, up);
     if (u != LV_OK)
@@ -1325,9 +1377,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
      * misses and renders again, and returns without waiting for the ray
      * cast. */
     auto timed_stream = [&](const uint64_t* ids, uint32_t n, uint32_t protect,
-                            uint32_t& loaded, uint64_t& bytes) -> lv_status {
+                            uint32_t& loaded, uint64_t& bytes, bool beside = false) -> lv_status {
         const auto t0 = std::chrono::steady_clock::now();
-        const lv_status r = stream_bricks(ctx, vol, ids, n, protect, s, loaded, bytes);
+        const lv_status r = stream_bricks(ctx, vol, ids, n, protect, s, loaded, bytes, beside);
         R.stats.stream_ms += std::chrono::duration<float, std::milli>(
                                  std::chrono::steady_clock::now() - t0)
                                  .count();
@@ -1475,6 +1527,49 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                      passes * 4u;
         return LV_OK;
     };
+    /* A frame queued while the previous one still ray casts (a fly-through
+     * rendered back to back) streams its missing bricks beside that ray cast:
+     * its visible nodes are looked up on the selection stream, and eviction
+     * spares the previous frame's bricks (stamped frame - 1 by its residency
+     * passes) as well as this frame's resident ones (stamped by the lookup),
+     * so no slot the running ray cast reads is overwritten. Only when the
+     * previous frame was a one-pass synchronous lv_render of this volume and
+     * no batch or server has used the pool since. */
+    bool prefetched = false;
+    if (overlap && desc->synchronous && R.last_desc.synchronous && R.passes == 0 &&
+        R.last_vol == vol && vol->streamed_last && frame > 1u &&
+        R.foreign_seen == ctx->foreign_pool_use.load())
+    {
+        const uint32_t cap = uint32_t(std::min<uint64_t>(R.visible_capacity, 0xFFFFFFFFu));
+        LV_CUDA(ctx, R.probe.reserve(sizeof(uint64_t) * cap));
+        LV_CUDA(ctx, R.probe_count.reserve(sizeof(uint32_t)));
+        LV_CUDA(ctx, R.h_probe.reserve(sizeof(uint64_t) * (size_t(cap) + 1)));
+        LV_CUDA(ctx, cudaMemsetAsync(R.probe_count.ptr, 0, sizeof(uint32_t), ss));
+        probe_kernel<<<256, 256, 0, ss>>>(RV, R.probe.as<uint64_t>(), R.probe_count.as<uint32_t>(),
+                                          cap);
+        LV_CUDA(ctx, cudaGetLastError());
+        ++R.launches;
+        uint32_t* hcount = R.h_probe.as<uint32_t>();
+        uint64_t* hids = R.h_probe.as<uint64_t>() + 1;
+        LV_CUDA(ctx, cudaMemcpyAsync(hcount, R.probe_count.ptr, sizeof(uint32_t),
+                                     cudaMemcpyDeviceToHost, ss));
+        LV_CUDA(ctx, cudaStreamSynchronize(ss));
+        const uint32_t n_probe = std::min(*hcount, cap);
+        if (n_probe)
+        {
+            LV_CUDA(ctx, cudaMemcpyAsync(hids, R.probe.ptr, sizeof(uint64_t) * n_probe,
+                                         cudaMemcpyDeviceToHost, ss));
+            LV_CUDA(ctx, cudaStreamSynchronize(ss));
+            uint32_t loaded = 0;
+            uint64_t bytes = 0;
+            st = timed_stream(hids, n_probe, frame - 1u, loaded, bytes, true);
+            R.stats.n_uploaded += loaded;
+            R.stats.bytes_uploaded += bytes;
+            if (st != LV_OK && st != LV_EAGAIN)
+                return st;
+            prefetched = true;
+        }
+    }
     R.passes = 0;
     bool multi = false;
     const uint64_t per_pass = ctx->pool->capacity_units / vol->slot_units;
@@ -1512,8 +1607,9 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             return st;
         LV_CUDA(ctx, cudaEventRecord(R.resolve_done, s));
         /* a volume that streamed last frame likely misses again: then the
-         * ray cast waits for the streaming instead of running twice */
-        const bool queued = !vol->streamed_last;
+         * ray cast waits for the streaming instead of running twice (unless
+         * this frame's misses were streamed beside the previous frame) */
+        const bool queued = !vol->streamed_last || prefetched;
         if (queued)
         {
             st = after_resolve();
@@ -1575,6 +1671,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     R.have_last = true;
     R.last_vol = vol;
     R.last_desc = *desc;
+    R.foreign_seen = ctx->foreign_pool_use.load();
     ++ctx->totals.frames;
     ctx->totals.bricks_uploaded += R.stats.n_uploaded;
     ctx->totals.bytes_uploaded += R.stats.bytes_uploaded;

@@ -431,6 +431,7 @@ void loop_batched(lv_server* S)
         std::vector<Req*> admitted, rejected;
         {
             std::lock_guard<std::mutex> lk(ctx->mutex);
+            ++ctx->foreign_pool_use; /* its batches read pool slots */
             admit(S, cand, admitted, rejected);
             if (!admitted.empty())
                 cudaEventRecord(S->uploads_done, S->sel_stream);
