@@ -19,6 +19,16 @@ def fly(lv, k, n, W, H):
 
 
 def make_volume(ctx, lv, placement):
+    if placement == "callback":
+        # a data-source callback (getData): bricks through the staging ring
+        import ctypes
+        vi = lv.VolumeInformation(512, 32, 1)
+
+        def get_data(node_id, dst, nbytes):
+            brick = np.random.default_rng(node_id).integers(0, 256, nbytes, dtype=np.uint8)
+            ctypes.memmove(dst, brick.ctypes.data, nbytes)
+            return True
+        return vi, ctx.callback_volume(vi, get_data)
     if placement == "blob_host":
         vi = lv.VolumeInformation(512, 32, 1)
         return vi, ctx.blob_volume(vi, 48, 5, 4, placement=lv.BLOB_HOST)
@@ -27,7 +37,8 @@ def make_volume(ctx, lv, placement):
 
 
 @pytest.mark.parametrize("placement,pool", [("blob_host", "half"), ("fbm_device", "half"),
-                                            ("blob_host", "tight"), ("fbm_device", "tight")])
+                                            ("blob_host", "tight"), ("fbm_device", "tight"),
+                                            ("callback", "half"), ("callback", "tight")])
 def test_back_to_back_frames_equal_waited_frames(native, placement, pool):
     import torch
     import livre_gb300 as lv
