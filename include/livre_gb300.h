@@ -122,7 +122,9 @@ uint32_t lv_abi_version(void);
  * reference's DFS order is restored only when the range slice needs it).
  * d_out_ids: capacity uint64 device slots; d_result: LV_SELECT_RESULT_WORDS
  * uint32 device words. Asynchronous on `stream`. Scratch (frontier queues) is
- * allocated by the context on first use and reused. */
+ * allocated by the context on first use and reused; lv_render's selection
+ * shares it, and each waits for the other's earlier use whatever the
+ * streams. */
 lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
                             const lv_camera* camera,
                             const lv_lod_params* params, uint64_t* d_out_ids,
