@@ -575,11 +575,24 @@ __device__ __forceinline__ void sample_cell_coord(const RayView& V, const RaySta
         f[a] = fmaf(fmaf(r.dir[a], t, V.eye[a]), V.gscale[a], V.goff[a]);
 }
 
+/* Leaf cell of a sample at cell coordinate f on one axis, or dims (outside
+ * the octree). The sample's parameter is in [tnearGlobal, tfarGlobal), so it
+ * lies in the volume's box: a cell index rounded one past the box's face (a
+ * sample on the entry or exit face, which the reference shader takes at
+ * tnear = tnearGlobal, fragRayCast.glsl:142-147) is the face cell. The low
+ * face is the box's on every axis (f = 0); the high face only on axes with
+ * the most cells (bm): shorter axes end inside the box, as the node boxes
+ * of LODNode.cpp:30-64 (cell side worldSize / maxBricks) do. */
+__device__ __forceinline__ uint32_t face_cell(float f, uint32_t dims, uint32_t bm)
+{
+    const uint32_t c = uint32_t(max(__float2int_rd(f), 0));
+    return dims == bm ? min(c, dims - 1u) : c;
+}
+
 /* The slow path of a sample (index r.kf, position f) that leaves the range
- * known to lie in the current brick: finds its leaf cell (floor(f) in one
- * conversion; 0 <= c < dims one unsigned compare, f is finite), the brick
- * there, and how far the ray stays in that brick. False: the sample is
- * outside the octree.
+ * known to lie in the current brick: finds its leaf cell (face_cell), the
+ * brick there, and how far the ray stays in that brick. False: the sample
+ * is outside the octree.
  *
  * The cell of a sample is monotone in its index along each axis (t, the
  * position and f are monotone single-rounding functions of it, and floor is
@@ -591,12 +604,13 @@ __device__ __forceinline__ void sample_cell_coord(const RayView& V, const RaySta
 template <int FILTER>
 __device__ __forceinline__ bool locate(const RayView& V, RayState& r, float step, const float f[3])
 {
+    const uint32_t bm = max(max(V.dims[0], V.dims[1]), V.dims[2]);
     uint32_t c[3];
     bool inside = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
     {
-        c[a] = uint32_t(__float2int_rd(f[a]));
+        c[a] = face_cell(f[a], V.dims[a], bm);
         inside = inside && c[a] < V.dims[a];
     }
     r.kf_safe = r.kf; /* this sample only, unless shown otherwise below */
@@ -659,7 +673,7 @@ __device__ __forceinline__ bool locate(const RayView& V, RayState& r, float step
 #pragma unroll
         for (int a = 0; a < 3; ++a)
         {
-            const uint32_t ca = uint32_t(__float2int_rd(g[a]));
+            const uint32_t ca = face_cell(g[a], V.dims[a], bm);
             in = in && ca < V.dims[a] && (ca >> sh) == c[a];
         }
         if (in)

@@ -504,6 +504,13 @@ void ray_setup32(const or_frustum& fr, const float* gmin, const float* gmax,
     r.t1 = std::min(std::min(tmax[0], tmax[1]), std::min(tmax[0], tmax[2]));
 }
 
+/* Whether a brick's entry parameter is the previous brick's exit: the ray
+ * crossed a face the two bricks share (diagnostics of or_raycast_px). */
+bool t_entry_face(double prev_exit, double entry)
+{
+    return std::fabs(entry - prev_exit) <= 1e-9 * std::max(1.0, std::fabs(entry));
+}
+
 /* double-precision slab test of fragRayCast.glsl:79-101 */
 bool intersect64(const double* o, const double* d, const double* bmin,
                  const double* bmax, double& t0, double& t1)
@@ -952,6 +959,17 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
                uint32_t row_begin, uint32_t row_end, double* out,
                uint64_t* n_samples_out)
 {
+    return or_raycast_px(vol, dtype, node_ids, n_nodes, bricks, tf_rgba, tf_n, view, mode,
+                         n_threads, row_begin, row_end, out, n_samples_out, nullptr,
+                         nullptr);
+}
+
+int or_raycast_px(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
+                  uint32_t n_nodes, const void* bricks, const float* tf_rgba,
+                  uint32_t tf_n, const or_view* view, int mode, int n_threads,
+                  uint32_t row_begin, uint32_t row_end, double* out,
+                  uint64_t* n_samples_out, uint32_t* px_samples, uint8_t* px_flags)
+{
     or_frustum fr;
     if (or_frustum_setup(view->mv, view->proj, &fr) != 0)
         return -2;
@@ -1084,7 +1102,15 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
             {
                 const float p = std::fmaf(r.dir[a], t, r.eye[a]);
                 f[a] = std::fmaf(p, gscale[a], goff[a]);
-                const float fl = std::floor(f[a]);
+                /* t in [tnearGlobal, tfarGlobal): the sample is in the
+                 * volume's box; a cell index rounded one past the box's face
+                 * (a sample on the entry or exit face, taken by the shader at
+                 * tnear = tnearGlobal, fragRayCast.glsl:142-147) is the face
+                 * cell. The high face is the box's only on the axes with the
+                 * most cells (node boxes: LODNode.cpp:30-64). */
+                float fl = std::max(std::floor(f[a]), 0.0f);
+                if (rs.dims[a] == bm)
+                    fl = std::min(fl, float(rs.dims[a] - 1u));
                 if (!(fl >= 0.0f) || !(fl < float(rs.dims[a])))
                     inside = false;
                 cell[a] = inside ? int32_t(fl) : 0;
@@ -1118,7 +1144,7 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
         }
     };
 
-    auto shader = [&](uint32_t px, uint32_t py, double* dst, uint64_t& cnt) {
+    auto shader = [&](uint32_t px, uint32_t py, double* dst, uint64_t& cnt, uint8_t& flags) {
         /* fragRayCast.glsl:113-207 per brick, in double precision */
         double invmv[16], invp[16];
         for (int i = 0; i < 16; ++i)
@@ -1156,6 +1182,10 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
         double tg, tgf;
         intersect64(eye, d, gmn, gmx, tg, tgf);
         const double stepd = 1.0 / double(view->n_samples);
+        /* grid index of the previous composited brick's last sample, and
+         * that brick's exit parameter (diagnostics only) */
+        int64_t prev_k = INT64_MIN;
+        double prev_tf = 0.0;
         for (uint32_t oi = 0; oi < n_nodes; ++oi)
         {
             if (dst[3] > sh.early)
@@ -1195,10 +1225,14 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
             }
             if (tn > tf)
                 continue;
-            const uint32_t L = nid_level(node_ids[n]);
-            (void)L;
+            const double t_entry = tn;
+            int64_t k_first = INT64_MIN, k_last = INT64_MIN;
             for (double t = tn; t < tf; t += stepd)
             {
+                const int64_t kg = std::llround((t - tg) / stepd);
+                if (k_first == INT64_MIN)
+                    k_first = kg;
+                k_last = kg;
                 double sv[3];
                 for (int a = 0; a < 3; ++a)
                 {
@@ -1215,6 +1249,20 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
                 if (dst[3] > sh.early)
                     break;
             }
+            if (k_first != INT64_MIN)
+            {
+                if (prev_k != INT64_MIN)
+                {
+                    if (k_first == prev_k)
+                        flags |= OR_PX_DUPLICATE;
+                    else if (k_first < prev_k)
+                        flags |= OR_PX_INVERTED;
+                    else if (k_first > prev_k + 1 && t_entry_face(prev_tf, t_entry))
+                        flags |= OR_PX_GAP;
+                }
+                prev_k = k_last;
+                prev_tf = tf;
+            }
         }
     };
 
@@ -1230,10 +1278,17 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
                 double* dst = out + (size_t(y) * W + x) * 4;
                 if (!accumulate)
                     dst[0] = dst[1] = dst[2] = dst[3] = 0.0;
+                const uint64_t before = cnt;
+                uint8_t flags = 0;
                 if (base_mode == OR_MODE_SHADER)
-                    shader(x, y, dst, cnt);
+                    shader(x, y, dst, cnt, flags);
                 else
                     per_ray(x, y, dst, cnt);
+                const size_t pi = size_t(y) * W + x;
+                if (px_samples)
+                    px_samples[pi] = uint32_t(cnt - before);
+                if (px_flags)
+                    px_flags[pi] = flags;
             }
         }
         total_samples += cnt;

@@ -157,6 +157,31 @@ int or_raycast(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
                uint32_t row_begin, uint32_t row_end, double* out_rgba,
                uint64_t* n_samples_out);
 
+/* Per-pixel diagnostics of a ray cast (either pointer may be null; both
+ * hold width*height entries, rows outside [row_begin, row_end) untouched).
+ * px_samples: samples composited on the pixel's ray.
+ * px_flags (shader mode only; 0 in per-ray mode): for each brick with at
+ * least one sample, its first sample's index on the ray's global grid
+ * (round((t - tnearGlobal) * nSamples)) against the last index of the brick
+ * composited before it:
+ *   OR_PX_DUPLICATE: equal, i.e. both bricks sampled the grid point on
+ *     their shared face (the per-brick snapping of fragRayCast.glsl:142-147
+ *     evaluated on each side of the face);
+ *   OR_PX_INVERTED: smaller, i.e. a brick nearer the eye along the ray was
+ *     composited after a farther one (the brick-centre distance order of
+ *     RayCastRenderer.cpp:57-81 is not the ray's order there);
+ *   OR_PX_GAP: larger by more than one while the previous brick's exit and
+ *     this brick's entry parameters are equal (a face grid point neither
+ *     brick sampled). */
+#define OR_PX_DUPLICATE 1u
+#define OR_PX_INVERTED 2u
+#define OR_PX_GAP 4u
+int or_raycast_px(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids,
+                  uint32_t n_nodes, const void* bricks, const float* tf_rgba,
+                  uint32_t tf_n, const or_view* view, int mode, int n_threads,
+                  uint32_t row_begin, uint32_t row_end, double* out_rgba,
+                  uint64_t* n_samples_out, uint32_t* px_samples, uint8_t* px_flags);
+
 #ifdef __cplusplus
 }
 #endif

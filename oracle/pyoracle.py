@@ -49,6 +49,11 @@ MODE_PER_RAY = 0
 MODE_SHADER = 1
 ACCUMULATE = 0x100  # flag: rays start from the colour already in `out`
 
+# per-pixel flags of raycast(..., diagnostics=True) in shader mode
+PX_DUPLICATE = 1  # a face grid point sampled by the bricks on both sides
+PX_INVERTED = 2   # a nearer brick composited after a farther one
+PX_GAP = 4        # a face grid point sampled by neither brick
+
 _lib = None
 
 
@@ -81,6 +86,7 @@ def lib():
             C.POINTER(Volume), C.c_uint32, C.POINTER(C.c_uint64), C.c_uint32, C.c_void_p,
             C.POINTER(C.c_float), C.c_uint32, C.POINTER(View), C.c_int, C.c_int,
             C.c_uint32, C.c_uint32, C.POINTER(C.c_double), C.POINTER(C.c_uint64)]
+        L.or_raycast_px.argtypes = L.or_raycast.argtypes + [C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -213,8 +219,10 @@ def make_view(mv, proj, width, height, n_samples, alpha_correction=None,
 
 
 def raycast(vol, dtype, node_ids, bricks, tf, view, mode=MODE_PER_RAY, n_threads=0,
-            rows=None, init=None):
-    """init: an image to composite behind (mode | ACCUMULATE is implied)."""
+            rows=None, init=None, diagnostics=False):
+    """init: an image to composite behind (mode | ACCUMULATE is implied).
+    diagnostics: also return per-pixel sample counts (uint32) and flags
+    (uint8, PX_* bits, shader mode only) as (image, n_samples, counts, flags)."""
     ids = np.ascontiguousarray(node_ids, np.uint64)
     bricks = np.ascontiguousarray(bricks)
     tf = np.ascontiguousarray(tf, np.float32).reshape(-1, 4)
@@ -225,10 +233,16 @@ def raycast(vol, dtype, node_ids, bricks, tf, view, mode=MODE_PER_RAY, n_threads
         mode |= ACCUMULATE
     r0, r1 = (0, view.height) if rows is None else rows
     ns = C.c_uint64()
-    rc = lib().or_raycast(C.byref(vol), dtype, ids.ctypes.data_as(C.POINTER(C.c_uint64)),
-                          len(ids), bricks.ctypes.data, _fptr(tf), tf.shape[0],
-                          C.byref(view), mode, n_threads, r0, r1,
-                          out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ns))
+    counts = np.zeros((view.height, view.width), np.uint32)
+    flags = np.zeros((view.height, view.width), np.uint8)
+    rc = lib().or_raycast_px(C.byref(vol), dtype, ids.ctypes.data_as(C.POINTER(C.c_uint64)),
+                             len(ids), bricks.ctypes.data, _fptr(tf), tf.shape[0],
+                             C.byref(view), mode, n_threads, r0, r1,
+                             out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(ns),
+                             counts.ctypes.data if diagnostics else None,
+                             flags.ctypes.data if diagnostics else None)
     if rc != 0:
         raise RuntimeError("or_raycast failed: %d" % rc)
+    if diagnostics:
+        return out, ns.value, counts, flags
     return out, ns.value

@@ -107,9 +107,11 @@ def test_nucleon_render_matches_oracle(ctx, oracle, filt):
     ref, ns = oracle.raycast(ovol, 1, [0], raw[None, :], tf_rgba, view)
     assert ns > 0
     assert np.abs(img - ref).max() <= 1.0 / 255.0
-    # one brick: the per-brick shader transcription (FP64) agrees too
-    shader, _ = oracle.raycast(ovol, 1, [0], raw[None, :], tf_rgba, view, mode=1)
-    assert np.abs(img - shader).max() <= 4.0 / 255.0
+    # one brick: the per-brick shader transcription (FP64, its own ray
+    # geometry) agrees too, sample counts within a face sample or two
+    shader, ns_shader = oracle.raycast(ovol, 1, [0], raw[None, :], tf_rgba, view, mode=1)
+    assert np.abs(img - shader).max() <= 1.0 / 255.0
+    assert abs(int(st["n_samples"]) - ns_shader) <= max(8, ns_shader // 20000)
     tf.close()
     v.close()
 
