@@ -140,9 +140,16 @@ lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
  * library (about 6.3 MB, held by every GPU that loads the library until the
  * process exits). Limits: at most 262144 nodes per octree level (larger
  * volumes return LV_ENOMEM) and range {0, 1} only (LV_EINVAL otherwise).
- * The first call on a device looks up that array's address; make it before
- * any stream capture on the device. All calls share the array: calls whose
- * work overlaps on the GPU race and must be ordered by the caller. */
+ * The first call on a device does a one-time set-up (it looks up that
+ * array's device address and the SM count); make that first call before any
+ * stream capture on the device. With CUDA's lazy module loading the array is
+ * reserved when the library's selection module first loads on a device (that
+ * first call, or the first selection of lv_render / lv_select_visible): make
+ * it before the application's allocator takes the GPU's memory. All calls
+ * share the array and it keeps the last call's contents (each call clears
+ * what must start at zero): calls whose work overlaps on the GPU race and
+ * must be ordered by the caller. An error already pending on the calling
+ * thread (cudaPeekAtLastError) returns LV_EDEVICE and is left in place. */
 lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
                                     const lv_camera* camera,
                                     const lv_lod_params* params,

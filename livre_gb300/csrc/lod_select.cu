@@ -562,22 +562,23 @@ void frustum_setup(const float* mv, const float* p, float inv_mv[16],
     }
 }
 
-lv_status make_lod_view(lv_ctx* ctx, const lv_volume_info& vol,
-                        const lv_camera& cam, const lv_lod_params& p,
-                        LodView& V)
+/* The per-view constants of a selection: LV_OK, or a status with the
+ * reason in *why. Shared by every selection entry point. */
+lv_status fill_lod_view(const lv_volume_info& vol, const lv_camera& cam,
+                        const lv_lod_params& p, LodView& V, const char** why)
 {
     if (vol.depth == 0 || vol.depth > kMaxLevels)
-        return fail(ctx, LV_EINVAL, "volume depth out of range");
+        return *why = "volume depth out of range", LV_EINVAL;
     if (p.window_height == 0)
-        return fail(ctx, LV_EINVAL, "window height is 0");
+        return *why = "window height is 0", LV_EINVAL;
     if (p.n_clip_planes > 6)
-        return fail(ctx, LV_EINVAL, "more than 6 clip planes");
+        return *why = "more than 6 clip planes", LV_EINVAL;
     float inv_mv[16], inv_p[16], lim[6], planes[6][4], eye[3], dir[3];
     bool ok = false;
     frustum_setup(cam.modelview, cam.projection, inv_mv, inv_p, lim, planes,
                   eye, dir, &ok);
     if (!ok)
-        return fail(ctx, LV_EINVAL, "singular modelview or projection");
+        return *why = "singular modelview or projection", LV_EINVAL;
     std::memset(&V, 0, sizeof(V));
     std::memcpy(V.planes, planes, sizeof(planes));
     V.nearp = lim[4];
@@ -591,7 +592,7 @@ lv_status make_lod_view(lv_ctx* ctx, const lv_volume_info& vol,
         V.half[i] = vol.world_size[i] * 0.5f;
         V.root_blocks[i] = vol.root_blocks[i];
         if (vol.max_block[i] <= 2u * vol.overlap[i])
-            return fail(ctx, LV_EINVAL, "max_block <= 2 * overlap");
+            return *why = "max_block <= 2 * overlap", LV_EINVAL;
         V.block[i] = vol.max_block[i] - 2u * vol.overlap[i];
     }
     V.n_clip = p.n_clip_planes;
@@ -601,6 +602,15 @@ lv_status make_lod_view(lv_ctx* ctx, const lv_volume_info& vol,
     V.depth = vol.depth;
     V.time_step = p.time_step;
     return LV_OK;
+}
+
+lv_status make_lod_view(lv_ctx* ctx, const lv_volume_info& vol,
+                        const lv_camera& cam, const lv_lod_params& p,
+                        LodView& V)
+{
+    const char* why = "";
+    const lv_status st = fill_lod_view(vol, cam, p, V, &why);
+    return st == LV_OK ? st : fail(ctx, st, why);
 }
 
 uint64_t max_frontier(const lv_volume_info& vol)
@@ -867,9 +877,17 @@ extern "C" lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
  *    (per-level counters, result words) on every call, but two calls whose
  *    work overlaps on the GPU (different streams, or different host threads
  *    without ordering) race on the array and give wrong results;
- *  - the first call on each device looks up the array's device address
- *    (cudaGetSymbolAddress, with that device current) and caches it; make
- *    that first call before any stream capture on the device.
+ *  - the first call on each device does a one-time set-up: it looks up the
+ *    array's device address (cudaGetSymbolAddress, with that device current)
+ *    and the SM count, and caches both; make that first call before any
+ *    stream capture on the device;
+ *  - the array is device memory of this file's module: with CUDA's lazy
+ *    module loading it is reserved when the module first loads on a device
+ *    (this call's set-up, or any selection of lv_render / lv_select_visible),
+ *    so make that first use before the application's allocator takes the
+ *    GPU's memory;
+ *  - the per-view constants reach the device as a kernel parameter (a
+ *    one-thread store into the array), so no host buffer outlives the call.
  * ---------------------------------------------------------------------- */
 namespace lv
 {
@@ -888,9 +906,11 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 std::mutex g_noalloc_mutex;
 unsigned char* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+int g_noalloc_sms[kNoAllocMaxDevices] = {};
 
-/* Device address of g_noalloc_scratch on `dev` (the current device). */
-lv_status noalloc_scratch(int dev, unsigned char** out)
+/* Device address of g_noalloc_scratch on `dev` (the current device) and the
+ * device's SM count, looked up once per device. */
+lv_status noalloc_scratch(int dev, unsigned char** out, int* sms)
 {
     if (dev < 0 || dev >= int(kNoAllocMaxDevices))
         return LV_EDEVICE;
@@ -898,53 +918,37 @@ lv_status noalloc_scratch(int dev, unsigned char** out)
     if (!g_noalloc_ptr[dev])
     {
         void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
+        int n = 0;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p ||
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            n <= 0)
         {
-            cudaGetLastError();
+            cudaGetLastError(); /* this call's own error: none was pending on entry */
             return LV_EDEVICE;
         }
+        g_noalloc_sms[dev] = n;
         g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
     }
     *out = g_noalloc_ptr[dev];
+    *sms = g_noalloc_sms[dev];
     return LV_OK;
 }
 
-/* The per-view constants of make_lod_view, with status codes only. */
-lv_status noalloc_lod_view(const lv_volume_info& vol, const lv_camera& cam,
-                           const lv_lod_params& p, LodView& V)
+/* A launch of this call failed: its error, cleared. */
+lv_status launched()
 {
-    if (vol.depth == 0 || vol.depth > kMaxLevels || p.window_height == 0 ||
-        p.n_clip_planes > 6)
-        return LV_EINVAL;
-    float inv_mv[16], inv_p[16], lim[6], planes[6][4], eye[3], dir[3];
-    bool ok = false;
-    frustum_setup(cam.modelview, cam.projection, inv_mv, inv_p, lim, planes, eye, dir, &ok);
-    if (!ok)
-        return LV_EINVAL;
-    std::memset(&V, 0, sizeof(V));
-    std::memcpy(V.planes, planes, sizeof(planes));
-    V.nearp = lim[4];
-    for (int i = 0; i < 3; ++i)
-        V.eye_near[i] = eye[i] - dir[i] * V.nearp;
-    V.wspp = (lim[3] - lim[2]) / float(p.window_height);
-    V.sse = p.screen_space_error;
-    for (int i = 0; i < 3; ++i)
-    {
-        if (vol.max_block[i] <= 2u * vol.overlap[i])
-            return LV_EINVAL;
-        V.world_size[i] = vol.world_size[i];
-        V.half[i] = vol.world_size[i] * 0.5f;
-        V.root_blocks[i] = vol.root_blocks[i];
-        V.block[i] = vol.max_block[i] - 2u * vol.overlap[i];
-    }
-    V.n_clip = p.n_clip_planes;
-    std::memcpy(V.clip, p.clip_planes, sizeof(V.clip));
-    V.min_lod = p.min_lod;
-    V.max_lod = p.max_lod;
-    V.depth = vol.depth;
-    V.time_step = p.time_step;
-    return LV_OK;
+    return cudaGetLastError() == cudaSuccess ? LV_OK : LV_EDEVICE;
+}
+
+/* Stores a selection's per-view constants, passed by value, at `dst`:
+ * the view reaches the device as a kernel parameter, not as a copy of
+ * host memory. */
+__global__ void lod_view_store_kernel(const __grid_constant__ LodView V, LodView* dst)
+{
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&V);
+    uint32_t* d = reinterpret_cast<uint32_t*>(dst);
+    for (uint32_t i = threadIdx.x; i < sizeof(LodView) / 4; i += blockDim.x)
+        d[i] = src[i];
 }
 } // namespace
 } // namespace lv
@@ -964,6 +968,10 @@ extern "C" lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
         return LV_EINVAL;
     if (max_frontier(*vol) > kNoAllocFrontier)
         return LV_ENOMEM; /* the octree needs more than the fixed scratch holds */
+    /* an error left by the caller's earlier work is not this call's: report
+     * it without clearing it */
+    if (cudaPeekAtLastError() != cudaSuccess)
+        return LV_EDEVICE;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)
     {
@@ -971,11 +979,13 @@ extern "C" lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
         return LV_EDEVICE;
     }
     unsigned char* base = nullptr;
-    lv_status st = noalloc_scratch(dev, &base);
+    int sms = 0;
+    lv_status st = noalloc_scratch(dev, &base, &sms);
     if (st != LV_OK)
         return st;
     LodView V;
-    st = noalloc_lod_view(*vol, *camera, *params, V);
+    const char* why = "";
+    st = fill_lod_view(*vol, *camera, *params, V, &why);
     if (st != LV_OK)
         return st;
     V.out_ids = d_out_ids;
@@ -991,26 +1001,22 @@ extern "C" lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
                           reinterpret_cast<uint32_t*>(base + kNoAllocViews) + kNoAllocFrontier};
     uint32_t* counts = reinterpret_cast<uint32_t*>(base + kNoAllocCounts);
     uint32_t* overflow = counts + kMaxLevels + 1;
-    /* V lives on the host stack: a copy from pageable memory has consumed it
-     * by the time cudaMemcpyAsync returns */
-    if (cudaMemcpyAsync(dview, &V, sizeof(V), cudaMemcpyHostToDevice, s) != cudaSuccess)
-    {
-        cudaGetLastError();
-        return LV_EDEVICE;
-    }
+    lod_view_store_kernel<<<1, 128, 0, s>>>(V, dview);
+    if ((st = launched()) != LV_OK)
+        return st;
     lod_roots_kernel<<<1, 128, 0, s>>>(dview, 1, ids[0], views[0], counts, kMaxLevels + 2,
                                        roots, kNoAllocFrontier, nullptr);
-    int sms = 152;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if ((st = launched()) != LV_OK)
+        return st;
     for (uint32_t l = 0; l < vol->depth; ++l)
     {
         const int in = l & 1, out = in ^ 1;
         lod_level_kernel<<<2 * sms, 256, 0, s>>>(dview, ids[in], views[in], counts + l,
                                                  ids[out], views[out], counts + l + 1,
                                                  kNoAllocFrontier, overflow);
+        if ((st = launched()) != LV_OK)
+            return st;
     }
     lod_finish_kernel<<<1, 128, 0, s>>>(dview, 1, overflow);
-    if (cudaGetLastError() != cudaSuccess)
-        return LV_EDEVICE;
-    return LV_OK;
+    return launched();
 }

@@ -49,6 +49,45 @@ def test_noalloc_matches_select_visible(native):
     ctx.close()
 
 
+def test_noalloc_capacity_lod_limits_and_clip(native):
+    """The parameters the no-allocation call takes apart from the view: a
+    capacity below the visible count (WRITTEN clamped, FOUND the full
+    count), minimum / maximum LOD and a clip plane, each equal to
+    lv_select_visible's result."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import livre_gb300 as lv
+    from livre_gb300 import _abi
+    ctx = lv.Context(0, pool_bytes=64 << 20)
+    vol = lv.VolumeInformation(1024, 32, 1)
+    mv, proj = lv.orbit_camera(5, 16, vol.world_size, 1280, 720, radius_scale=0.8)
+    res = torch.zeros(_abi.SELECT_RESULT_WORDS, dtype=torch.int32, device="cuda")
+    # capacity below the visible count
+    want, wr = ctx.select_visible(vol, mv, proj, 720, 1.0)
+    assert wr[_abi.SEL_FOUND] > 16
+    small = torch.empty(16, dtype=torch.int64, device="cuda")
+    got, r = _call_noalloc(native, _abi, vol, lv.make_camera(mv, proj), lv.make_lod(720, 1.0),
+                           small, res)
+    assert r[_abi.SEL_WRITTEN] == 16 and len(got) == 16
+    assert r[_abi.SEL_FOUND] == wr[_abi.SEL_FOUND]
+    assert set(got.tolist()) <= set(want.tolist())
+    # LOD limits and a clip plane
+    out = torch.empty(vol.node_count(), dtype=torch.int64, device="cuda")
+    clip = [(0.3, 1.0, -0.2, 0.05)]
+    for min_lod, max_lod in [(2, 3), (0, 1), (3, 3)]:
+        lod = lv.make_lod(720, 1.0, min_lod, max_lod, clip_planes=clip)
+        got, r = _call_noalloc(native, _abi, vol, lv.make_camera(mv, proj), lod, out, res)
+        want, wr = ctx.select_visible(vol, mv, proj, 720, 1.0, min_lod, max_lod,
+                                      clip_planes=clip)
+        assert len(got) > 0
+        assert got.tolist() == sorted(want.tolist()), (min_lod, max_lod)
+        assert r[_abi.SEL_FOUND] == wr[_abi.SEL_FOUND]
+        assert r[_abi.SEL_VISITED] == wr[_abi.SEL_VISITED]
+        assert r[_abi.SEL_MAX_LEVEL] == wr[_abi.SEL_MAX_LEVEL]
+    ctx.close()
+
+
 def test_noalloc_rejects_oversized_volume(native):
     import torch
     if not torch.cuda.is_available():
