@@ -15,15 +15,24 @@ metric through the public C ABI with host buffers: the brick pool starts
 empty, bricks stream host->device from a page-locked host store on a miss,
 and each frame is converted to RGBA8 and copied back to host memory.
 
+Frames: the timed steps visit orbit frames spread evenly over the whole
+64-frame orbit (step i renders frame floor(i * 64 / steps)).
+
 `--impl reference` times the CPU restatement of the reference path (the
-reference itself needs an OpenGL context and cannot run here): the FP32 LOD
-selection single-threaded as on the reference render thread, plus the FP64
-ray cast on every host thread over a bounded sample of rows of the same
-frame, extrapolated to the full frame.
+reference itself needs an OpenGL context and cannot run here): per step one
+whole frame, the FP32 LOD selection single-threaded as on the reference
+render thread plus the FP64 ray cast of every row on every host thread,
+with the host's CPU model and thread count stated.
+
+Extra keys of the default line: `plain256` (the CPU-runnable plain workload:
+256^3 uint8 in 32^3 bricks, 512x512), `parity` (device frames of both plain
+workloads against the oracle on this host: per-ray mode, shader-order mode),
+`batched`, `served`, `outofcore` (the 128-frame fly-through).
 """
 import argparse
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -52,18 +61,20 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="plain2048", choices=sorted(CONFIGS))
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-rows", type=int, default=12)
     p.add_argument("--pool-gib", type=int, default=None,
                    help="brick pool size (default: the config's)")
     p.add_argument("--ooc-voxels", type=int, default=8192,
                    help="out-of-core volume edge (a smaller one for ncu captures)")
     p.add_argument("--ooc-pool-gib", type=int, default=64)
-    p.add_argument("--ooc-frames", type=int, default=16,
+    p.add_argument("--ooc-frames", type=int, default=128,
                    help="frames of the 128-frame out-of-core fly-through to render")
-    p.add_argument("--modes", default="plain,batched,served,outofcore",
-                   help="comma list: plain (headline), batched (64 uneven views in one "
-                        "persistent launch), served (Poisson request stream), outofcore "
-                        "(8192^3 u16 fly-through through a 64 GiB pool)")
+    p.add_argument("--modes", default="plain,plain256,parity,batched,served,outofcore",
+                   help="comma list: plain (headline), plain256 (the 256^3 / 512^2 plain "
+                        "workload), parity (device frames against the oracle), batched (64 "
+                        "uneven views in one persistent launch), served (Poisson request "
+                        "stream), outofcore (8192^3 u16 fly-through through a 64 GiB pool)")
+    p.add_argument("--cpu-frames", type=int, default=2,
+                   help="whole frames the CPU baseline of the default line ray casts")
     p.add_argument("--serve-seconds", type=float, default=1.5)
     p.add_argument("--serve-rates", type=lambda t: [int(x) for x in t.split(",")],
                    default=[200, 500, 1000, 2000], help="Poisson request rates (req/s)")
@@ -139,33 +150,95 @@ class ClockSampler:
 
 
 # ------------------------------------------------------ CPU baseline
-def cpu_frame_estimate(cfg, k=0, rows=12):
-    """Seconds per frame of the CPU restatement: LOD selection (1 thread) +
-    FP64 ray cast (all threads) of `rows` evenly spaced rows, extrapolated."""
-    import concurrent.futures as cf
-    import numpy as np
-    import livre_gb300 as lv
-    from oracle import pyoracle as O
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
 
-    W, H = cfg["width"], cfg["height"]
-    ovol = O.volume(cfg["voxels"], cfg["block"], cfg["overlap"])
-    mv, proj = lv.orbit_camera(k, cfg["frames"], tuple(ovol.world_size), W, H)
-    t0 = time.perf_counter()
-    ids, _ = O.select_visible(ovol, mv, proj, H, cfg["sse"])
-    t_lod = time.perf_counter() - t0
-    bp = O.blob_params(cfg["n_blobs"], cfg["seed"], cfg["noise"], 1)
-    with cf.ThreadPoolExecutor(os.cpu_count()) as ex:
-        bricks = np.stack(list(ex.map(lambda i: O.blob_brick(ovol, bp, int(i)), ids)))
-    max_level = max(int(i) & 0xF for i in ids)
-    n_samples = (2 * cfg["voxels"]) >> (ovol.depth - 1 - max_level)
-    view = O.make_view(mv, proj, W, H, n_samples, early_exit=cfg["early"])
-    tf = transfer_function(cfg)
-    picks = [int((j + 0.5) * H / rows) for j in range(rows)]
-    t0 = time.perf_counter()
-    for y in picks:
-        O.raycast(ovol, 1, ids, bricks, tf, view, rows=(y, y + 1))
-    t_rows = time.perf_counter() - t0
-    return t_lod + t_rows * H / rows, t_lod, t_rows
+
+def orbit_frame(i, steps, n_frames):
+    """Orbit frame of step i: steps spread evenly over the whole orbit."""
+    return (i * n_frames) // max(steps, 1) % n_frames
+
+
+class CpuFrames:
+    """The oracle (CPU restatement of the reference path) on one workload:
+    bricks generated once per node, then per frame the FP32 LOD selection on
+    one thread (the reference's render thread) and the FP64 ray cast on every
+    host thread."""
+
+    def __init__(self, cfg):
+        from oracle import pyoracle as O
+        self.O, self.cfg = O, cfg
+        self.ovol = O.volume(cfg["voxels"], cfg["block"], cfg["overlap"])
+        self.bp = O.blob_params(cfg["n_blobs"], cfg["seed"], cfg["noise"], 1)
+        self.tf = transfer_function(cfg)
+        self.bricks = {}
+
+    def camera(self, k):
+        import livre_gb300 as lv
+        c = self.cfg
+        return lv.orbit_camera(k, c["frames"], tuple(self.ovol.world_size), c["width"],
+                               c["height"])
+
+    def inputs(self, k):
+        """(mv, proj, visible ids, seconds of the selection)."""
+        mv, proj = self.camera(k)
+        t0 = time.perf_counter()
+        ids, _ = self.O.select_visible(self.ovol, mv, proj, self.cfg["height"], self.cfg["sse"])
+        return mv, proj, ids, time.perf_counter() - t0
+
+    def brick_stack(self, ids):
+        import concurrent.futures as cf
+        import numpy as np
+        miss = [int(i) for i in ids if int(i) not in self.bricks]
+        with cf.ThreadPoolExecutor(os.cpu_count()) as ex:
+            for i, b in zip(miss, ex.map(lambda n: self.O.blob_brick(self.ovol, self.bp, n),
+                                         miss)):
+                self.bricks[i] = b
+        return np.stack([self.bricks[int(i)] for i in ids])
+
+    def view(self, mv, proj, ids, early=None):
+        c = self.cfg
+        max_level = max(int(i) & 0xF for i in ids)
+        n_samples = (2 * c["voxels"]) >> (self.ovol.depth - 1 - max_level)
+        return self.O.make_view(mv, proj, c["width"], c["height"], n_samples,
+                                early_exit=c["early"] if early is None else early)
+
+    def frame(self, k, rows=None, mode=0, diagnostics=False):
+        """Renders frame k: (result of the oracle's raycast, selection s,
+        ray-cast s)."""
+        mv, proj, ids, t_lod = self.inputs(k)
+        bricks = self.brick_stack(ids)
+        view = self.view(mv, proj, ids)
+        t0 = time.perf_counter()
+        res = self.O.raycast(self.ovol, 1, ids, bricks, self.tf, view, rows=rows, mode=mode,
+                             diagnostics=diagnostics)
+        return res, t_lod, time.perf_counter() - t0
+
+
+def cpu_sample(cfg, frames):
+    """Whole frames of the oracle: (seconds per frame, selection s per frame,
+    frames rendered)."""
+    cf_ = CpuFrames(cfg)
+    tot, lod = 0.0, 0.0
+    for k in frames:
+        _, t_lod, t_ray = cf_.frame(k)
+        tot += t_lod + t_ray
+        lod += t_lod
+    return tot / len(frames), lod / len(frames)
 
 
 def workload_config(cfg, world):
@@ -187,25 +260,40 @@ def reference_arm(args, cfg):
         return
     from oracle import build as ob
     ob.build()
-    times = []
-    for s in range(args.warmup + args.steps):
-        sec, t_lod, t_rows = cpu_frame_estimate(cfg, k=s % cfg["frames"], rows=args.cpu_rows)
-        if s >= args.warmup:
-            times.append(sec)
+    cf_ = CpuFrames(cfg)
+    H = cfg["height"]
+    times, lods, samples = [], [], 0
+    wall0 = time.perf_counter()
+    for s_ in range(args.warmup + args.steps):
+        timed = s_ >= args.warmup
+        k = orbit_frame(s_ - args.warmup, args.steps, cfg["frames"]) if timed else \
+            orbit_frame(s_, args.warmup, cfg["frames"])
+        (img, ns), t_lod, t_ray = cf_.frame(k)
+        if timed:
+            times.append(t_lod + t_ray)
+            lods.append(t_lod)
+            samples += ns
+    wall = time.perf_counter() - wall0
     ms = 1000.0 * sum(times) / len(times)
     fps = 1000.0 / ms
     cores = os.cpu_count()
+    model = cpu_model()
     line = {"impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(cfg, 1),
             "note": "CPU restatement of the reference path (the reference renders through "
-                    "OpenGL, unavailable on this box)",
-            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-                             "sample": "per step: full-frame FP32 LOD selection (1 thread) + "
-                                       "FP64 ray cast of %d evenly spaced rows (all threads), "
-                                       "extrapolated to %d rows" % (args.cpu_rows, cfg["height"])},
+                    "OpenGL, unavailable on this box); every step one whole frame",
+            "samples_per_s": samples / (sum(times)),
+            "lod_select_ms_mean": 1000.0 * sum(lods) / len(lods),
+            "wall_s": wall,
+            "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores,
+                             "cpu_model": model, "kind": "port",
+                             "sample": "per step one whole %dx%d orbit frame (frames spread "
+                                       "evenly over the orbit): FP32 LOD selection (1 thread) "
+                                       "+ FP64 ray cast of all %d rows (%d threads)"
+                                       % (cfg["width"], H, H, cores)},
             "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -499,6 +587,115 @@ def outofcore_mode(local, args, dev):
     return res
 
 
+# ------------------------------------------------ plain 256^3 and parity
+def plain256_mode(local, args, dev, steps=64):
+    """The CPU-runnable plain workload (256^3 uint8, 32^3 bricks, 16 blobs,
+    512x512, linear ramp, LOD 1 px, early termination 0.999): the 64 orbit
+    frames with every brick resident, CUDA events per frame, L2 flushed."""
+    import numpy as np
+    import torch
+    import livre_gb300 as lv
+    cfg = CONFIGS["plain256"]
+    W, H = cfg["width"], cfg["height"]
+    ctx = lv.Context(local, pool_bytes=cfg["pool_gib"] << 30)
+    vi = lv.VolumeInformation(cfg["voxels"], cfg["block"], cfg["overlap"])
+    vol = ctx.blob_volume(vi, cfg["n_blobs"], cfg["seed"], cfg["noise"])
+    tf = ctx.transfer_function(transfer_function(cfg))
+    descs = [ctx.render_desc(mv, pr, W, H, sse=cfg["sse"], early_exit=cfg["early"],
+                             step_policy=lv.STEP_HALF_VOXEL) for mv, pr in
+             cameras(cfg, vi.world_size)]
+    out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for d in descs + descs[: args.warmup]:
+        ctx.render(vol, tf, d, out)
+        ctx.last_stats()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    stats = []
+    for i in range(steps):
+        flush.fill_(i & 0xFF)
+        ev[i][0].record(stream)
+        ctx.render(vol, tf, descs[orbit_frame(i, steps, cfg["frames"])], out)
+        ev[i][1].record(stream)
+        stats.append(ctx.last_stats())
+    torch.cuda.synchronize()
+    ms = np.array([a.elapsed_time(b) for a, b in ev])
+    ray = np.array([st["raycast_ms"] for st in stats])
+    ns = np.array([st["n_samples"] for st in stats], np.float64)
+    alg = ns * 8 + W * H * 16
+    res = {"workload": cfg["workload"], "frames": steps, "frames_per_s": 1000.0 * steps / ms.sum(),
+           "p50_ms": float(np.percentile(ms, 50)), "p99_ms": float(np.percentile(ms, 99)),
+           "raycast_ms_mean": float(ray.mean()),
+           "select_ms_mean": float(np.mean([st["select_ms"] for st in stats])),
+           "samples_per_s": float(ns.sum() / (ms.sum() / 1000.0)),
+           "visible_bricks_mean": float(np.mean([st["n_visible"] for st in stats])),
+           "raycast_gbs": float(alg.sum() / (ray.sum() / 1000.0) / 1e9)}
+    vol.close()
+    tf.close()
+    ctx.close()
+    return res
+
+
+def parity_mode(ctx, vol, tf, cfg, args, dev):
+    """Device frames of both plain workloads against the oracle on this host:
+    max per-channel error against the per-ray mode (the parity bar, 1/255),
+    and against the shader-order mode (brick-by-brick, brick-centre distance
+    order) the pixels over 1/255 and the sample-count difference."""
+    import numpy as np
+    import torch
+    import livre_gb300 as lv
+    res = {"tolerance": 1.0 / 255.0}
+
+    def compare(cpu, img, k, st, rows=None, shader=True):
+        (ref, ns), _, _ = cpu.frame(k, rows=rows)
+        sl = slice(None) if rows is None else slice(rows[0], rows[1])
+        r = {"frame": k, "rows": list(rows) if rows else "all",
+             "max_err_255": float(np.abs(img[sl] - ref[sl]).max() * 255.0),
+             "device_samples": int(st["n_samples"]) if rows is None else None,
+             "oracle_samples": int(ns)}
+        if shader:
+            (shd, nss, c_shd, flags), _, _ = cpu.frame(k, rows=rows, mode=1, diagnostics=True)
+            d = np.abs(img[sl] - shd[sl]).max(axis=2)
+            r["shader_order"] = {"max_err_255": float(d.max() * 255.0),
+                                 "pixels_over_1_255": int((d > 1.0 / 255.0).sum()),
+                                 "pixels": int(d.size), "samples": int(nss),
+                                 "inverted_pixels": int(((flags[sl] & 2) != 0).sum())}
+        return r
+
+    # workload 1 (256^3 / 512^2), full frames
+    c1 = CONFIGS["plain256"]
+    c1ctx = lv.Context(dev.index or 0, pool_bytes=c1["pool_gib"] << 30)
+    vi = lv.VolumeInformation(c1["voxels"], c1["block"], c1["overlap"])
+    v1 = c1ctx.blob_volume(vi, c1["n_blobs"], c1["seed"], c1["noise"])
+    t1 = c1ctx.transfer_function(transfer_function(c1))
+    cpu1 = CpuFrames(c1)
+    res["plain256"] = []
+    for k in (0, 32):
+        mv, pr = cpu1.camera(k)
+        d = c1ctx.render_desc(mv, pr, c1["width"], c1["height"], sse=c1["sse"],
+                              early_exit=c1["early"], step_policy=lv.STEP_HALF_VOXEL)
+        img = c1ctx.render(v1, t1, d).cpu().numpy()
+        res["plain256"].append(compare(cpu1, img, k, c1ctx.last_stats()))
+    v1.close()
+    t1.close()
+    c1ctx.close()
+    # workload 2 (the headline), row bands of two frames
+    cpu2 = CpuFrames(cfg)
+    res[args.config] = []
+    for k in (0, 40):
+        mv, pr = cpu2.camera(k)
+        d = ctx.render_desc(mv, pr, cfg["width"], cfg["height"], sse=cfg["sse"],
+                            early_exit=cfg["early"], step_policy=lv.STEP_HALF_VOXEL)
+        img = ctx.render(vol, tf, d).cpu().numpy()
+        st = ctx.last_stats()
+        for r0 in (cfg["height"] * 3 // 8, cfg["height"] // 2):
+            res[args.config].append(compare(cpu2, img, k, st, rows=(r0, r0 + 16)))
+    res["max_err_255"] = max(r["max_err_255"] for key in ("plain256", args.config)
+                             for r in res[key])
+    return res
+
+
 # ------------------------------------------------------------ GPU arm
 def gb300_arm(args, cfg):
     import numpy as np
@@ -537,7 +734,8 @@ def gb300_arm(args, cfg):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def frame_of(i):
-        return my_frames[i % len(my_frames)]
+        """Frame of timed step i: spread evenly over this rank's frames."""
+        return my_frames[orbit_frame(i, args.steps, len(my_frames))]
 
     # ---- e2e: cold pool, bricks streamed from the host store, RGBA8 back.
     # Each frame's RGBA8 copy to the host runs on a copy stream while the
@@ -661,14 +859,20 @@ def gb300_arm(args, cfg):
         sctx.close()
     if "outofcore" in modes:
         line["outofcore"] = outofcore_mode(local, args, dev)
+    if "plain256" in modes:
+        line["plain256"] = plain256_mode(local, args, dev)
+    if "parity" in modes:
+        line["parity"] = parity_mode(ctx, vol, tf, cfg, args, dev)
     if world == 1 and not args.no_cpu_baseline:
-        sec, t_lod, t_rows = cpu_frame_estimate(cfg, k=0, rows=args.cpu_rows)
+        ks = [orbit_frame(j, args.cpu_frames, cfg["frames"]) for j in range(args.cpu_frames)]
+        sec, t_lod = cpu_sample(cfg, ks)
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "frames/s", "cores": os.cpu_count(),
-                                "kind": "port", "lod_select_ms": 1e3 * t_lod,
-                                "sample": "frame 0: FP32 LOD selection (1 thread, %.3f s) + FP64 "
-                                          "ray cast of %d evenly spaced rows on all threads "
-                                          "(%.2f s), extrapolated to %d rows"
-                                          % (t_lod, args.cpu_rows, t_rows, H)}
+                                "cpu_model": cpu_model(), "kind": "port",
+                                "lod_select_ms": 1e3 * t_lod,
+                                "sample": "orbit frames %s, whole %dx%d frames: FP32 LOD "
+                                          "selection (1 thread) + FP64 ray cast of every row "
+                                          "(%d threads), %.1f s per frame"
+                                          % (ks, W, H, os.cpu_count(), sec)}
     print(json.dumps(line), flush=True)
 
 

@@ -1,8 +1,8 @@
 """Extracts the reference's golden vectors for the hot path into JSON fixtures.
 
-Run in the build container, where the reference tree is mounted:
-    python tests/golden/make_golden.py /root/reference
-It reads, as text:
+Run where a checkout of the reference (BlueBrain/Livre) is available:
+    python tests/golden/make_golden.py <path to the Livre source tree>
+(or set LIVRE_SOURCE_DIR). It reads, as text:
   - tests/data/lodSelection.cpp:70-207  (getVisibles cases and expected ids)
   - tests/core/tf_f.1dt                 (transfer-function file of
                                           tests/core/transferFunction.cpp:53-62)
@@ -65,4 +65,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LIVRE_SOURCE_DIR")
+    if not src:
+        sys.exit("usage: make_golden.py <Livre source tree> (or set LIVRE_SOURCE_DIR)")
+    main(src)

@@ -26,7 +26,7 @@ def test_reference_arm_json_line(oracle):
     assert "workload" in line["config"]
     cb = line["cpu_baseline"]
     assert cb["value"] == line["value"] and cb["cores"] >= 1
-    assert cb["kind"] in ("reference", "port") and cb["sample"]
+    assert cb["kind"] in ("reference", "port") and cb["sample"] and cb["cpu_model"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
