@@ -131,6 +131,30 @@ lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
                             uint32_t capacity, uint32_t* d_result,
                             void* stream);
 
+/* The visible set of one view in host memory: lv_select_visible into the
+ * context's own device buffer, then copied to `ids` (capacity uint64 host
+ * slots) and `result` (LV_SELECT_RESULT_WORDS host words). Synchronous. The
+ * output port "VisibleNodes" of VisibleSetGeneratorFilter::execute
+ * (livre/lib/pipeline/VisibleSetGeneratorFilter.cpp:40-66), which
+ * RenderPipeline::render hands to Renderer::render
+ * (livre/lib/pipeline/RenderPipeline.cpp:92-158). */
+lv_status lv_select_visible_host(lv_ctx* ctx, const lv_volume_info* vol,
+                                 const lv_camera* camera,
+                                 const lv_lod_params* params, uint64_t* ids,
+                                 uint32_t capacity, uint32_t* result);
+
+/* Test hook of the selection's failure path; no counterpart in the
+ * reference (its CPU traversal has no barrier). The next single-view
+ * selection that runs as one cooperative launch (lv_select_visible, or
+ * lv_render's selection when the previous frame has finished) launches with
+ * one CTA that never arrives at the grid barrier and a wait limit of `polls`
+ * polls (64 ns sleeps) instead of 2^22: the other CTAs give up, the launch
+ * returns, and the selection reports LV_SEL_OVERFLOW = 2 (lv_select_visible)
+ * or error_flags 4 (lv_render). Selections of octrees whose widest level
+ * fits one CTA (<= 256 nodes) run on one CTA and are not affected. polls:
+ * 1 .. 2^22. */
+lv_status lv_test_fail_grid_barrier(lv_ctx* ctx, uint32_t polls);
+
 /* LOD selection that allocates nothing, for callers that cannot allocate
  * device memory (a host application whose own caching allocator owns the
  * GPU's memory, or a per-frame path that must not risk the device-wide
@@ -584,6 +608,10 @@ lv_status lv_batch_graph_stats(lv_batch* batch, uint64_t* captures,
 lv_status lv_batch_autotune(lv_batch* batch, const lv_batch_view* views,
                             uint32_t n, void* stream, uint32_t reps,
                             lv_batch_config* chosen);
+/* Every configuration the last lv_batch_autotune of this batch ran, with its
+ * mean ray-cast time in ms (up to `capacity`; *n = how many it ran). */
+lv_status lv_batch_autotune_results(const lv_batch* batch, lv_batch_config* configs,
+                                    float* raycast_ms, uint32_t capacity, uint32_t* n);
 
 /* -------------------------------------------------------------- serving */
 

@@ -156,6 +156,9 @@ _SIGNATURES = {
                                     C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "lv_select_visible_noalloc": (C.c_int, [P(VolumeInfo), P(Camera), P(LodParams), C.c_void_p,
                                             C.c_uint32, C.c_void_p, C.c_void_p]),
+    "lv_test_fail_grid_barrier": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "lv_select_visible_host": (C.c_int, [C.c_void_p, P(VolumeInfo), P(Camera), P(LodParams),
+                                         C.c_void_p, C.c_uint32, C.c_void_p]),
     "lv_pool_configure": (C.c_int, [C.c_void_p, C.c_size_t]),
     "lv_pool_purge": (C.c_int, [C.c_void_p]),
     "lv_volume_create": (C.c_int, [C.c_void_p, P(VolumeInfo), GET_DATA_FN, C.c_void_p,
@@ -199,6 +202,8 @@ _SIGNATURES = {
                                  P(C.c_float)]),
     "lv_batch_autotune": (C.c_int, [C.c_void_p, P(BatchView), C.c_uint32, C.c_void_p,
                                     C.c_uint32, P(BatchConfig)]),
+    "lv_batch_autotune_results": (C.c_int, [C.c_void_p, P(BatchConfig), P(C.c_float),
+                                            C.c_uint32, P(C.c_uint32)]),
     "lv_server_create": (C.c_int, [C.c_void_p, P(ServerConfig), P(C.c_void_p)]),
     "lv_server_submit": (C.c_int, [C.c_void_p, P(Request), P(C.c_uint64)]),
     "lv_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32, P(RequestResult)]),

@@ -147,6 +147,8 @@ struct lv_ctx
     std::string error;
     cudaStream_t upload_stream = nullptr;
     lv::SelectScratch sel;
+    lv::DeviceBuffer sel_host_out; /* lv_select_visible_host's device output */
+    uint32_t test_barrier_polls = 0; /* lv_test_fail_grid_barrier */
     lv::Pool* pool = nullptr;
     lv::Renderer* renderer = nullptr;
     size_t pool_bytes = size_t(3072) << 20;
