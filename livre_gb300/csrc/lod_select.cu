@@ -323,7 +323,7 @@ __global__ void lod_finish_kernel(const LodView* __restrict__ views,
 constexpr uint32_t kSpinLimit = 1u << 22; /* ~0.3 s of 64 ns sleeps */
 constexpr uint32_t kSoloItems = 1024;     /* frontier one CTA visits alone */
 
-__device__ __forceinline__ void grid_barrier(uint32_t* bar)
+__device__ __forceinline__ void grid_barrier(uint32_t* bar, uint32_t spin_limit)
 {
     __syncthreads();
     if (threadIdx.x == 0)
@@ -342,7 +342,7 @@ __device__ __forceinline__ void grid_barrier(uint32_t* bar)
             uint32_t polls = 0;
             while (*gen == g)
             {
-                if (++polls > kSpinLimit)
+                if (++polls > spin_limit)
                 {
                     atomicExch(bar + 2, 1u); /* gave up: results unusable */
                     break;
@@ -359,8 +359,13 @@ __global__ void __launch_bounds__(256)
     lod_fused_kernel(const __grid_constant__ LodView V, uint32_t max_depth,
                      uint64_t* __restrict__ ids0, uint32_t* __restrict__ view0,
                      uint64_t* __restrict__ ids1, uint32_t* __restrict__ view1,
-                     uint32_t* __restrict__ counts, uint32_t capacity)
+                     uint32_t* __restrict__ counts, uint32_t capacity,
+                     uint32_t spin_limit, uint32_t absent_cta)
 {
+    /* test hook (lv_test_fail_grid_barrier): this CTA never arrives, so the
+     * others' bounded waits give up and the result reports it */
+    if (blockIdx.x == absent_cta)
+        return;
     uint32_t* overflow = counts + kMaxLevels + 1;
     uint32_t* bar = counts + kMaxLevels + 2;
     uint32_t* solo_end = counts + kMaxLevels + 5;
@@ -406,11 +411,11 @@ __global__ void __launch_bounds__(256)
             if (threadIdx.x == 0)
                 *solo_end = l;
         }
-        grid_barrier(bar);
+        grid_barrier(bar, spin_limit);
         l = __ldcg(solo_end);
     }
     else
-        grid_barrier(bar);
+        grid_barrier(bar, spin_limit);
     for (; l < max_depth; ++l)
     {
         const uint32_t n = min(__ldcg(counts + l), capacity);
@@ -420,7 +425,7 @@ __global__ void __launch_bounds__(256)
         level_items<true>(views, even ? ids0 : ids1, even ? view0 : view1, n,
                           even ? ids1 : ids0, even ? view1 : view0, counts + l + 1, capacity,
                           overflow);
-        grid_barrier(bar);
+        grid_barrier(bar, spin_limit);
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
@@ -695,8 +700,6 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
         uint64_t* ids1 = S.ids[1].as<uint64_t>();
         uint32_t* view0 = S.view[0].as<uint32_t>();
         uint32_t* view1 = S.view[1].as<uint32_t>();
-        void* args[] = {&V, &max_depth, &ids0, &view0, &ids1, &view1, &counts,
-                        const_cast<uint32_t*>(&cap)};
         /* no level holds more nodes than the octree's widest one: a CTA more
          * than it needs would only add an arrival to each grid barrier */
         uint64_t widest = uint64_t(V.root_blocks[0]) * V.root_blocks[1] * V.root_blocks[2];
@@ -704,6 +707,15 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
             widest <<= 3;
         const uint32_t used =
             uint32_t(std::max<uint64_t>(1, std::min<uint64_t>(grid, (widest + 255) / 256)));
+        uint32_t spin = kSpinLimit, absent = 0xFFFFFFFFu;
+        if (ctx->test_barrier_polls && used > 1)
+        {
+            spin = ctx->test_barrier_polls;
+            absent = used - 1; /* never CTA 0, which writes the result */
+            ctx->test_barrier_polls = 0;
+        }
+        void* args[] = {&V, &max_depth, &ids0, &view0, &ids1, &view1, &counts,
+                        const_cast<uint32_t*>(&cap), &spin, &absent};
         LV_CUDA(ctx, cudaLaunchCooperativeKernel(reinterpret_cast<void*>(lod_fused_kernel),
                                                  dim3(used), dim3(256), args, 0, stream));
         return LV_OK;
@@ -854,6 +866,36 @@ extern "C" lv_status lv_select_visible(lv_ctx* ctx, const lv_volume_info* vol,
             return st;
     }
     return scratch_release(ctx, ctx->sel, s);
+}
+
+extern "C" lv_status lv_select_visible_host(lv_ctx* ctx, const lv_volume_info* vol,
+                                            const lv_camera* camera,
+                                            const lv_lod_params* params, uint64_t* ids,
+                                            uint32_t capacity, uint32_t* result)
+{
+    using namespace lv;
+    if (!ctx || !vol || !camera || !params || !result || (!ids && capacity))
+        return fail(ctx, LV_EINVAL, "null argument");
+    uint64_t* d_ids = nullptr;
+    uint32_t* d_res = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(ctx->mutex);
+        LV_CUDA(ctx, cudaSetDevice(ctx->device));
+        const size_t id_bytes = (sizeof(uint64_t) * size_t(capacity) + 255) & ~size_t(255);
+        LV_CUDA(ctx, ctx->sel_host_out.reserve(id_bytes + 4 * LV_SELECT_RESULT_WORDS));
+        d_ids = ctx->sel_host_out.as<uint64_t>();
+        d_res = reinterpret_cast<uint32_t*>(ctx->sel_host_out.as<uint8_t>() + id_bytes);
+    }
+    /* the legacy default stream: ordered after the context's earlier work on
+     * blocking streams, and this call waits for it */
+    lv_status st = lv_select_visible(ctx, vol, camera, params, d_ids, capacity, d_res, nullptr);
+    if (st != LV_OK)
+        return st;
+    LV_CUDA(ctx, cudaMemcpy(result, d_res, 4 * LV_SELECT_RESULT_WORDS, cudaMemcpyDeviceToHost));
+    const uint32_t n = std::min(result[LV_SEL_WRITTEN], capacity);
+    if (n)
+        LV_CUDA(ctx, cudaMemcpy(ids, d_ids, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost));
+    return LV_OK;
 }
 
 /* ------------------------------------------------------------------------
@@ -1019,4 +1061,14 @@ extern "C" lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
     }
     lod_finish_kernel<<<1, 128, 0, s>>>(dview, 1, overflow);
     return launched();
+}
+
+extern "C" lv_status lv_test_fail_grid_barrier(lv_ctx* ctx, uint32_t polls)
+{
+    using namespace lv;
+    if (!ctx || polls == 0 || polls > kSpinLimit)
+        return fail(ctx, LV_EINVAL, "polls must be in [1, 2^22]");
+    std::lock_guard<std::mutex> lock(ctx->mutex);
+    ctx->test_barrier_polls = polls;
+    return LV_OK;
 }
