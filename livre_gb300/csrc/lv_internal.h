@@ -95,6 +95,10 @@ struct RayView
     uint32_t W, H;          /* pixels rendered: the rect (tiles cover these) */
     uint32_t x0, y0;        /* the rect's corner in the frame */
     uint32_t FW, FH;        /* the frame (ray directions, output rows) */
+    uint32_t cull[4];       /* frame pixels [cull[0], cull[2]) x [cull[1], cull[3]):
+                               a conservative bound of the pixels whose ray can
+                               reach the volume's box; the others start and end
+                               with no sample */
     uint32_t samples_fixed; /* 0 = policy */
     uint32_t step_policy;
     uint32_t max_voxel_dim;

@@ -321,14 +321,39 @@ struct Taps
     float fx, fy, fz;
 };
 
+/* The view constants the per-sample steps read (the transfer function and
+ * its coordinate map, the early-termination opacity, the last trilinear
+ * base voxel). A kernel that renders one view passes its RayView parameter
+ * itself (constant-bank operands); the persistent batch kernel, whose view
+ * changes from tile to tile, passes this register copy instead of reading
+ * its shared-memory view on every sample. */
+struct HotView
+{
+    const float4* tf;
+    float tf_mul, tf_add, tf_last, early;
+    uint32_t max_base;
+};
+
+__device__ __forceinline__ HotView hot_view(const RayView& V)
+{
+    HotView h;
+    h.tf = V.tf;
+    h.tf_mul = V.tf_mul;
+    h.tf_add = V.tf_add;
+    h.tf_last = V.tf_last;
+    h.early = V.early;
+    h.max_base = V.max_base;
+    return h;
+}
+
 /* Voxels around slot coordinate s (nearest: s = local position; trilinear:
  * s = local position - 0.5, texel centres on integers). EDGE = 1 clamps every
  * tap to the brick (GL_CLAMP_TO_EDGE, needed without overlap); EDGE = 0 uses
  * one base address and offsets to the other taps, valid when every overlap
  * >= 1; EDGE = n > 1 is EDGE = 0 for bricks of n x n voxels in x and y (the
  * row and slice pitches become immediate offsets of one pointer). */
-template <int DT, int FILTER, int EDGE>
-__device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick,
+template <int DT, int FILTER, int EDGE, class HV>
+__device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const uint8_t* brick,
                                           const float s[3], Taps<FILTER>& T)
 {
     const int bpv = DT == LV_DT_UINT16 ? 2 : DT == LV_DT_UINT8 ? 1 : int(V.bpv);
@@ -370,7 +395,7 @@ __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick
          * [O - 1/2, O + B - 1/2], so the base voxel is in [0, N - 2] on each
          * axis and all eight taps are in the slot. One unsigned clamp of the
          * linear base keeps any tap inside the slot whatever the inputs. */
-        const uint32_t base = min(uint32_t((iz * n1 + iy) * n0 + ix), V.max_base);
+        const uint32_t base = min(uint32_t((iz * n1 + iy) * n0 + ix), H.max_base);
         const int dy = n0 * bpv, dz = n0 * n1 * bpv;
         const uint8_t* p00 = brick + base * bpv;
         const uint8_t* p01 = p00 + dy;
@@ -387,19 +412,28 @@ __device__ __forceinline__ void load_taps(const RayView& V, const uint8_t* brick
     }
 }
 
-/* Trilinear weights applied x, then y, then z (the oracle's order). */
+/* Trilinear weights applied x, then y, then z (the oracle's order):
+ *   a0 = lerp(c0, c1, fx)  a1 = lerp(c2, c3, fx)  a2 = lerp(c4, c5, fx)
+ *   a3 = lerp(c6, c7, fx)  b0 = lerp(a0, a1, fy)  b1 = lerp(a2, a3, fy)
+ *   v  = lerp(b0, b1, fz), lerp(a, b, f) = fma(b - a, f, a).
+ * Independent lerps run as pairs in packed FP32 instructions (FFMA2: one
+ * issue for two IEEE fused multiply-adds, each rounded as the scalar one;
+ * b - a as fma(a, -1, b) is the same single rounding), paired so that every
+ * result lands in the register pair the next stage reads: (a0, a2) and
+ * (a1, a3), then (b0, b1). */
 template <int FILTER>
 __device__ __forceinline__ float interp(const Taps<FILTER>& T)
 {
     if (FILTER == LV_FILTER_NEAREST)
         return T.c[0];
-    const float a0 = fmaf(T.c[1] - T.c[0], T.fx, T.c[0]);
-    const float a1 = fmaf(T.c[3] - T.c[2], T.fx, T.c[2]);
-    const float a2 = fmaf(T.c[5] - T.c[4], T.fx, T.c[4]);
-    const float a3 = fmaf(T.c[7] - T.c[6], T.fx, T.c[6]);
-    const float b0 = fmaf(a1 - a0, T.fy, a0);
-    const float b1 = fmaf(a3 - a2, T.fy, a2);
-    return fmaf(b1 - b0, T.fz, b0);
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    const float2 fx = make_float2(T.fx, T.fx);
+    const float2 lo0 = make_float2(T.c[0], T.c[4]), hi0 = make_float2(T.c[1], T.c[5]);
+    const float2 lo1 = make_float2(T.c[2], T.c[6]), hi1 = make_float2(T.c[3], T.c[7]);
+    const float2 a02 = __ffma2_rn(__ffma2_rn(lo0, m1, hi0), fx, lo0);
+    const float2 a13 = __ffma2_rn(__ffma2_rn(lo1, m1, hi1), fx, lo1);
+    const float2 b01 = __ffma2_rn(__ffma2_rn(a02, m1, a13), make_float2(T.fy, T.fy), a02);
+    return fmaf(b01.y - b01.x, T.fz, b01.x);
 }
 
 /* Linear, clamp-to-edge lookup of the transfer function at voxel value v
@@ -407,18 +441,21 @@ __device__ __forceinline__ float interp(const Taps<FILTER>& T)
  * interleaved (value_i, value_{i+1} - value_i) pairs (last difference 0).
  * Clamping the coordinate to [0, tfn - 1] before splitting it gives the
  * same texel pair and weight as clamping the texel index after. */
-template <int TFS>
-__device__ __forceinline__ float4 tf_lookup(const RayView& V, float v)
+template <int TFS, class HV>
+__device__ __forceinline__ float4 tf_lookup(const HV& H, float v)
 {
-    const float s = fminf(fmaxf(fmaf(v, V.tf_mul, V.tf_add), 0.0f), V.tf_last);
+    const float s = fminf(fmaxf(fmaf(v, H.tf_mul, H.tf_add), 0.0f), H.tf_last);
     const int i0 = int(s);
     const float f = s - float(i0);
     /* TFS: the table is in shared memory (generic loads), else read-only global */
-    const float4* e = V.tf + 2 * i0;
+    const float4* e = H.tf + 2 * i0;
     const float4 a = TFS ? e[0] : __ldg(e);
     const float4 b = TFS ? e[1] : __ldg(e + 1);
-    return make_float4(fmaf(b.x, f, a.x), fmaf(b.y, f, a.y), fmaf(b.z, f, a.z),
-                       fmaf(b.w, f, a.w));
+    /* value + difference * f per channel, two channels per FFMA2 */
+    const float2 f2 = make_float2(f, f);
+    const float2 rg = __ffma2_rn(make_float2(b.x, b.y), f2, make_float2(a.x, a.y));
+    const float2 ba = __ffma2_rn(make_float2(b.z, b.w), f2, make_float2(a.z, a.w));
+    return make_float4(rg.x, rg.y, ba.x, ba.y);
 }
 
 __device__ __forceinline__ float Md(const float* m, int r, int c)
@@ -440,11 +477,22 @@ __device__ __forceinline__ uint64_t frame_index(const RayView& V, uint32_t px, u
 }
 
 /* Ray through the centre of pixel (px, py) of the rendered rect (frame pixel
- * (x0 + px, y0 + py)); FP32 IEEE ops in fixed order. */
+ * (x0 + px, y0 + py)); FP32 IEEE ops in fixed order. A pixel outside the
+ * view's conservative screen rectangle of the volume's box (V.cull) misses
+ * the box: it returns no hit without the set-up arithmetic, as the full
+ * computation would (about 85 % of a 1080p orbit frame's pixels). */
 __device__ __forceinline__ RayGeom ray_setup(const RayView& V, uint32_t px,
                                              uint32_t py)
 {
     RayGeom g;
+    const uint32_t fx = px + V.x0, fy = py + V.y0;
+    if (fx < V.cull[0] || fx >= V.cull[2] || fy < V.cull[1] || fy >= V.cull[3])
+    {
+        g.dir[0] = g.dir[1] = g.dir[2] = 0.0f;
+        g.tg = g.tlo = g.thi = 0.0f;
+        g.hit = false;
+        return g;
+    }
     const float nx =
         __fsub_rn(__fdiv_rn(__fmul_rn(__fadd_rn(__uint2float_rn(px + V.x0), 0.5f), 2.0f),
                             __uint2float_rn(V.FW)),
@@ -688,9 +736,9 @@ __device__ __forceinline__ bool locate(const RayView& V, RayState& r, float step
 /* Advances the ray to its next sample. Returns 0 once the ray has left its
  * segment, 1 for a sample without data (outside the octree or no brick
  * rendered there), 2 with the sample's voxels in T. */
-template <int DT, int FILTER, int EDGE>
-__device__ __forceinline__ int fetch_sample(const RayView& V, RayState& r, float step,
-                                            Taps<FILTER>& T)
+template <int DT, int FILTER, int EDGE, class HV>
+__device__ __forceinline__ int fetch_sample(const RayView& V, const HV& H, RayState& r,
+                                            float step, Taps<FILTER>& T)
 {
     const float t = fmaf(r.kf, step, r.tg);
     if (!(t < r.thi))
@@ -712,18 +760,18 @@ __device__ __forceinline__ int fetch_sample(const RayView& V, RayState& r, float
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         sc[a] = fmaf(t, r.sa[a], r.sb[a]);
-    load_taps<DT, FILTER, EDGE>(V, r.brick, sc, T);
+    load_taps<DT, FILTER, EDGE>(V, H, r.brick, sc, T);
     return 2;
 }
 
 /* Transfer function, opacity correction and front-to-back blending of one
  * sample (fragRayCast.glsl:103-111); false once the early-termination
  * opacity is reached. */
-template <int FILTER, int TFS>
-__device__ __forceinline__ bool composite_sample(const RayView& V, RayState& r, float ac,
+template <int FILTER, int TFS, class HV>
+__device__ __forceinline__ bool composite_sample(const HV& H, RayState& r, float ac,
                                                  const Taps<FILTER>& T, uint32_t& nsamp)
 {
-    const float4 src = tf_lookup<TFS>(V, interp<FILTER>(T));
+    const float4 src = tf_lookup<TFS>(H, interp<FILTER>(T));
     const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
     const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
     const float w = alpha * (1.0f - r.dst.w);
@@ -732,16 +780,16 @@ __device__ __forceinline__ bool composite_sample(const RayView& V, RayState& r, 
     r.dst.z = fmaf(src.z, w, r.dst.z);
     r.dst.w = fmaf(alpha, 1.0f - r.dst.w, r.dst.w);
     ++nsamp;
-    return !(r.dst.w > V.early);
+    return !(r.dst.w > H.early);
 }
 
 /* One sample of the ray: false once the ray has ended or reached the
  * early-termination opacity. The steps of fetch_sample and composite_sample
  * in one straight body (fewer registers live across the loop than the two
  * calls). */
-template <int DT, int FILTER, int TFS, int EDGE>
-__device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float step, float ac,
-                                         uint32_t& nsamp)
+template <int DT, int FILTER, int TFS, int EDGE, class HV>
+__device__ __forceinline__ bool ray_step(const RayView& V, const HV& H, RayState& r, float step,
+                                         float ac, uint32_t& nsamp)
 {
     const float t = fmaf(r.kf, step, r.tg);
     if (!(t < r.thi))
@@ -764,8 +812,8 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     for (int a = 0; a < 3; ++a)
         sc[a] = fmaf(t, r.sa[a], r.sb[a]);
     Taps<FILTER> T;
-    load_taps<DT, FILTER, EDGE>(V, r.brick, sc, T);
-    const float4 src = tf_lookup<TFS>(V, interp<FILTER>(T));
+    load_taps<DT, FILTER, EDGE>(V, H, r.brick, sc, T);
+    const float4 src = tf_lookup<TFS>(H, interp<FILTER>(T));
     const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
     const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
     const float w = alpha * (1.0f - r.dst.w);
@@ -774,7 +822,7 @@ __device__ __forceinline__ bool ray_step(const RayView& V, RayState& r, float st
     r.dst.z = fmaf(src.z, w, r.dst.z);
     r.dst.w = fmaf(alpha, 1.0f - r.dst.w, r.dst.w);
     ++nsamp;
-    return !(r.dst.w > V.early);
+    return !(r.dst.w > H.early);
 }
 
 /* A ray has ended: report an index check it failed. */
@@ -797,33 +845,37 @@ __device__ __forceinline__ float4 initial_dst(const RayView& V, uint32_t px, uin
  * ray runs faster; more registers per thread). Samples, values and the
  * compositing order are those of ray_step either way; after an early
  * termination the loads of one extra sample are dropped. */
-template <int DT, int FILTER, int TFS, int EDGE, int LOOKAHEAD = 0>
-__device__ float4 march(const RayView& V, const RayGeom& g, float step,
+template <int DT, int FILTER, int TFS, int EDGE, int LOOKAHEAD, class HV>
+__device__ float4 march(const RayView& V, const HV& H, const RayGeom& g, float step,
                         float ac, uint32_t& nsamp,
                         float4 init = make_float4(0.f, 0.f, 0.f, 0.f))
 {
     RayState r;
-    if (!ray_begin(g, step, r) || init.w > V.early)
+    if (!ray_begin(g, step, r) || init.w > H.early)
         return init;
     r.dst = init;
     if (!LOOKAHEAD)
     {
-        while (ray_step<DT, FILTER, TFS, EDGE>(V, r, step, ac, nsamp))
+        while (ray_step<DT, FILTER, TFS, EDGE>(V, H, r, step, ac, nsamp))
         {
         }
         flush_error(V, r);
         return r.dst;
     }
-    Taps<FILTER> T0;
-    int s0 = fetch_sample<DT, FILTER, EDGE>(V, r, step, T0);
+    /* two tap sets in turn (no copy of the taps between samples): fetch the
+     * next sample into one while the other is composited */
+    Taps<FILTER> T0, T1;
+    int s0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0);
     while (s0)
     {
-        Taps<FILTER> T1;
-        const int s1 = fetch_sample<DT, FILTER, EDGE>(V, r, step, T1);
-        if (s0 == 2 && !composite_sample<FILTER, TFS>(V, r, ac, T0, nsamp))
+        const int s1 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T1);
+        if (s0 == 2 && !composite_sample<FILTER, TFS>(H, r, ac, T0, nsamp))
             break;
-        s0 = s1;
-        T0 = T1;
+        if (!s1)
+            break;
+        s0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0);
+        if (s1 == 2 && !composite_sample<FILTER, TFS>(H, r, ac, T1, nsamp))
+            break;
     }
     flush_error(V, r);
     return r.dst;
@@ -843,7 +895,7 @@ __global__ void __launch_bounds__(256) raycast_kernel(const RayView V)
     {
         const RayGeom g = ray_setup(V, px, py);
         const float4 r =
-            march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
+            march<DT, FILTER, 0, EDGE, LA>(V, V, g, step, ac, nsamp, initial_dst(V, px, py));
         V.out[frame_index(V, px, py)] = r;
     }
     /* warp-aggregated 64-bit sample count */
@@ -872,6 +924,7 @@ __global__ void __launch_bounds__(256)
         atomicCAS(Q.clock, 0ull, globaltimer());
     uint32_t cached = 0xFFFFFFFFu;
     float step = 0.f, ac = 0.f;
+    HotView H{};
     for (;;)
     {
         if (threadIdx.x == 0)
@@ -915,6 +968,7 @@ __global__ void __launch_bounds__(256)
                 __syncthreads();
             }
             cached = v;
+            H = hot_view(sV);
             const uint32_t n = sV.counters[FC_SAMPLES_PER_RAY];
             step = __fdiv_rn(1.0f, __uint2float_rn(n));
             ac = __fdiv_rn(32.0f, __uint2float_rn(n));
@@ -927,7 +981,7 @@ __global__ void __launch_bounds__(256)
         if (px < sV.W && py < sV.H && threadIdx.x < Q.tile_w * Q.tile_h)
         {
             const RayGeom g = ray_setup(sV, px, py);
-            const float4 r = march<DT, FILTER, TF_SHARED, EDGE>(sV, g, step, ac, nsamp);
+            const float4 r = march<DT, FILTER, TF_SHARED, EDGE, 0>(sV, H, g, step, ac, nsamp);
             sV.out[frame_index(sV, px, py)] = r;
         }
         unsigned long long sum = nsamp;
@@ -1057,7 +1111,7 @@ __global__ void __launch_bounds__(256)
         {
             const RayGeom g = ray_setup(V, px, py);
             V.out[frame_index(V, px, py)] =
-                march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
+                march<DT, FILTER, 0, EDGE, LA>(V, V, g, step, ac, nsamp, initial_dst(V, px, py));
         }
     }
     unsigned long long sum = nsamp;
@@ -1086,7 +1140,7 @@ __global__ void __launch_bounds__(256)
     {
         const RayGeom g = ray_setup(V, px, py);
         V.out[frame_index(V, px, py)] =
-            march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
+            march<DT, FILTER, 0, EDGE, LA>(V, V, g, step, ac, nsamp, initial_dst(V, px, py));
     }
     unsigned long long sum = nsamp;
 #pragma unroll
@@ -1125,7 +1179,7 @@ __global__ void __launch_bounds__(128)
         {
             const RayGeom g = ray_setup(V, px, py);
             V.out[frame_index(V, px, py)] =
-                march<DT, FILTER, 0, EDGE, LA>(V, g, step, ac, nsamp, initial_dst(V, px, py));
+                march<DT, FILTER, 0, EDGE, LA>(V, V, g, step, ac, nsamp, initial_dst(V, px, py));
         }
         __syncwarp();
     }
@@ -1372,7 +1426,7 @@ __device__ __forceinline__ void refill_body(const RayView& V, RayView* sv,
         }
         if (active)
             for (uint32_t k = 0; k < checks; ++k)
-                if (!ray_step<DT, FILTER, 0, EDGE>(V, r, K.step, K.ac, nsamp))
+                if (!ray_step<DT, FILTER, 0, EDGE>(V, V, r, K.step, K.ac, nsamp))
                 {
                     active = false;
                     V.out[frame_index(V, px, py)] = r.dst;

@@ -579,6 +579,55 @@ void drop_volume_residency(lv_ctx* ctx, lv_volume* v)
     }
 }
 
+/* Frame pixels whose centre ray can reach the box [lo, hi]: the bounding
+ * rectangle of the projected box corners (P * MV, in double), widened by two
+ * pixels so that FP32 rounding of a grazing ray cannot reach past it. A
+ * corner at or behind the eye plane (w <= 1e-6) gives the whole frame. The
+ * result is half-open: [r[0], r[2]) x [r[1], r[3]). */
+void screen_rect(const lv_camera& cam, const float* lo, const float* hi, uint32_t W, uint32_t H,
+                 uint32_t r[4])
+{
+    double pm[16];
+    for (int row = 0; row < 4; ++row)
+        for (int col = 0; col < 4; ++col)
+        {
+            double acc = 0.0;
+            for (int k = 0; k < 4; ++k)
+                acc += double(cam.projection[k * 4 + row]) * double(cam.modelview[col * 4 + k]);
+            pm[col * 4 + row] = acc;
+        }
+    double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+    for (int c = 0; c < 8; ++c)
+    {
+        const double p[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1],
+                             (c & 4) ? hi[2] : lo[2]};
+        double q[4];
+        for (int row = 0; row < 4; ++row)
+            q[row] = pm[row] * p[0] + pm[4 + row] * p[1] + pm[8 + row] * p[2] + pm[12 + row];
+        if (!(q[3] > 1e-6))
+        {
+            r[0] = r[1] = 0;
+            r[2] = W;
+            r[3] = H;
+            return;
+        }
+        /* pixel index whose centre is at this position: (ndc + 1) / 2 * W - 1/2 */
+        const double x = (q[0] / q[3] + 1.0) * 0.5 * W - 0.5;
+        const double y = (q[1] / q[3] + 1.0) * 0.5 * H - 0.5;
+        xmin = std::min(xmin, x);
+        xmax = std::max(xmax, x);
+        ymin = std::min(ymin, y);
+        ymax = std::max(ymax, y);
+    }
+    auto clampi = [](double v, uint32_t n) {
+        return uint32_t(std::min(std::max(v, 0.0), double(n)));
+    };
+    r[0] = clampi(std::floor(xmin) - 2.0, W);
+    r[1] = clampi(std::floor(ymin) - 2.0, H);
+    r[2] = clampi(std::ceil(xmax) + 3.0, W);
+    r[3] = clampi(std::ceil(ymax) + 3.0, H);
+}
+
 lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
                         const lv_render_desc& desc, const lv_lod_params& lod, float* d_rgba,
                         uint32_t* leaf, uint32_t* counters, RayView& V)
@@ -631,6 +680,7 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     V.early = desc.early_exit;
     V.FW = desc.width;
     V.FH = desc.height;
+    screen_rect(desc.camera, V.gmin, V.gmax, desc.width, desc.height, V.cull);
     if (desc.rect[2] && desc.rect[3])
     {
         if (uint64_t(desc.rect[0]) + desc.rect[2] > desc.width ||
