@@ -66,18 +66,26 @@ def parse():
     p.add_argument("--ooc-voxels", type=int, default=8192,
                    help="out-of-core volume edge (a smaller one for ncu captures)")
     p.add_argument("--ooc-pool-gib", type=int, default=64)
+    p.add_argument("--ooc-host-frames", type=int, default=3,
+                   help="host-generated frames after frame 0 in the outofcore_host mode")
     p.add_argument("--ooc-frames", type=int, default=128,
                    help="frames of the 128-frame out-of-core fly-through to render")
-    p.add_argument("--modes", default="plain,plain256,parity,batched,served,outofcore",
+    p.add_argument("--modes", default="plain,plain256,parity,launches,batched,served,outofcore",
                    help="comma list: plain (headline), plain256 (the 256^3 / 512^2 plain "
-                        "workload), parity (device frames against the oracle), batched (64 "
+                        "workload), parity (device frames against the oracle), launches "
+                        "(ray-cast time of every lv_render launch shape), batched (64 "
                         "uneven views in one persistent launch), served (Poisson request "
-                        "stream), outofcore (8192^3 u16 fly-through through a 64 GiB pool)")
+                        "stream), outofcore (8192^3 u16 fly-through through a 64 GiB pool), "
+                        "outofcore_host (the same with host-generated bricks; not in the "
+                        "default list: host generation takes tens of seconds per frame)")
     p.add_argument("--cpu-frames", type=int, default=2,
                    help="whole frames the CPU baseline of the default line ray casts")
     p.add_argument("--serve-seconds", type=float, default=1.5)
     p.add_argument("--serve-rates", type=lambda t: [int(x) for x in t.split(",")],
-                   default=[200, 500, 1000, 2000], help="Poisson request rates (req/s)")
+                   default=[200, 250, 300, 350, 400, 450, 500, 1000, 2000],
+                   help="Poisson request rates (req/s)")
+    p.add_argument("--slo-ms", type=float, default=150.0,
+                   help="p99 latency objective of the serving capacity figure")
     return p.parse_args()
 
 
@@ -351,21 +359,57 @@ def batched_mode(ctx, args, dev, seed=7):
     t0 = time.time()
     cfg = batch.autotune(items, reps=2)
     tune_s = time.time() - t0
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    batch_ms, ray_ms = [], []
-    for r in range(args.warmup + reps * 4):
-        e0.record()
-        batch.render(items)
-        e1.record()
-        stats, total, ray = batch.stats(len(items))
-        if r >= args.warmup:
-            batch_ms.append(e0.elapsed_time(e1))
-            ray_ms.append(ray)
-    batch_ms = np.array(batch_ms)
+    table = batch.autotune_results()
+    queue_names = {lv.QUEUE_CTA_TILES: "persistent_cta_tiles",
+                   lv.QUEUE_VIEW_KERNELS: "per_view_kernels",
+                   lv.QUEUE_WARP_REFILL: "persistent_warp_refill"}
     n = len(items)
-    samples = float(sum(st["n_samples"] for st in stats))
     pixels = float(sum(d.width * d.height for _, _, d, _ in items))
+
+    def timed(config, rounds):
+        batch.set_config(**{k: config[k] for k in ("tile_w", "tile_h", "ctas_per_sm",
+                                                   "tf_shared", "use_graph", "queue",
+                                                   "samples_per_check", "order",
+                                                   "lookahead")})
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms, ray, dev_ms, host_ms = [], [], [], []
+        cap0, rep0, _ = batch.graph_stats()
+        for r in range(args.warmup + rounds):
+            e0.record()
+            h0 = time.perf_counter()
+            batch.render(items)
+            h1 = time.perf_counter()
+            e1.record()
+            st, total, ray_ms = batch.stats(n)
+            if r >= args.warmup:
+                ms.append(e0.elapsed_time(e1))
+                ray.append(ray_ms)
+                dev_ms.append(total)
+                host_ms.append(1e3 * (h1 - h0))
+        cap1, rep1, _ = batch.graph_stats()
+        ms = np.array(ms)
+        return {"queue": queue_names.get(config["queue"], str(config["queue"])),
+                "config": config, "frames_per_s": 1000.0 * n / ms.mean(),
+                "batch_ms_p50": float(np.percentile(ms, 50)),
+                "batch_ms_p99": float(np.percentile(ms, 99)),
+                "raycast_ms_mean": float(np.mean(ray)),
+                # the batch's device time (its first to its last event) and the
+                # host time of the lv_batch_render call that enqueued it
+                "device_batch_ms_mean": float(np.mean(dev_ms)),
+                "host_render_call_ms_mean": float(np.mean(host_ms)),
+                "samples_per_batch": float(sum(x["n_samples"] for x in st)),
+                "gpu_launches_per_batch": int(st[0]["n_launches"]),
+                "graph_captures": int(cap1 - cap0), "graph_replays": int(rep1 - rep0),
+                "graph_used": bool(rep1 > rep0)}
+
+    reps = min(4, max(2, args.steps // 16))
+    best = timed(cfg, reps * 4)
+    # the best persistent-kernel configuration (one launch per voxel-type
+    # group, replayed as a CUDA graph), timed the same way whatever won
+    pers = [(c, ms) for c, ms in table if c["queue"] == lv.QUEUE_CTA_TILES]
+    persistent = timed(min(pers, key=lambda x: x[1])[0], reps * 4) if pers else None
     out = {"views": n, "volumes": "512^3 u8, 1024^3 u8, 2048^3 u8, 1024^3 u16 (64^3 bricks)",
+           "pixels_per_batch": pixels,
            "plain": {"frames_per_s": 1000.0 * len(plain_ms) / plain_ms.sum(),
                      "p50_ms": float(np.percentile(plain_ms, 50)),
                      "p99_ms": float(np.percentile(plain_ms, 99)),
@@ -373,14 +417,13 @@ def batched_mode(ctx, args, dev, seed=7):
                      # (the batched views all complete at the batch's end)
                      "completion_p50_ms": float(np.percentile(plain_done, 50)),
                      "completion_p99_ms": float(np.percentile(plain_done, 99))},
-           "batched": {"frames_per_s": 1000.0 * n / batch_ms.mean(),
-                       "batch_ms_p50": float(np.percentile(batch_ms, 50)),
-                       "batch_ms_p99": float(np.percentile(batch_ms, 99)),
-                       "raycast_ms_mean": float(np.mean(ray_ms)),
-                       "samples_per_batch": samples, "pixels_per_batch": pixels,
-                       "autotuned": cfg, "autotune_s": tune_s,
-                       "gpu_launches_per_batch": int(stats[0]["n_launches"])}}
-    out["speedup_frames_per_s"] = out["batched"]["frames_per_s"] / out["plain"]["frames_per_s"]
+           "batched": best, "persistent": persistent, "autotune_s": tune_s,
+           # every configuration the autotuner ran: queue kind, tile, order,
+           # TF staging, look-ahead, refill interval -> mean ray-cast ms
+           "autotune_table": [[queue_names.get(c["queue"], c["queue"]), c["tile_w"], c["tile_h"],
+                               c["order"], c["tf_shared"], c["lookahead"],
+                               c["samples_per_check"], round(ms, 3)] for c, ms in table]}
+    out["speedup_frames_per_s"] = best["frames_per_s"] / out["plain"]["frames_per_s"]
     batch.close()
     for v, _ in vols:
         v.close()
@@ -396,12 +439,17 @@ def served_mode(ctx, args, dev, seed=11):
     import torch
     import livre_gb300 as lv
     rng = np.random.default_rng(seed)
-    specs = [(256, lv.DT_UINT8), (512, lv.DT_UINT8), (512, lv.DT_UINT16), (1024, lv.DT_UINT8),
-             (1024, lv.DT_UINT16), (2048, lv.DT_UINT8), (2048, lv.DT_UINT16), (4096, lv.DT_UINT8)]
+    # (edge, type, generator): blob volumes and two fBm volumes (device fBm)
+    specs = [(256, lv.DT_UINT8, "blob"), (512, lv.DT_UINT8, "blob"), (512, lv.DT_UINT16, "fbm"),
+             (1024, lv.DT_UINT8, "blob"), (1024, lv.DT_UINT16, "blob"),
+             (2048, lv.DT_UINT8, "fbm"), (2048, lv.DT_UINT16, "blob"), (4096, lv.DT_UINT8, "blob")]
     vols = []
-    for k, (n, dt) in enumerate(specs):
+    for k, (n, dt, gen) in enumerate(specs):
         vi = lv.VolumeInformation(n, 64, 1, dtype=dt)
-        vols.append((ctx.blob_volume(vi, int(rng.integers(64, 513)), 300 + k, noise=4), vi))
+        if gen == "fbm":
+            vols.append((ctx.fbm_volume(vi, 300 + k, octaves=6, frequency=8.0), vi))
+        else:
+            vols.append((ctx.blob_volume(vi, int(rng.integers(64, 513)), 300 + k, noise=4), vi))
     tfs = [ctx.transfer_function(lv.gaussian_peaks_tf(256, seed=100 + k)) for k in range(16)]
     viewports = [(512, 512), (1920, 1080), (3840, 2160)]
 
@@ -464,8 +512,9 @@ def served_mode(ctx, args, dev, seed=11):
     for v, t, d in warm:
         ctx.render(v, t, d, take(d.width, d.height))
     ctx.last_stats()
-    out = {"volumes": "8 blob volumes 256^3..4096^3 u8/u16, 64^3 bricks",
-           "pool_gib": args.pool_gib or 96, "rates": []}
+    out = {"volumes": "8 volumes 256^3..4096^3 u8/u16, 64^3 bricks: 6 blob, 2 fBm "
+                      "(512^3 u16, 2048^3 u8)",
+           "pool_gib": args.pool_gib or 96, "slo_p99_ms": args.slo_ms, "rates": []}
     for rate in args.serve_rates:
         reqs = [make_request() for _ in range(max(64, int(rate * args.serve_seconds)))]
         # every brick the stream needs made resident first, so neither mode
@@ -476,6 +525,14 @@ def served_mode(ctx, args, dev, seed=11):
         served = run(0, rate, reqs)
         plain = run(1, rate, reqs)
         out["rates"].append({"served": served, "plain": plain})
+    # capacity at the latency objective: the highest offered rate whose p99
+    # stays within it, and the frames/s delivered there
+    for mode in ("served", "plain"):
+        ok = [r[mode] for r in out["rates"] if r[mode]["p99_ms"] <= args.slo_ms]
+        top = max(ok, key=lambda r: r["rate_req_s"]) if ok else None
+        out["capacity_%s" % mode] = ({"rate_req_s": top["rate_req_s"],
+                                      "frames_per_s": top["frames_per_s"],
+                                      "p99_ms": top["p99_ms"]} if top else None)
     for v, _ in vols:
         v.close()
     for t in tfs:
@@ -587,6 +644,47 @@ def outofcore_mode(local, args, dev):
     return res
 
 
+# ------------------------------------------------------ launch sweep
+def launch_sweep(ctx, vol, tf, descs, dev, frames=64):
+    """Mean ray-cast time of the headline workload's orbit (every brick
+    resident, no L2 flush) for each lv_render launch shape, then the default
+    launch restored: {name: ms}."""
+    import numpy as np
+    import torch
+    import livre_gb300 as lv
+    default = ctx.render_launch()
+    G, T, Q, W, R = (lv.LAUNCH_GRID, lv.LAUNCH_TILE_GRID, lv.LAUNCH_TILE_QUEUE,
+                     lv.LAUNCH_WARP_TILES, lv.LAUNCH_WARP_REFILL)
+    LF, RA = lv.ORDER_LONGEST_FIRST, lv.ORDER_RASTER
+    shapes = [("tile_grid 8x16 longest-first look-ahead", T, 8, 16, 0, LF, 1),
+              ("tile_grid 8x16 longest-first", T, 8, 16, 0, LF, 0),
+              ("tile_grid 8x8 longest-first look-ahead", T, 8, 8, 0, LF, 1),
+              ("tile_grid 8x4 longest-first look-ahead", T, 8, 4, 0, LF, 1),
+              ("tile_grid 16x8 longest-first look-ahead", T, 16, 8, 0, LF, 1),
+              ("tile_grid 16x16 longest-first look-ahead", T, 16, 16, 0, LF, 1),
+              ("tile_grid 32x8 longest-first look-ahead", T, 32, 8, 0, LF, 1),
+              ("tile_grid 8x16 raster look-ahead", T, 8, 16, 0, RA, 1),
+              ("grid 8x16 (hardware-scheduled blocks) look-ahead", G, 8, 16, 0, RA, 1),
+              ("warp_tiles 8x4 longest-first look-ahead", W, 8, 4, 0, LF, 1),
+              ("tile_queue 8x16 longest-first look-ahead", Q, 8, 16, 0, LF, 1),
+              ("warp_refill 8x4 every 8 samples", R, 8, 4, 8, RA, 0)]
+    out = {}
+    out_t = torch.empty((descs[0].height, descs[0].width, 4), dtype=torch.float32, device=dev)
+    for name, kind, tw, th, spc, order, la in shapes:
+        ctx.set_render_launch(kind, tw, th, spc, order, la)
+        for d in descs[:4]:
+            ctx.render(vol, tf, d, out_t)
+            ctx.last_stats()
+        ray = []
+        for k in range(frames):
+            ctx.render(vol, tf, descs[k % len(descs)], out_t)
+            ray.append(ctx.last_stats()["raycast_ms"])
+        out[name] = round(float(np.mean(ray)), 4)
+    ctx.set_render_launch(default["kind"], default["tile_w"], default["tile_h"],
+                          default["samples_per_check"], default["order"], default["lookahead"])
+    return out
+
+
 # ------------------------------------------------ plain 256^3 and parity
 def plain256_mode(local, args, dev, steps=64):
     """The CPU-runnable plain workload (256^3 uint8, 32^3 bricks, 16 blobs,
@@ -693,6 +791,114 @@ def parity_mode(ctx, vol, tf, cfg, args, dev):
             res[args.config].append(compare(cpu2, img, k, st, rows=(r0, r0 + 16)))
     res["max_err_255"] = max(r["max_err_255"] for key in ("plain256", args.config)
                              for r in res[key])
+    return res
+
+
+def outofcore_host_mode(local, args, dev):
+    """The out-of-core fly-through with its bricks generated on the host, as
+    the configuration states: a callback volume (a data-source plugin's
+    getData) served from a brick store that a producer thread fills ahead of
+    the path with the host fBm generator (lv_fbm_brick, every host thread),
+    one frame ahead of the frame being rendered. Frame 0 (about 7 000 bricks)
+    is filled from the device generator, which produces the same bytes, so
+    the timed frames 1.. measure the host-fed steady state."""
+    import ctypes
+    import queue as queue_
+    import numpy as np
+    import torch
+    import livre_gb300 as lv
+    W, H, n_path = 1920, 1080, 128
+    frames = max(2, args.ooc_host_frames + 1)
+    ctx = lv.Context(local, pool_bytes=args.ooc_pool_gib << 30)
+    vi = lv.VolumeInformation(args.ooc_voxels, 128, 1, dtype=lv.DT_UINT16)
+    seed = 3
+    store, ready = {}, threading.Condition()
+    stats = {"host_bricks": 0, "host_s": 0.0, "waits": 0, "served": 0}
+
+    def put(nid, data):
+        with ready:
+            store[nid] = data
+            ready.notify_all()
+
+    def get_data(node_id, dst, nbytes):
+        with ready:
+            if node_id not in store:
+                stats["waits"] += 1
+                # the producer is on it; a brick it never schedules is
+                # generated here after a bounded wait
+                ready.wait_for(lambda: node_id in store, timeout=60.0)
+            data = store.get(node_id)
+            stats["served"] += 1
+        if data is None:
+            data = lv.fbm_brick(vi, node_id, seed, n_threads=1)
+        ctypes.memmove(dst, data.ctypes.data, nbytes)
+        return True
+
+    vol = ctx.callback_volume(vi, get_data)
+    vol.fetch_threads = 0
+    tf = ctx.transfer_function(lv.gaussian_peaks_tf(4096, seed=12))
+    out = torch.empty((H, W, 4), dtype=torch.float32, device=dev)
+    descs, visible = [], []
+    for k in range(frames):
+        mv, proj = fly_through(k, n_path, W, H)
+        descs.append(ctx.render_desc(mv, proj, W, H, sse=1.0, step_policy=lv.STEP_REFERENCE,
+                                     early_exit=0.999))
+        ids, _ = ctx.select_visible(vi, mv, proj, H, 1.0)
+        visible.append([int(i) for i in ids])
+    # frame 0: device generator (same bytes), into the store
+    first = visible[0]
+    for a in range(0, len(first), 256):
+        chunk = first[a:a + 256]
+        dev_bricks = ctx.fbm_bricks(vi, chunk, seed).cpu().numpy()
+        for nid, b in zip(chunk, dev_bricks):
+            put(nid, b)
+    jobs = queue_.Queue()
+
+    def producer():
+        while True:
+            k = jobs.get()
+            if k is None:
+                return
+            for nid in visible[k]:
+                with ready:
+                    have = nid in store
+                if have:
+                    continue
+                t0 = time.perf_counter()
+                b = lv.fbm_brick(vi, nid, seed, n_threads=0)
+                stats["host_s"] += time.perf_counter() - t0
+                stats["host_bricks"] += 1
+                put(nid, b)
+
+    th = threading.Thread(target=producer, daemon=True)
+    th.start()
+    jobs.put(1)  # prefetch one frame ahead of the path
+    rows = []
+    for k in range(frames):
+        t0 = time.perf_counter()
+        ctx.render(vol, tf, descs[k], out)
+        st = ctx.last_stats()
+        rows.append((time.perf_counter() - t0, st))
+        if k + 2 < frames:
+            jobs.put(k + 2)
+    jobs.put(None)
+    th.join()
+    timed = rows[1:]
+    wall = np.array([r[0] for r in timed])
+    res = {"workload": "outofcore_%dc_u16_128b_1080p_flythrough128_hostgen" % args.ooc_voxels,
+           "generator": "host fBm (lv_fbm_brick, %d threads) for frames 1..%d, prefetched one "
+                        "frame ahead of the path; frame 0 from the device generator (same "
+                        "bytes)" % (os.cpu_count(), frames - 1),
+           "timed_frames": len(timed), "frames_per_s": float(len(timed) / wall.sum()),
+           "frame_s": [round(float(x), 3) for x in wall],
+           "streamed_bricks_per_frame": float(np.mean([r[1]["n_uploaded"] for r in timed])),
+           "host_generated_bricks": stats["host_bricks"],
+           "host_bricks_per_s": stats["host_bricks"] / max(stats["host_s"], 1e-9),
+           "fetch_waits_for_producer": stats["waits"],
+           "raycast_ms_mean": float(np.mean([r[1]["raycast_ms"] for r in timed]))}
+    vol.close()
+    tf.close()
+    ctx.close()
     return res
 
 
@@ -859,6 +1065,10 @@ def gb300_arm(args, cfg):
         sctx.close()
     if "outofcore" in modes:
         line["outofcore"] = outofcore_mode(local, args, dev)
+    if "outofcore_host" in modes:
+        line["outofcore_host"] = outofcore_host_mode(local, args, dev)
+    if "launches" in modes:
+        line["launch_sweep_raycast_ms"] = launch_sweep(ctx, vol, tf, descs, dev)
     if "plain256" in modes:
         line["plain256"] = plain256_mode(local, args, dev)
     if "parity" in modes:

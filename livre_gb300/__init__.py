@@ -832,6 +832,16 @@ class Batch:
                                       C.byref(c)), self.ctx.handle)
         return c.as_dict()
 
+    def autotune_results(self):
+        """[(config dict, mean ray-cast ms)] of every configuration the last
+        autotune ran."""
+        n = C.c_uint32()
+        check(lib().lv_batch_autotune_results(self.handle, None, None, 0, C.byref(n)))
+        cfgs = (_abi.BatchConfig * max(n.value, 1))()
+        ms = (C.c_float * max(n.value, 1))()
+        check(lib().lv_batch_autotune_results(self.handle, cfgs, ms, n.value, C.byref(n)))
+        return [(cfgs[i].as_dict(), float(ms[i])) for i in range(n.value)]
+
 
 class Server:
     """Render server (lv_server): continuous batching or plain per-request."""

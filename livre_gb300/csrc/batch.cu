@@ -107,6 +107,9 @@ struct lv_batch
     uint32_t last_n = 0;
     uint32_t sel_generation = 0; /* b->sel.generation the cached graphs use */
     uint64_t captures = 0, replays = 0;
+    /* the last lv_batch_autotune: every candidate and its mean ray-cast ms */
+    std::vector<lv_batch_config> tune_cfgs;
+    std::vector<float> tune_ms;
 
     ~lv_batch()
     {
@@ -487,14 +490,25 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         const uint32_t n_streams = std::min<uint32_t>(n, kViewStreams);
         for (uint32_t k = 0; k < n_streams; ++k)
             LV_CUDA(ctx, cudaStreamWaitEvent(aux[k], b->fork, 0));
+        /* the views with the most pixels first, dealt round-robin over the
+         * streams: the costliest views start at once instead of queueing
+         * behind light ones, which shortens the batch and the latency of
+         * its heaviest requests */
+        std::vector<uint32_t> by_cost(n);
         for (uint32_t i = 0; i < n; ++i)
+            by_cost[i] = i;
+        std::stable_sort(by_cost.begin(), by_cost.end(), [&](uint32_t a, uint32_t c) {
+            return uint64_t(h_rays[a].W) * h_rays[a].H > uint64_t(h_rays[c].W) * h_rays[c].H;
+        });
+        for (uint32_t j = 0; j < n; ++j)
         {
+            const uint32_t i = by_cost[j];
             if (h_rays[i].W == 0) /* padding view */
                 continue;
             uint8_t* scratch = b->cfg.order == LV_ORDER_LONGEST_FIRST
                                    ? b->view_scratch.as<uint8_t>() + offs[i]
                                    : nullptr;
-            cudaStream_t vs = aux[i % n_streams];
+            cudaStream_t vs = aux[j % n_streams];
             st = launch_view_raycast(ctx, h_rays[i], L, scratch, vs);
             if (st != LV_OK)
                 return st;
@@ -953,6 +967,8 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
     lv_batch_config best = start;
     float best_ms = 1e30f;
     reps = reps ? reps : 3;
+    b->tune_cfgs.clear();
+    b->tune_ms.clear();
     for (const lv_batch_config& cfg : cands)
     {
         if (lv_batch_set_config(b, &cfg) != LV_OK)
@@ -971,6 +987,11 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
             if (r > 0)
                 total += ray;
         }
+        if (ok)
+        {
+            b->tune_cfgs.push_back(cfg);
+            b->tune_ms.push_back(total / reps);
+        }
         if (ok && total / reps < best_ms)
         {
             best_ms = total / reps;
@@ -981,4 +1002,20 @@ extern "C" lv_status lv_batch_autotune(lv_batch* b, const lv_batch_view* views, 
     if (chosen)
         *chosen = best;
     return best_ms < 1e30f ? LV_OK : fail(b->ctx, LV_EINVAL, "no configuration ran");
+}
+
+extern "C" lv_status lv_batch_autotune_results(const lv_batch* b, lv_batch_config* configs,
+                                               float* raycast_ms, uint32_t capacity,
+                                               uint32_t* n)
+{
+    if (!b || !n || (capacity && (!configs || !raycast_ms)))
+        return LV_EINVAL;
+    *n = uint32_t(b->tune_cfgs.size());
+    const uint32_t k = std::min<uint32_t>(capacity, *n);
+    for (uint32_t i = 0; i < k; ++i)
+    {
+        configs[i] = b->tune_cfgs[i];
+        raycast_ms[i] = b->tune_ms[i];
+    }
+    return LV_OK;
 }
