@@ -14,7 +14,7 @@
  *      and their misses streamed on the upload stream;
  *   3. renders the admitted requests as one lv_batch_render (all bricks
  *      resident, so each result equals the same request rendered alone).
- * Two lv_batch objects alternate, so step 2 for the next batch runs while the
+ * Four lv_batch objects take turns, so step 2 for the next batch runs while the
  * previous one renders. Mode LV_SERVE_PLAIN instead renders every request
  * alone with lv_render (synchronous residency), the per-request baseline.
  *
@@ -87,6 +87,12 @@ struct lv_server_hook
 };
 } // namespace
 
+/* Batches in flight at once: a batch is admitted and launched while up to
+ * kSlots - 1 earlier ones still render (each later one on lower-priority
+ * streams), so a heavy batch does not hold back the requests queued behind
+ * it. */
+constexpr int kSlots = 4;
+
 struct lv_server
 {
     lv_ctx* ctx = nullptr;
@@ -98,15 +104,15 @@ struct lv_server
     std::unordered_map<uint64_t, Req*> reqs;
     uint64_t next_ticket = 1;
     bool stop = false;
-    lv_batch* batches[2] = {nullptr, nullptr};
+    lv_batch* batches[kSlots] = {};
     int cur = 0;
     std::deque<Inflight> inflight;
     std::vector<cudaEvent_t> free_events;
     cudaStream_t sel_stream = nullptr;
     /* one launch stream per batch object: consecutive batches overlap */
-    cudaStream_t launch_stream[2] = {nullptr, nullptr};
-    lv_server_hook hooks[2];
-    std::vector<uint64_t> current[2]; /* tickets of the views in flight per batch object */
+    cudaStream_t launch_stream[kSlots] = {};
+    lv_server_hook hooks[kSlots];
+    std::vector<uint64_t> current[kSlots]; /* tickets of the views in flight per batch object */
     cudaEvent_t uploads_done = nullptr;
     /* dry-run selection buffers */
     SelectScratch sel;
@@ -407,7 +413,7 @@ void loop_batched(lv_server* S)
                 S->cv.wait(lk, [&] { return S->stop || !S->queue.empty(); });
                 continue;
             }
-            if (S->inflight.size() >= 2)
+            if (S->inflight.size() >= kSlots)
             {
                 Inflight f = S->inflight.front();
                 S->inflight.pop_front();
@@ -479,7 +485,7 @@ void loop_batched(lv_server* S)
         }
         const int bi = S->cur;
         lv_batch* b = S->batches[bi];
-        S->cur ^= 1;
+        S->cur = (S->cur + 1) % kSlots;
         cudaStream_t ls = S->launch_stream[bi];
         Inflight f;
         f.batch = b;
@@ -588,14 +594,18 @@ extern "C" lv_status lv_server_create(lv_ctx* ctx, const lv_server_config* cfg, 
     cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     if (cudaStreamCreateWithPriority(&S->sel_stream, cudaStreamNonBlocking, hi_prio) !=
             cudaSuccess ||
-        cudaStreamCreateWithFlags(&S->launch_stream[0], cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&S->launch_stream[1], cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&S->uploads_done, cudaEventDisableTiming) != cudaSuccess)
     {
         delete S;
         return fail(ctx, LV_EDEVICE, "server streams");
     }
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < kSlots; ++i)
+        if (cudaStreamCreateWithFlags(&S->launch_stream[i], cudaStreamNonBlocking) != cudaSuccess)
+        {
+            delete S;
+            return fail(ctx, LV_EDEVICE, "server streams");
+        }
+    for (int i = 0; i < kSlots; ++i)
     {
         lv_status st = lv_batch_create(ctx, &S->batches[i]);
         if (st != LV_OK)
@@ -723,7 +733,7 @@ extern "C" void lv_server_destroy(lv_server* S)
             cudaStreamSynchronize(ls); /* host functions done */
         complete(S, f);
     }
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < kSlots; ++i)
         lv_batch_destroy(S->batches[i]);
     for (cudaEvent_t e : S->free_events)
         cudaEventDestroy(e);
