@@ -80,9 +80,11 @@ def parse():
                         "default list: host generation takes tens of seconds per frame)")
     p.add_argument("--cpu-frames", type=int, default=2,
                    help="whole frames the CPU baseline of the default line ray casts")
-    p.add_argument("--serve-seconds", type=float, default=1.5)
+    p.add_argument("--serve-seconds", type=float, default=3.0,
+                   help="request stream length per rate below 1000 req/s (half of it "
+                        "from 1000 req/s: the saturated rates)")
     p.add_argument("--serve-rates", type=lambda t: [int(x) for x in t.split(",")],
-                   default=[200, 250, 300, 350, 400, 450, 500, 1000, 2000],
+                   default=[200, 250, 300, 350, 400, 450, 500, 550, 600, 2000],
                    help="Poisson request rates (req/s)")
     p.add_argument("--slo-ms", type=float, default=150.0,
                    help="p99 latency objective of the serving capacity figure")
@@ -473,13 +475,22 @@ def served_mode(ctx, args, dev, seed=11):
         ring_pos[(W, H)] = (k + 1) % len(ring)
         return ring[k]
 
+    # One request sequence and one sequence of unit-rate exponential gaps for
+    # every rate and both modes (common random numbers): a rate's stream is a
+    # prefix of the requests arriving at gaps / rate, so the two modes and
+    # neighbouring rates see the same mix of volumes, viewports and LODs.
+    counts = {rate: max(64, int(rate * args.serve_seconds * (0.5 if rate >= 1000 else 1.0)))
+              for rate in args.serve_rates}
+    pool = [make_request() for _ in range(max(counts.values()))]
+    gaps = rng.exponential(1.0, len(pool))
+
     def run(mode, rate, reqs):
         srv = lv.Server(ctx, mode=mode, max_batch=64, max_pixels=16 << 20)
         # warm-up burst (graph captures, per-batch buffers), not timed
         for tk in [srv.submit(v, t, d, take(d.width, d.height)) for v, t, d in reqs[:64]]:
             srv.wait(tk, 600000)
         prof0 = srv.profile()
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs)))
+        arrivals = np.cumsum(gaps[:len(reqs)]) / rate
         tickets, outs = [], []
         t0 = time.perf_counter()
         for (v, t, d), at in zip(reqs, arrivals):
@@ -516,7 +527,7 @@ def served_mode(ctx, args, dev, seed=11):
                       "(512^3 u16, 2048^3 u8)",
            "pool_gib": args.pool_gib or 96, "slo_p99_ms": args.slo_ms, "rates": []}
     for rate in args.serve_rates:
-        reqs = [make_request() for _ in range(max(64, int(rate * args.serve_seconds)))]
+        reqs = pool[:counts[rate]]
         # every brick the stream needs made resident first, so neither mode
         # pays (or is spared) streaming the other mode already did
         for v, t, d in reqs:

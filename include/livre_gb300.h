@@ -544,8 +544,11 @@ enum
     LV_QUEUE_VIEW_KERNELS = 2 /* one ray cast per view (lv_render's one-CTA-per-
                                  tile kernel, view constants as kernel
                                  parameters) on parallel streams, so a view's
-                                 last tiles overlap the next view; no CUDA
-                                 graph. The default. */
+                                 last tiles overlap the next view. With
+                                 use_graph the whole batch is captured on
+                                 every call and applied to the cached
+                                 executable graph (cudaGraphExecUpdate): one
+                                 graph launch per batch. The default. */
 };
 
 /* Launch shape of the persistent ray-cast kernel. */
@@ -592,10 +595,13 @@ lv_status lv_batch_render(lv_batch* batch, const lv_batch_view* views,
  * (device global timer, first CTA start to last CTA end). */
 lv_status lv_batch_stats(lv_batch* batch, lv_frame_stats* out, uint32_t n,
                          float* batch_ms, float* raycast_ms);
-/* CUDA-graph cache of a batch: graphs captured and launches replayed so
- * far, and the graphs held now. A batch of n views runs as a launch for the
- * next power of two (padded with empty views), so batch sizes 1..64 share 7
- * graphs per set of kernel variants. */
+/* CUDA-graph cache of a batch: graphs instantiated (`captures`) and
+ * launches of an already instantiated graph (`replays`) so far, and the
+ * graphs held now. Persistent queues: a batch of n views runs as a launch
+ * for the next power of two (padded with empty views), so batch sizes 1..64
+ * share 7 graphs per set of kernel variants, replayed as captured. Per-view
+ * kernels: every call is captured and, when its graph has the cached one's
+ * topology, applied to it by an update and counted as a replay. */
 lv_status lv_batch_graph_stats(lv_batch* batch, uint64_t* captures,
                                uint64_t* replays, uint32_t* cached);
 /* Times the persistent ray cast on this batch (reps timed launches each)

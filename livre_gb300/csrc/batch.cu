@@ -6,9 +6,13 @@
  *  - one residency pass, prune and leaf-grid splat over all views
  *    (blockIdx.y = view),
  *  - one persistent ray-cast launch per voxel type / filter, whose CTAs pop
- *    (view, tile) items from a device work queue,
- *  - the whole sequence is captured once into a CUDA graph and replayed; the
- *    per-view constants travel in one host->device copy inside the graph.
+ *    (view, tile) items from a device work queue, or one ray-cast kernel per
+ *    view on parallel streams (LV_QUEUE_VIEW_KERNELS),
+ *  - the whole sequence runs as one CUDA graph launch: persistent queues are
+ *    captured once and replayed (the per-view constants travel in one
+ *    host->device copy inside the graph); per-view kernels, whose constants
+ *    and grids are launch parameters, are captured on every call and applied
+ *    to the cached executable graph by an update.
  *
  * Residency follows the reference's asynchronous mode (RenderPipeline::
  * renderAsync, livre/lib/pipeline/RenderPipeline.cpp:160-225): missing bricks
@@ -69,8 +73,10 @@ struct lv_batch
     cudaStream_t aux_low[kGroups] = {}; /* lowest priority: a batch overlapping another */
     bool low_priority = false;
     cudaEvent_t fork = nullptr, join[kGroups] = {};
-    /* per-view kernels: tile-order scratch and ray-cast timing */
+    /* per-view kernels: tile-order scratch (offset of each view's region)
+     * and ray-cast timing */
     lv::DeviceBuffer view_scratch;
+    std::vector<uint64_t> view_offs;
     cudaEvent_t t_vk0 = nullptr, t_vk1 = nullptr;
     bool vk_timed = false;
     /* per-view completion hook (per-view kernels only) */
@@ -106,7 +112,7 @@ struct lv_batch
     uint32_t launches = 0;
     uint32_t last_n = 0;
     uint32_t sel_generation = 0; /* b->sel.generation the cached graphs use */
-    uint64_t captures = 0, replays = 0;
+    uint64_t captures = 0, replays = 0, updates = 0;
     /* the last lv_batch_autotune: every candidate and its mean ray-cast ms */
     std::vector<lv_batch_config> tune_cfgs;
     std::vector<float> tune_ms;
@@ -172,6 +178,9 @@ ParamLayout param_layout(uint32_t n)
     return L;
 }
 
+/* bytes of one view's id, slot and stamp lists */
+uint64_t lists_per_view(const lv_batch* b) { return b->nodes_stride * (8 + 8 + 4 + 4); }
+
 constexpr uint64_t kOrderHistBytes = 2 * 64 * sizeof(uint32_t);
 uint64_t order_keys_bytes(uint32_t cap) { return (uint64_t(cap) + 255) & ~uint64_t(255); }
 uint64_t order_region_bytes(uint32_t cap)
@@ -236,14 +245,16 @@ lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
     LV_CUDA(ctx, b->h_params.reserve(PL.bytes));
     LV_CUDA(ctx, b->zeroed.reserve(sizeof(uint32_t) * (kOutWords * vcap + 64)));
     LV_CUDA(ctx, b->leafs.reserve(sizeof(uint32_t) * b->cells_stride * vcap));
-    /* visible + render ids (u64) + render slots + view stamps (u32) + missing */
-    const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
+    /* per view: visible + render ids (u64) + render slots + view stamps
+     * (u32); then the missing lists of all views, contiguous so that one
+     * plain copy brings them to the host */
+    const uint64_t lists_bytes = lists_per_view(b) * vcap + b->missing_stride * 8 * vcap;
     b->lists.release();
-    LV_CUDA(ctx, b->lists.reserve(per_view * vcap));
+    LV_CUDA(ctx, b->lists.reserve(lists_bytes));
     LV_CUDA(ctx, b->h_out.reserve(sizeof(uint32_t) * (kOutWords * vcap + 64) +
                                   sizeof(uint64_t) * b->missing_stride * vcap));
     /* view stamps start at 0; launch ids start at 1 */
-    LV_CUDA(ctx, cudaMemset(b->lists.ptr, 0, per_view * vcap));
+    LV_CUDA(ctx, cudaMemset(b->lists.ptr, 0, lists_bytes));
     for (auto& kv : b->graphs)
         cudaGraphExecDestroy(kv.second);
     b->graphs.clear();
@@ -253,14 +264,13 @@ lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
 
 ViewSlots view_slots(const lv_batch* b, uint32_t i)
 {
-    const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
-    const uint64_t base = per_view * i;
+    const uint64_t base = lists_per_view(b) * i;
     ViewSlots s;
     s.visible = base;
     s.render_ids = base + b->nodes_stride * 8;
     s.render_slots = s.render_ids + b->nodes_stride * 8;
     s.view_stamp = s.render_slots + b->nodes_stride * 4;
-    s.missing = s.view_stamp + b->nodes_stride * 4;
+    s.missing = lists_per_view(b) * b->views_cap + b->missing_stride * 8 * i;
     s.leaf = uint64_t(i) * b->cells_stride * 4;
     return s;
 }
@@ -429,6 +439,45 @@ lv_status fill_params(lv_batch* b, const lv_batch_view* views, uint32_t n, uint3
     return LV_OK;
 }
 
+/* Per-view kernels: each view's tile-order region in view_scratch and the
+ * host words and hook arguments of its completion, sized before the launch
+ * is enqueued (or captured: nothing here may run inside a capture). */
+lv_status prepare_view_kernels(lv_batch* b, uint32_t n)
+{
+    lv_ctx* ctx = b->ctx;
+    const ParamLayout PL = param_layout(b->views_cap);
+    const RayView* h_rays = reinterpret_cast<const RayView*>(b->h_params.as<uint8_t>() + PL.ray);
+    const lv_render_launch L{LV_LAUNCH_TILE_GRID, b->cfg.tile_w, b->cfg.tile_h, 0,
+                             b->cfg.order, b->cfg.lookahead};
+    b->view_offs.assign(n + 1, 0);
+    for (uint32_t i = 0; i < n; ++i)
+        b->view_offs[i + 1] =
+            b->view_offs[i] + ((tile_order_bytes(h_rays[i], L) + 255) & ~size_t(255));
+    if (b->cfg.order == LV_ORDER_LONGEST_FIRST && b->view_scratch.bytes < b->view_offs[n])
+    {
+        LV_CUDA(ctx, cudaStreamSynchronize(b->stream));
+        LV_CUDA(ctx, b->view_scratch.reserve(b->view_offs[n] + b->view_offs[n] / 2));
+    }
+    if (b->hook)
+    {
+        LV_CUDA(ctx, b->h_view_words.reserve(sizeof(uint32_t) * kOutWords * n));
+        b->hook_args.resize(n);
+        for (uint32_t i = 0; i < n; ++i)
+            b->hook_args[i] = lv_batch::HookArg{b, i};
+    }
+    return LV_OK;
+}
+
+/* A timing event on `s`: inside a stream capture it becomes an event-record
+ * node of the graph (recorded on every replay), else a plain record. */
+cudaError_t record_time(cudaEvent_t e, cudaStream_t s)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+        return cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    return cudaEventRecord(e, s);
+}
+
 void CUDART_CB view_done_trampoline(void* p)
 {
     const auto* a = static_cast<const lv_batch::HookArg*>(p);
@@ -470,22 +519,10 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         const RayView* h_rays = reinterpret_cast<const RayView*>(b->h_params.as<uint8_t>() + PL.ray);
         const lv_render_launch L{LV_LAUNCH_TILE_GRID, b->cfg.tile_w, b->cfg.tile_h, 0,
                                  b->cfg.order, b->cfg.lookahead};
-        std::vector<uint64_t> offs(n + 1, 0);
-        for (uint32_t i = 0; i < n; ++i)
-            offs[i + 1] = offs[i] + ((tile_order_bytes(h_rays[i], L) + 255) & ~size_t(255));
-        if (b->cfg.order == LV_ORDER_LONGEST_FIRST && b->view_scratch.bytes < offs[n])
-        {
-            LV_CUDA(ctx, cudaStreamSynchronize(s));
-            LV_CUDA(ctx, b->view_scratch.reserve(offs[n] + offs[n] / 2));
-        }
-        if (b->hook)
-        {
-            LV_CUDA(ctx, b->h_view_words.reserve(sizeof(uint32_t) * kOutWords * n));
-            b->hook_args.resize(n);
-            for (uint32_t i = 0; i < n; ++i)
-                b->hook_args[i] = lv_batch::HookArg{b, i};
-        }
-        LV_CUDA(ctx, cudaEventRecord(b->t_vk0, s));
+        const std::vector<uint64_t>& offs = b->view_offs; /* prepare_view_kernels */
+        if (offs.size() < size_t(n) + 1 || (b->hook && b->hook_args.size() < n))
+            return fail(ctx, LV_EINVAL, "view-kernel batch not prepared");
+        LV_CUDA(ctx, record_time(b->t_vk0, s));
         LV_CUDA(ctx, cudaEventRecord(b->fork, s));
         const uint32_t n_streams = std::min<uint32_t>(n, kViewStreams);
         for (uint32_t k = 0; k < n_streams; ++k)
@@ -527,7 +564,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
             LV_CUDA(ctx, cudaEventRecord(b->join[k], aux[k]));
             LV_CUDA(ctx, cudaStreamWaitEvent(s, b->join[k], 0));
         }
-        LV_CUDA(ctx, cudaEventRecord(b->t_vk1, s));
+        LV_CUDA(ctx, record_time(b->t_vk1, s));
         b->vk_timed = true;
     }
     const bool ordered = b->cfg.order == LV_ORDER_LONGEST_FIRST;
@@ -576,12 +613,10 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     LV_CUDA(ctx, cudaMemcpyAsync(b->h_out.ptr, b->zeroed.ptr,
                                  sizeof(uint32_t) * (kOutWords * n + kGroups + 4),
                                  cudaMemcpyDeviceToHost, s));
-    /* missing lists, one strided copy */
+    /* missing lists, one copy */
     uint8_t* hmiss = b->h_out.as<uint8_t>() + sizeof(uint32_t) * (kOutWords * b->views_cap + 64);
-    const uint64_t per_view = b->nodes_stride * (8 + 8 + 4 + 4) + b->missing_stride * 8;
-    LV_CUDA(ctx, cudaMemcpy2DAsync(hmiss, b->missing_stride * 8,
-                                   b->lists.as<uint8_t>() + view_slots(b, 0).missing, per_view,
-                                   b->missing_stride * 8, n, cudaMemcpyDeviceToHost, s));
+    LV_CUDA(ctx, cudaMemcpyAsync(hmiss, b->lists.as<uint8_t>() + view_slots(b, 0).missing,
+                                 b->missing_stride * 8 * n, cudaMemcpyDeviceToHost, s));
     return LV_OK;
 }
 
@@ -743,8 +778,9 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     /* the host staging is read by the previous launch until it completes */
     LV_CUDA(ctx, cudaEventSynchronize(b->done));
     uint32_t n_run = n;
-    const bool graphed = b->cfg.use_graph && b->cfg.queue != LV_QUEUE_VIEW_KERNELS;
-    if (graphed)
+    const bool graphed = b->cfg.use_graph != 0;
+    const bool vk = b->cfg.queue == LV_QUEUE_VIEW_KERNELS;
+    if (graphed && !vk)
         while (n_run & (n_run - 1))
             n_run += n_run & (~n_run + 1); /* round up to a power of two */
     st = ensure_regions(b, views, n, user, n_run);
@@ -778,6 +814,8 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
     st = ensure_order(b, max_items);
     if (st != LV_OK)
         return st;
+    if (vk && (st = prepare_view_kernels(b, n)) != LV_OK)
+        return st;
     if (b->cfg.tf_shared && tfn_max > 2048)
         return fail(ctx, LV_EINVAL, "shared-memory transfer functions hold at most 2048 entries");
     uint32_t mask = 0;
@@ -796,13 +834,15 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
             b->cfg.tf_shared ? tfn_max : 0u, b->depth_max, b->generation,
             uintptr_t(b->sel.generation));
         auto it = b->graphs.find(key);
-        if (it == b->graphs.end())
+        /* Persistent kernels read every per-launch value from the copied
+         * parameter block, so a cached graph replays as captured. Per-view
+         * kernels take their view's constants and grid as launch
+         * parameters: the batch is captured on every call and the capture
+         * applied to the cached executable graph (cudaGraphExecUpdate), which
+         * keeps the instantiated graph while its topology (views, streams,
+         * hooks) is unchanged; otherwise the graph is instantiated anew. */
+        if (it == b->graphs.end() || vk)
         {
-            if (b->graphs.size() >= 32)
-            {
-                cudaGraphExecDestroy(b->graphs.begin()->second);
-                b->graphs.erase(b->graphs.begin());
-            }
             cudaGraph_t g = nullptr;
             LV_CUDA(ctx, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
             st = enqueue_batch(b, n_run, groups, total_roots, tfn_max);
@@ -814,12 +854,40 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
                 return st;
             }
             LV_CUDA(ctx, ce);
-            cudaGraphExec_t exec = nullptr;
-            const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+            if (it != b->graphs.end())
+            {
+                cudaGraphExecUpdateResultInfo info{};
+                if (cudaGraphExecUpdate(it->second, g, &info) == cudaSuccess)
+                {
+                    ++b->updates;
+                    ++b->replays;
+                }
+                else
+                {
+                    cudaGetLastError(); /* topology changed: instantiate anew */
+                    cudaGraphExecDestroy(it->second);
+                    b->graphs.erase(it);
+                    it = b->graphs.end();
+                }
+            }
+            if (it == b->graphs.end())
+            {
+                if (b->graphs.size() >= 32)
+                {
+                    cudaGraphExecDestroy(b->graphs.begin()->second);
+                    b->graphs.erase(b->graphs.begin());
+                }
+                cudaGraphExec_t exec = nullptr;
+                const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+                if (ie != cudaSuccess)
+                {
+                    cudaGraphDestroy(g);
+                    LV_CUDA(ctx, ie);
+                }
+                it = b->graphs.emplace(key, exec).first;
+                ++b->captures;
+            }
             cudaGraphDestroy(g);
-            LV_CUDA(ctx, ie);
-            it = b->graphs.emplace(key, exec).first;
-            ++b->captures;
         }
         else
             ++b->replays;

@@ -48,6 +48,11 @@ def test_batch_equals_single_views(gpu_ctx):
             assert torch.equal(a, b) or float((a - b).abs().max()) <= 1e-6, (rep, i)
         assert all(s["n_not_available"] == 0 for s in stats)
         assert ray_ms > 0
+    # the default queue (per-view kernels) runs each batch as one graph
+    # launch: instantiated once, then the later captures update it
+    caps, reps, cached = batch.graph_stats()
+    assert batch.config()["queue"] == lv.QUEUE_VIEW_KERNELS
+    assert (caps, reps) == (1, 2), (caps, reps)
     batch.close()
     for v, _ in volumes:
         v.close()
