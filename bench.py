@@ -763,6 +763,13 @@ def parity_mode(ctx, vol, tf, cfg, args, dev):
              "max_err_255": float(np.abs(img[sl] - ref[sl]).max() * 255.0),
              "device_samples": int(st["n_samples"]) if rows is None else None,
              "oracle_samples": int(ns)}
+        # the same oracle with its trilinear weights rounded to 1/256, the
+        # fixed-point weights of a texture unit's linear filter: what bricks
+        # in 3D textures with hardware filtering would cost in parity
+        (q, _), _, _ = cpu.frame(k, rows=rows, mode=0x200)
+        dq = np.abs(q[sl] - ref[sl]).max(axis=2)
+        r["texture_filter_weights"] = {"max_err_255": float(dq.max() * 255.0),
+                                       "pixels_over_1_255": int((dq > 1.0 / 255.0).sum())}
         if shader:
             (shd, nss, c_shd, flags), _, _ = cpu.frame(k, rows=rows, mode=1, diagnostics=True)
             d = np.abs(img[sl] - shd[sl]).max(axis=2)
@@ -802,6 +809,9 @@ def parity_mode(ctx, vol, tf, cfg, args, dev):
             res[args.config].append(compare(cpu2, img, k, st, rows=(r0, r0 + 16)))
     res["max_err_255"] = max(r["max_err_255"] for key in ("plain256", args.config)
                              for r in res[key])
+    res["texture_filter_weights_max_err_255"] = max(
+        r["texture_filter_weights"]["max_err_255"] for key in ("plain256", args.config)
+        for r in res[key])
     return res
 
 

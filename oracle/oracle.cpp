@@ -339,6 +339,7 @@ struct RenderSet
     uint32_t Lf;       /* finest level */
     uint32_t dims[3];  /* leaf grid cells per axis */
     std::vector<int32_t> leaf; /* index into ids, -1 empty */
+    bool quant_weights = false; /* OR_QUANT_WEIGHTS */
 
     double voxel(uint32_t brick, int x, int y, int z) const
     {
@@ -377,6 +378,8 @@ struct RenderSet
             const float fl = std::floor(s[a]);
             i0[a] = int(fl);
             f[a] = double(s[a] - fl);
+            if (quant_weights) /* round to the nearest 1/256 */
+                f[a] = std::nearbyint(f[a] * 256.0) / 256.0;
         }
         double c[2][2][2];
         for (int dz = 0; dz < 2; ++dz)
@@ -978,8 +981,9 @@ int or_raycast_px(const or_volume* vol, uint32_t dtype, const uint64_t* node_ids
     /* OR_ACCUMULATE: rays start from the colour in `out` (a later pass of a
      * multi-pass frame, RenderPipeline.cpp:92-158) */
     const bool accumulate = (mode & OR_ACCUMULATE) != 0;
-    const int base_mode = mode & ~OR_ACCUMULATE;
+    const int base_mode = mode & ~(OR_ACCUMULATE | OR_QUANT_WEIGHTS);
     RenderSet rs;
+    rs.quant_weights = (mode & OR_QUANT_WEIGHTS) != 0;
     rs.vol = vol;
     rs.dtype = dtype;
     for (int a = 0; a < 3; ++a)

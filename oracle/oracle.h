@@ -127,7 +127,12 @@ enum
 {
     OR_MODE_PER_RAY = 0, /* samples on the global grid, per-ray brick order */
     OR_MODE_SHADER = 1,  /* per-brick shader loop, DistanceOperator order */
-    OR_ACCUMULATE = 0x100 /* flag: rays start from the colour in `out` */
+    OR_ACCUMULATE = 0x100, /* flag: rays start from the colour in `out` */
+    OR_QUANT_WEIGHTS = 0x200 /* flag (per-ray mode): trilinear weights rounded
+                                to 8 fractional bits, the fixed-point weights of
+                                a texture unit's linear filter; measures what
+                                hardware filtering would cost, nothing renders
+                                with it */
 };
 
 typedef struct

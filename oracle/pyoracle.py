@@ -48,6 +48,7 @@ class View(C.Structure):
 MODE_PER_RAY = 0
 MODE_SHADER = 1
 ACCUMULATE = 0x100  # flag: rays start from the colour already in `out`
+QUANT_WEIGHTS = 0x200  # flag: trilinear weights rounded to 1/256 (texture-unit filter)
 
 # per-pixel flags of raycast(..., diagnostics=True) in shader mode
 PX_DUPLICATE = 1  # a face grid point sampled by the bricks on both sides
