@@ -310,6 +310,34 @@ __device__ __forceinline__ float ldv(const uint8_t* p, uint32_t dt)
     }
 }
 
+/* One voxel as a float, read only when `on` (else 0). For uint8 and uint16
+ * the load itself is predicated (inline PTX), so a masked sample of the
+ * look-ahead march costs no branch and touches no memory; the other types
+ * branch. */
+template <int DT>
+__device__ __forceinline__ float ldv_masked(const uint8_t* p, uint32_t dt, bool on)
+{
+    if (DT == LV_DT_UINT8)
+    {
+        uint32_t v = 0;
+        asm("{\n\t.reg .pred q;\n\t.reg .u64 g;\n\tcvta.to.global.u64 g, %1;\n\t"
+            "setp.ne.b32 q, %2, 0;\n\t@q ld.global.nc.u8 %0, [g];\n\t}"
+            : "+r"(v)
+            : "l"(p), "r"(uint32_t(on)));
+        return float(v);
+    }
+    if (DT == LV_DT_UINT16)
+    {
+        uint32_t v = 0;
+        asm("{\n\t.reg .pred q;\n\t.reg .u64 g;\n\tcvta.to.global.u64 g, %1;\n\t"
+            "setp.ne.b32 q, %2, 0;\n\t@q ld.global.nc.u16 %0, [g];\n\t}"
+            : "+r"(v)
+            : "l"(p), "r"(uint32_t(on)));
+        return float(v);
+    }
+    return on ? ldv<DT>(p, dt) : 0.0f;
+}
+
 /* The voxels a sample reads and its interpolation weights; loaded one
  * sample ahead of the compositing (march) so that the loads of the next
  * sample are in flight while the current one is composited. */
@@ -352,12 +380,15 @@ __device__ __forceinline__ HotView hot_view(const RayView& V)
  * one base address and offsets to the other taps, valid when every overlap
  * >= 1; EDGE = n > 1 is EDGE = 0 for bricks of n x n voxels in x and y (the
  * row and slice pitches become immediate offsets of one pointer). */
-template <int DT, int FILTER, int EDGE, class HV>
+template <int DT, int FILTER, int EDGE, class HV, bool MASKED = false>
 __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const uint8_t* brick,
-                                          const float s[3], Taps<FILTER>& T)
+                                          const float s[3], Taps<FILTER>& T, bool on = true)
 {
+    /* MASKED: the voxels are read only when `on` (0 otherwise) */
+    auto ld = [&](const uint8_t* q) {
+        return MASKED ? ldv_masked<DT>(q, V.dtype, on) : ldv<DT>(q, V.dtype);
+    };
     const int bpv = DT == LV_DT_UINT16 ? 2 : DT == LV_DT_UINT8 ? 1 : int(V.bpv);
-    const uint32_t dt = V.dtype;
     constexpr int NX = EDGE > 1 ? EDGE : 0;
     const int n0 = NX ? NX : int(V.N[0]), n1 = NX ? NX : int(V.N[1]), n2 = int(V.N[2]);
     if (FILTER == LV_FILTER_NEAREST)
@@ -365,7 +396,7 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         const int x = min(max(int(floorf(s[0])), 0), n0 - 1);
         const int y = min(max(int(floorf(s[1])), 0), n1 - 1);
         const int z = min(max(int(floorf(s[2])), 0), n2 - 1);
-        T.c[0] = ldv<DT>(brick + ((z * n1 + y) * n0 + x) * bpv, dt);
+        T.c[0] = ld(brick + ((z * n1 + y) * n0 + x) * bpv);
         return;
     }
     const float fx0 = floorf(s[0]), fy0 = floorf(s[1]), fz0 = floorf(s[2]);
@@ -380,14 +411,14 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         const int z0 = min(max(iz, 0), n2 - 1), z1 = min(max(iz + 1, 0), n2 - 1);
         const int r00 = (z0 * n1 + y0) * n0, r01 = (z0 * n1 + y1) * n0;
         const int r10 = (z1 * n1 + y0) * n0, r11 = (z1 * n1 + y1) * n0;
-        T.c[0] = ldv<DT>(brick + (r00 + x0) * bpv, dt);
-        T.c[1] = ldv<DT>(brick + (r00 + x1) * bpv, dt);
-        T.c[2] = ldv<DT>(brick + (r01 + x0) * bpv, dt);
-        T.c[3] = ldv<DT>(brick + (r01 + x1) * bpv, dt);
-        T.c[4] = ldv<DT>(brick + (r10 + x0) * bpv, dt);
-        T.c[5] = ldv<DT>(brick + (r10 + x1) * bpv, dt);
-        T.c[6] = ldv<DT>(brick + (r11 + x0) * bpv, dt);
-        T.c[7] = ldv<DT>(brick + (r11 + x1) * bpv, dt);
+        T.c[0] = ld(brick + (r00 + x0) * bpv);
+        T.c[1] = ld(brick + (r00 + x1) * bpv);
+        T.c[2] = ld(brick + (r01 + x0) * bpv);
+        T.c[3] = ld(brick + (r01 + x1) * bpv);
+        T.c[4] = ld(brick + (r10 + x0) * bpv);
+        T.c[5] = ld(brick + (r10 + x1) * bpv);
+        T.c[6] = ld(brick + (r11 + x0) * bpv);
+        T.c[7] = ld(brick + (r11 + x1) * bpv);
     }
     else
     {
@@ -401,14 +432,14 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         const uint8_t* p01 = p00 + dy;
         const uint8_t* p10 = p00 + dz;
         const uint8_t* p11 = p10 + dy;
-        T.c[0] = ldv<DT>(p00, dt);
-        T.c[1] = ldv<DT>(p00 + bpv, dt);
-        T.c[2] = ldv<DT>(p01, dt);
-        T.c[3] = ldv<DT>(p01 + bpv, dt);
-        T.c[4] = ldv<DT>(p10, dt);
-        T.c[5] = ldv<DT>(p10 + bpv, dt);
-        T.c[6] = ldv<DT>(p11, dt);
-        T.c[7] = ldv<DT>(p11 + bpv, dt);
+        T.c[0] = ld(p00);
+        T.c[1] = ld(p00 + bpv);
+        T.c[2] = ld(p01);
+        T.c[3] = ld(p01 + bpv);
+        T.c[4] = ld(p10);
+        T.c[5] = ld(p10 + bpv);
+        T.c[6] = ld(p11);
+        T.c[7] = ld(p11 + bpv);
     }
 }
 
@@ -733,96 +764,68 @@ __device__ __forceinline__ bool locate(const RayView& V, RayState& r, float step
     return true;
 }
 
-/* Advances the ray to its next sample. Returns 0 once the ray has left its
- * segment, 1 for a sample without data (outside the octree or no brick
- * rendered there), 2 with the sample's voxels in T. */
+/* Advances the ray to its next sample (index r.kf) with one divergent
+ * region, the brick lookup where the ray leaves its safe range; false once
+ * the ray has left its segment. The sample's voxels are read into T only
+ * when it has data (`valid`: inside the segment and in a rendered brick, not
+ * outside the octree or in a cell no brick covers), by predicated loads, so
+ * a sample without data costs no branch. */
 template <int DT, int FILTER, int EDGE, class HV>
-__device__ __forceinline__ int fetch_sample(const RayView& V, const HV& H, RayState& r,
-                                            float step, Taps<FILTER>& T)
+__device__ __forceinline__ bool fetch_sample(const RayView& V, const HV& H, RayState& r, float step,
+                                         Taps<FILTER>& T, bool& valid)
 {
     const float t = fmaf(r.kf, step, r.tg);
-    if (!(t < r.thi))
-        return 0;
-    if (!(r.kf <= r.kf_safe))
+    const bool live = t < r.thi;
+    if (live && !(r.kf <= r.kf_safe))
     {
         float f[3];
         sample_cell_coord(V, r, t, f);
         if (!locate<FILTER>(V, r, step, f))
-        {
-            r.kf += 1.0f;
-            return 1;
-        }
+            r.entry = kLeafEmpty; /* outside the octree: this sample has no data */
     }
     r.kf += 1.0f;
-    if (r.entry == kLeafEmpty)
-        return 1;
+    valid = live && r.entry != kLeafEmpty;
     float sc[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         sc[a] = fmaf(t, r.sa[a], r.sb[a]);
-    load_taps<DT, FILTER, EDGE>(V, H, r.brick, sc, T);
-    return 2;
+    load_taps<DT, FILTER, EDGE, HV, true>(V, H, r.brick, sc, T, valid);
+    return live;
 }
 
 /* Transfer function, opacity correction and front-to-back blending of one
  * sample (fragRayCast.glsl:103-111); false once the early-termination
- * opacity is reached. */
+ * opacity is reached. A sample without data (!valid) is blended with opacity
+ * 0 (the colour and opacity stay bit for bit as they were) and not counted,
+ * so the march needs no branch around it. */
 template <int FILTER, int TFS, class HV>
 __device__ __forceinline__ bool composite_sample(const HV& H, RayState& r, float ac,
-                                                 const Taps<FILTER>& T, uint32_t& nsamp)
+                                                 const Taps<FILTER>& T, bool valid,
+                                                 uint32_t& nsamp)
 {
     const float4 src = tf_lookup<TFS>(H, interp<FILTER>(T));
     const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
-    const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
+    const float alpha = valid ? 1.0f - ex2_approx(ac * lg2_approx(1.0f - am)) : 0.0f;
     const float w = alpha * (1.0f - r.dst.w);
     r.dst.x = fmaf(src.x, w, r.dst.x);
     r.dst.y = fmaf(src.y, w, r.dst.y);
     r.dst.z = fmaf(src.z, w, r.dst.z);
     r.dst.w = fmaf(alpha, 1.0f - r.dst.w, r.dst.w);
-    ++nsamp;
+    nsamp += valid ? 1u : 0u;
     return !(r.dst.w > H.early);
 }
 
-/* One sample of the ray: false once the ray has ended or reached the
- * early-termination opacity. The steps of fetch_sample and composite_sample
- * in one straight body (fewer registers live across the loop than the two
- * calls). */
+/* One sample of the ray, fetched and composited with one tap set: false
+ * once the ray has ended or reached the early-termination opacity. */
 template <int DT, int FILTER, int TFS, int EDGE, class HV>
 __device__ __forceinline__ bool ray_step(const RayView& V, const HV& H, RayState& r, float step,
                                          float ac, uint32_t& nsamp)
 {
-    const float t = fmaf(r.kf, step, r.tg);
-    if (!(t < r.thi))
-        return false;
-    if (!(r.kf <= r.kf_safe))
-    {
-        float f[3];
-        sample_cell_coord(V, r, t, f);
-        if (!locate<FILTER>(V, r, step, f))
-        {
-            r.kf += 1.0f;
-            return true;
-        }
-    }
-    r.kf += 1.0f;
-    if (r.entry == kLeafEmpty)
-        return true;
-    float sc[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-        sc[a] = fmaf(t, r.sa[a], r.sb[a]);
     Taps<FILTER> T;
-    load_taps<DT, FILTER, EDGE>(V, H, r.brick, sc, T);
-    const float4 src = tf_lookup<TFS>(H, interp<FILTER>(T));
-    const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
-    const float alpha = 1.0f - ex2_approx(ac * lg2_approx(1.0f - am));
-    const float w = alpha * (1.0f - r.dst.w);
-    r.dst.x = fmaf(src.x, w, r.dst.x);
-    r.dst.y = fmaf(src.y, w, r.dst.y);
-    r.dst.z = fmaf(src.z, w, r.dst.z);
-    r.dst.w = fmaf(alpha, 1.0f - r.dst.w, r.dst.w);
-    ++nsamp;
-    return !(r.dst.w > H.early);
+    bool valid;
+    const bool live = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T, valid);
+    const bool cont = composite_sample<FILTER, TFS>(H, r, ac, T, valid, nsamp);
+    return live && cont;
 }
 
 /* A ray has ended: report an index check it failed. */
@@ -863,18 +866,19 @@ __device__ float4 march(const RayView& V, const HV& H, const RayGeom& g, float s
         return r.dst;
     }
     /* two tap sets in turn (no copy of the taps between samples): fetch the
-     * next sample into one while the other is composited */
+     * next sample into one while the other is composited. A sample without
+     * data is fetched and composited masked, so each sample has one
+     * divergent region (a brick lookup) and one loop exit. */
     Taps<FILTER> T0, T1;
-    int s0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0);
-    while (s0)
+    bool v0, v1;
+    bool live0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0, v0);
+    while (live0)
     {
-        const int s1 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T1);
-        if (s0 == 2 && !composite_sample<FILTER, TFS>(H, r, ac, T0, nsamp))
+        const bool live1 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T1, v1);
+        if (!(composite_sample<FILTER, TFS>(H, r, ac, T0, v0, nsamp) && live1))
             break;
-        if (!s1)
-            break;
-        s0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0);
-        if (s1 == 2 && !composite_sample<FILTER, TFS>(H, r, ac, T1, nsamp))
+        live0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0, v0);
+        if (!composite_sample<FILTER, TFS>(H, r, ac, T1, v1, nsamp))
             break;
     }
     flush_error(V, r);
