@@ -153,7 +153,7 @@ struct lv_ctx
     lv::Renderer* renderer = nullptr;
     size_t pool_bytes = size_t(3072) << 20;
     /* lv_render's ray cast */
-    lv_render_launch launch{LV_LAUNCH_TILE_GRID, 8, 16, 0, LV_ORDER_LONGEST_FIRST, 1};
+    lv_render_launch launch{LV_LAUNCH_TILE_GRID, 8, 8, 0, LV_ORDER_LONGEST_FIRST, 1};
     /* host fetchers of callback sources (created on first use) */
     lv::HostPool* host_pool = nullptr;
     lv_ctx_totals totals{}; /* since creation, host-side (lv_get_totals) */

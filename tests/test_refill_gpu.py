@@ -70,7 +70,7 @@ def test_render_launch_validation(gpu_ctx):
                 (1, 8, 16, 0, 2), (1, 8, 16, 0, 0, 2), (2, 8, 8, 8, 0, 1)]:
         with pytest.raises(lv.LivreError):
             gpu_ctx.set_render_launch(*bad)
-    assert gpu_ctx.render_launch() == {"kind": 3, "tile_w": 8, "tile_h": 16,
+    assert gpu_ctx.render_launch() == {"kind": 3, "tile_w": 8, "tile_h": 8,
                                        "samples_per_check": 0, "order": 1, "lookahead": 1}
 
 
