@@ -572,10 +572,9 @@ typedef struct lv_batch_config
     uint32_t lookahead;      /* view kernels: 1 = one-sample look-ahead (the
                                 voxels of the next sample load while the
                                 current one composites), as lv_render_launch.
-                                Default 0: on the mixed 64-view batch, 97 ms
-                                without against 108 ms with it (many view
-                                kernels share the SMs, and the look-ahead's
-                                registers cost resident warps) */
+                                The default configuration is lv_render's
+                                launch: view kernels, 8 x 8 tiles, longest
+                                first, look-ahead 1 */
 } lv_batch_config;
 
 /* A batch renderer on ctx (its own stream, graphs and per-view buffers).

@@ -62,7 +62,7 @@ struct lv_batch
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr, user_ready = nullptr;
     cudaEvent_t t_sel0 = nullptr, t_ray0 = nullptr, t_ray1 = nullptr;
-    lv_batch_config cfg{8, 16, 0, 0, 1, LV_QUEUE_VIEW_KERNELS, 8, LV_ORDER_LONGEST_FIRST, 0};
+    lv_batch_config cfg{8, 8, 0, 0, 1, LV_QUEUE_VIEW_KERNELS, 8, LV_ORDER_LONGEST_FIRST, 1};
     /* per-group longest-first order: hist (128 words) | keys | order, each
      * group at a fixed offset sized for order_cap items (grow-only) */
     lv::DeviceBuffer order_buf;

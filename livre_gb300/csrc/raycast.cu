@@ -478,10 +478,23 @@ __device__ __forceinline__ float4 tf_lookup(const HV& H, float v)
     const float s = fminf(fmaxf(fmaf(v, H.tf_mul, H.tf_add), 0.0f), H.tf_last);
     const int i0 = int(s);
     const float f = s - float(i0);
-    /* TFS: the table is in shared memory (generic loads), else read-only global */
+    /* TFS: the table is in shared memory (generic loads); else read-only
+     * global memory, the texel pair's 32 bytes (value, difference) in one
+     * 256-bit load: the table is a device allocation, so every pair is
+     * 32-byte aligned */
     const float4* e = H.tf + 2 * i0;
-    const float4 a = TFS ? e[0] : __ldg(e);
-    const float4 b = TFS ? e[1] : __ldg(e + 1);
+    float4 a, b;
+    if (TFS)
+    {
+        a = e[0];
+        b = e[1];
+    }
+    else
+        asm("{\n\t.reg .u64 g;\n\tcvta.to.global.u64 g, %8;\n\t"
+            "ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [g];\n\t}"
+            : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z),
+              "=f"(b.w)
+            : "l"(e));
     /* value + difference * f per channel, two channels per FFMA2 */
     const float2 f2 = make_float2(f, f);
     const float2 rg = __ffma2_rn(make_float2(b.x, b.y), f2, make_float2(a.x, a.y));
