@@ -38,6 +38,14 @@ import sys
 import threading
 import time
 
+# The serving mode keeps a few hundred CUDA streams busy (batches in flight,
+# each with its view streams at several priority levels). With CUDA's default
+# of 8 hardware work queues, an admission selection's first kernel can wait
+# behind a ray cast queued on another stream that shares its queue; 32 (the
+# maximum) spreads them out. Read when CUDA initialises, so set before any
+# CUDA call of this process.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 

@@ -689,6 +689,11 @@ typedef struct lv_server_profile
     double wait_ms;    /* blocked on in-flight batches */
     double device_ms;  /* device time of the batches (events around each) */
     double raycast_ms; /* of which the ray-cast launches */
+    double select_device_ms; /* admission selections: device time of their
+                                kernels (events around them) */
+    double select_ids_ms;    /* admission selections: host wall time from
+                                their kernels' end to the visible ids on the
+                                host */
 } lv_server_profile;
 lv_status lv_server_get_profile(lv_server* server, lv_server_profile* out);
 /* Finishes every queued request, then stops the server thread. */

@@ -122,7 +122,8 @@ class ServerProfile(C.Structure):
                 ("graph_captures", C.c_uint64), ("select_ms", C.c_double),
                 ("stream_ms", C.c_double), ("launch_ms", C.c_double),
                 ("wait_ms", C.c_double), ("device_ms", C.c_double),
-                ("raycast_ms", C.c_double)]
+                ("raycast_ms", C.c_double), ("select_device_ms", C.c_double),
+                ("select_ids_ms", C.c_double)]
 
 
 class ServerConfig(C.Structure):

@@ -69,9 +69,9 @@ struct lv_batch
     uint32_t order_cap = 0;
     /* one stream per non-first group: the groups' persistent launches run
      * side by side, so one group's last tiles overlap the next group */
-    cudaStream_t aux[kGroups] = {};
-    cudaStream_t aux_low[kGroups] = {}; /* lowest priority: a batch overlapping another */
-    bool low_priority = false;
+    /* at each priority level (batch_set_priority_level) */
+    cudaStream_t aux[lv::kBatchPriorityLevels][kGroups] = {};
+    int prio_level = 0;
     cudaEvent_t fork = nullptr, join[kGroups] = {};
     /* per-view kernels: tile-order scratch (offset of each view's region)
      * and ray-cast timing */
@@ -141,10 +141,9 @@ struct lv_batch
         {
             if (join[g])
                 cudaEventDestroy(join[g]);
-            if (aux[g])
-                cudaStreamDestroy(aux[g]);
-            if (aux_low[g])
-                cudaStreamDestroy(aux_low[g]);
+            for (int l = 0; l < lv::kBatchPriorityLevels; ++l)
+                if (aux[l][g])
+                    cudaStreamDestroy(aux[l][g]);
         }
         if (stream)
             cudaStreamDestroy(stream);
@@ -478,6 +477,49 @@ cudaError_t record_time(cudaEvent_t e, cudaStream_t s)
     return cudaEventRecord(e, s);
 }
 
+/* The batch's parameter block from mapped page-locked host memory, by a
+ * kernel rather than a copy (as the read-backs below): a copy waiting for
+ * its stream would hold up the copy engine's queue. Grid-stride over
+ * 16-byte words (the block is 256-byte aligned and sized). */
+__global__ void params_from_host_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst,
+                                        uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+/* One view's counter words to mapped page-locked host memory by a kernel
+ * rather than a copy: a copy waiting for its stream's ray cast holds up the
+ * copies queued behind it on the copy engine (other batches' read-backs, a
+ * server's admission read-back); a kernel holds up only its own stream. */
+__global__ void view_words_to_host_kernel(const uint32_t* __restrict__ src, uint32_t* dst,
+                                          uint32_t n)
+{
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        dst[i] = src[i];
+    __threadfence_system();
+}
+
+/* The batch's counter words and every view's missing list (its first
+ * FC_MISSING entries, at most `stride`) to mapped host memory, the same
+ * way: CTA v copies view v's list, CTA 0 also the words. */
+__global__ void batch_to_host_kernel(const uint32_t* __restrict__ words, uint32_t n_words,
+                                     const uint64_t* __restrict__ missing, uint32_t stride,
+                                     uint32_t n_views, uint32_t* h_words, uint64_t* h_missing)
+{
+    const uint32_t v = blockIdx.x;
+    if (v == 0)
+        for (uint32_t i = threadIdx.x; i < n_words; i += blockDim.x)
+            h_words[i] = words[i];
+    if (v < n_views)
+    {
+        const uint32_t k = min(words[kOutWords * v + FC_MISSING], stride);
+        for (uint32_t i = threadIdx.x; i < k; i += blockDim.x)
+            h_missing[uint64_t(stride) * v + i] = missing[uint64_t(stride) * v + i];
+    }
+    __threadfence_system();
+}
+
 void CUDART_CB view_done_trampoline(void* p)
 {
     const auto* a = static_cast<const lv_batch::HookArg*>(p);
@@ -493,7 +535,12 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     cudaStream_t s = b->stream;
     const ParamLayout PL = param_layout(b->views_cap);
     uint8_t* d = b->params.as<uint8_t>();
-    LV_CUDA(ctx, cudaMemcpyAsync(d, b->h_params.ptr, PL.bytes, cudaMemcpyHostToDevice, s));
+    {
+        const uint32_t n16 = uint32_t(PL.bytes / 16);
+        params_from_host_kernel<<<std::min<uint32_t>((n16 + 255) / 256, 64u), 256, 0, s>>>(
+            static_cast<const uint4*>(b->h_params.dev), reinterpret_cast<uint4*>(d), n16);
+        LV_CUDA(ctx, cudaGetLastError());
+    }
     LV_CUDA(ctx, cudaMemsetAsync(b->zeroed.ptr, 0, sizeof(uint32_t) * (kOutWords * n + 64), s));
     LV_CUDA(ctx, cudaMemsetAsync(b->leafs.ptr, 0xFF, sizeof(uint32_t) * b->cells_stride * n, s));
     const uint32_t* tables = reinterpret_cast<const uint32_t*>(d + PL.tables);
@@ -512,7 +559,7 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
     unsigned long long* clock = reinterpret_cast<unsigned long long*>(heads + kGroups);
     const RayView* d_rays = reinterpret_cast<RayView*>(d + PL.ray);
     b->vk_timed = false;
-    cudaStream_t* aux = b->low_priority ? b->aux_low : b->aux;
+    cudaStream_t* aux = b->aux[b->prio_level];
     if (b->cfg.queue == LV_QUEUE_VIEW_KERNELS)
     {
         /* lv_render's ray cast per view, views spread over the aux streams */
@@ -552,10 +599,10 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
             if (b->hook)
             {
                 /* this view is done: its counters to the host, then the hook */
-                LV_CUDA(ctx, cudaMemcpyAsync(b->h_view_words.as<uint32_t>() + kOutWords * i,
-                                             b->zeroed.as<uint32_t>() + kOutWords * i,
-                                             sizeof(uint32_t) * kOutWords,
-                                             cudaMemcpyDeviceToHost, vs));
+                view_words_to_host_kernel<<<1, 32, 0, vs>>>(
+                    b->zeroed.as<uint32_t>() + kOutWords * i,
+                    static_cast<uint32_t*>(b->h_view_words.dev) + kOutWords * i, kOutWords);
+                LV_CUDA(ctx, cudaGetLastError());
                 LV_CUDA(ctx, cudaLaunchHostFunc(vs, view_done_trampoline, &b->hook_args[i]));
             }
         }
@@ -610,13 +657,15 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
         }
         first = false;
     }
-    LV_CUDA(ctx, cudaMemcpyAsync(b->h_out.ptr, b->zeroed.ptr,
-                                 sizeof(uint32_t) * (kOutWords * n + kGroups + 4),
-                                 cudaMemcpyDeviceToHost, s));
-    /* missing lists, one copy */
-    uint8_t* hmiss = b->h_out.as<uint8_t>() + sizeof(uint32_t) * (kOutWords * b->views_cap + 64);
-    LV_CUDA(ctx, cudaMemcpyAsync(hmiss, b->lists.as<uint8_t>() + view_slots(b, 0).missing,
-                                 b->missing_stride * 8 * n, cudaMemcpyDeviceToHost, s));
+    /* counter words and missing lists to the host */
+    uint8_t* hmiss =
+        static_cast<uint8_t*>(b->h_out.dev) + sizeof(uint32_t) * (kOutWords * b->views_cap + 64);
+    batch_to_host_kernel<<<std::max(n, 1u), 128, 0, s>>>(
+        b->zeroed.as<uint32_t>(), kOutWords * n + kGroups + 4,
+        reinterpret_cast<const uint64_t*>(b->lists.as<uint8_t>() + view_slots(b, 0).missing),
+        uint32_t(b->missing_stride), n, static_cast<uint32_t*>(b->h_out.dev),
+        reinterpret_cast<uint64_t*>(hmiss));
+    LV_CUDA(ctx, cudaGetLastError());
     return LV_OK;
 }
 
@@ -624,10 +673,32 @@ lv_status enqueue_batch(lv_batch* b, uint32_t n, const std::vector<Group>& group
 
 namespace lv
 {
-void batch_set_low_priority(lv_batch* b, bool low)
+void batch_set_priority_level(lv_batch* b, int level)
 {
     std::lock_guard<std::mutex> lock(b->ctx->mutex);
-    b->low_priority = low;
+    level = std::min(std::max(level, 0), kBatchPriorityLevels - 1);
+    /* the streams of a level are created on its first use (only a server
+     * uses levels above 0) */
+    if (!b->aux[level][0])
+    {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        const int high = greatest < least ? greatest + 1 : greatest;
+        for (int g = 0; g < kGroups; ++g)
+            if (cudaStreamCreateWithPriority(&b->aux[level][g], cudaStreamNonBlocking,
+                                             std::min(high + level, least)) != cudaSuccess)
+            {
+                cudaGetLastError();
+                for (int k = 0; k <= g; ++k)
+                    if (b->aux[level][k])
+                    {
+                        cudaStreamDestroy(b->aux[level][k]);
+                        b->aux[level][k] = nullptr;
+                    }
+                return; /* stays at its current level */
+            }
+    }
+    b->prio_level = level;
 }
 
 void batch_set_view_hook(lv_batch* b, BatchViewDone fn, void* user)
@@ -677,20 +748,25 @@ extern "C" lv_status lv_batch_create(lv_ctx* ctx, lv_batch** out)
         delete b;
         return fail(ctx, LV_EDEVICE, "batch stream/events");
     }
-    /* ray-cast streams one step below the highest priority (kept for
-     * admission work); the low set at the lowest priority */
+    /* ray-cast streams from one step below the highest priority (kept for
+     * admission work) down, one step per level (a smaller number is a
+     * higher priority), clamped to the lowest */
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
     const int high = greatest < least ? greatest + 1 : greatest;
     for (int g = 0; g < kGroups; ++g)
-        if (cudaStreamCreateWithPriority(&b->aux[g], cudaStreamNonBlocking, high) != cudaSuccess ||
-            cudaStreamCreateWithPriority(&b->aux_low[g], cudaStreamNonBlocking, least) !=
-                cudaSuccess ||
-            cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming) != cudaSuccess)
+    {
+        /* level 0 now, the others on first use (batch_set_priority_level) */
+        const bool ok =
+            cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming) == cudaSuccess &&
+            cudaStreamCreateWithPriority(&b->aux[0][g], cudaStreamNonBlocking, high) ==
+                cudaSuccess;
+        if (!ok)
         {
             delete b;
             return fail(ctx, LV_EDEVICE, "batch stream/events");
         }
+    }
     *out = b;
     return LV_OK;
 }
@@ -830,7 +906,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
         const auto key = std::make_tuple(
             n_run, mask, b->cfg.tile_w, b->cfg.tile_h,
             b->cfg.ctas_per_sm | (b->cfg.queue << 8) | (b->cfg.samples_per_check << 16) |
-                (b->cfg.order << 24),
+                (b->cfg.order << 24) | (uint32_t(b->prio_level) << 28),
             b->cfg.tf_shared ? tfn_max : 0u, b->depth_max, b->generation,
             uintptr_t(b->sel.generation));
         auto it = b->graphs.find(key);
@@ -877,8 +953,12 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
                     cudaGraphExecDestroy(b->graphs.begin()->second);
                     b->graphs.erase(b->graphs.begin());
                 }
+                /* the kernels keep the priority of the streams they were
+                 * captured on (an update cannot change it: the priority
+                 * level is part of the cache key) */
                 cudaGraphExec_t exec = nullptr;
-                const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+                const cudaError_t ie =
+                    cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
                 if (ie != cudaSuccess)
                 {
                     cudaGraphDestroy(g);

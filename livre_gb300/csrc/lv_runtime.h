@@ -212,10 +212,14 @@ uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth,
                             bool allow_fused = true);
 
 /* Enqueues the selection kernels for n views whose constants are already
- * on the device (capturable: no host synchronisation). */
+ * on the device (capturable: no host synchronisation). level_ctas: CTAs of
+ * each per-level launch (grid-stride), 0 = two per SM. A selection that
+ * must start while other kernels fill the SMs (a server's admission) asks
+ * for few: each level launch waits until its CTAs find free slots. */
 lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* d_views,
                             uint32_t n_views, uint32_t total_roots, uint32_t max_depth,
-                            cudaStream_t stream, const uint32_t* d_total_roots = nullptr);
+                            cudaStream_t stream, const uint32_t* d_total_roots = nullptr,
+                            uint32_t level_ctas = 0);
 /* Grows the frontier queues of S to hold `nodes` per level (synchronises `s`
  * when it reallocates). */
 lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaStream_t s);
@@ -354,9 +358,15 @@ int batch_group(const RayView& V);
  * The callback must not call CUDA. */
 typedef void (*BatchViewDone)(void* user, uint32_t view, const uint32_t* words);
 void batch_set_view_hook(lv_batch* b, BatchViewDone fn, void* user);
-/* Ray casts of the next launches on the lowest-priority streams (a batch
- * that overlaps another takes only the SM slots the other leaves free). */
-void batch_set_low_priority(lv_batch* b, bool low);
+/* Stream priority levels of a batch's ray casts: level 0 is one step below
+ * the device's highest priority (kept for admission work), each further
+ * level one step lower (clamped to the lowest). */
+constexpr int kBatchPriorityLevels = 4;
+/* Ray casts of the next launches at priority `level` (0 .. levels - 1): a
+ * server launches each batch one level below the batches still rendering,
+ * so older requests keep the SM slots first and a younger batch takes the
+ * slots they leave free. */
+void batch_set_priority_level(lv_batch* b, int level);
 /* Frame statistics from a view's counter words. */
 void batch_decode_stats(const uint32_t* words, lv_frame_stats& s);
 

@@ -88,10 +88,14 @@ struct lv_server_hook
 } // namespace
 
 /* Batches in flight at once: a batch is admitted and launched while up to
- * kSlots - 1 earlier ones still render (each later one on lower-priority
- * streams), so a heavy batch does not hold back the requests queued behind
- * it. */
-constexpr int kSlots = 4;
+ * kSlots - 1 earlier ones still render (each later one a priority level
+ * below them), so a heavy batch does not hold back the requests queued
+ * behind it. */
+constexpr int kSlots = lv::kBatchPriorityLevels;
+
+/* CTAs of each level launch of the admission selection (grid-stride over
+ * the frontier) */
+constexpr uint32_t kAdmissionCtas = 16;
 
 struct lv_server
 {
@@ -114,6 +118,7 @@ struct lv_server
     lv_server_hook hooks[kSlots];
     std::vector<uint64_t> current[kSlots]; /* tickets of the views in flight per batch object */
     cudaEvent_t uploads_done = nullptr;
+    cudaEvent_t sel_t0 = nullptr, sel_t1 = nullptr; /* admission selection timing */
     /* dry-run selection buffers */
     SelectScratch sel;
     DeviceBuffer vis, res, views;
@@ -219,6 +224,36 @@ void fail_request(lv_server* S, Req* r, lv_status st)
     S->cv_done.notify_all();
 }
 
+/* The admission selection's per-view constants from mapped page-locked
+ * host memory, by a kernel rather than a copy: a copy would queue on the
+ * copy engine behind the batches' own parameter copies, each waiting for
+ * its stream. */
+__global__ void views_from_host_kernel(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                       uint32_t n)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+/* An admission selection's result words and visible ids (the first
+ * WRITTEN of each view's list) to mapped page-locked host memory, one CTA
+ * per view. A kernel rather than copies: under load the copy engine holds
+ * the batches' read-backs, each waiting for its ray cast, and a copy queued
+ * behind them waits as long. */
+__global__ void selection_to_host_kernel(const uint32_t* __restrict__ res,
+                                         const uint64_t* __restrict__ vis, uint32_t stride,
+                                         uint32_t* h_res, uint64_t* h_vis)
+{
+    const uint32_t v = blockIdx.x;
+    const uint32_t* r = res + LV_SELECT_RESULT_WORDS * v;
+    for (uint32_t i = threadIdx.x; i < LV_SELECT_RESULT_WORDS; i += blockDim.x)
+        h_res[LV_SELECT_RESULT_WORDS * v + i] = r[i];
+    const uint32_t k = min(r[LV_SEL_WRITTEN], stride);
+    for (uint32_t i = threadIdx.x; i < k; i += blockDim.x)
+        h_vis[uint64_t(stride) * v + i] = vis[uint64_t(stride) * v + i];
+    __threadfence_system();
+}
+
 /* Dry-run selection of the candidates; returns the visible ids per view. */
 lv_status dry_run(lv_server* S, const std::vector<Req*>& cand,
                   std::vector<std::vector<uint64_t>>& visible)
@@ -262,31 +297,41 @@ lv_status dry_run(lv_server* S, const std::vector<Req*>& cand,
                  q.volume->info.root_blocks[2];
         depth = std::max(depth, q.volume->info.depth);
     }
-    LV_CUDA(ctx, cudaMemcpyAsync(S->views.ptr, hv, sizeof(LodView) * n, cudaMemcpyHostToDevice, s));
-    st = enqueue_selection(ctx, S->sel, S->views.as<LodView>(), n, roots, depth, s);
+    LV_CUDA(ctx, cudaEventRecord(S->sel_t0, s));
+    {
+        const uint32_t words = uint32_t(sizeof(LodView) * n / 4);
+        views_from_host_kernel<<<(words + 255) / 256, 256, 0, s>>>(
+            static_cast<const uint32_t*>(S->h_views.dev), S->views.as<uint32_t>(), words);
+        LV_CUDA(ctx, cudaGetLastError());
+    }
+    /* a narrow grid: under load the SMs are full of ray-cast CTAs, and each
+     * level launch waits until its CTAs find free slots */
+    st = enqueue_selection(ctx, S->sel, S->views.as<LodView>(), n, roots, depth, s, nullptr,
+                           kAdmissionCtas);
     if (st != LV_OK)
         return st;
-    LV_CUDA(ctx, cudaMemcpyAsync(S->h_res.ptr, S->res.ptr,
-                                 sizeof(uint32_t) * LV_SELECT_RESULT_WORDS * n,
-                                 cudaMemcpyDeviceToHost, s));
+    LV_CUDA(ctx, cudaEventRecord(S->sel_t1, s));
+    selection_to_host_kernel<<<n, 256, 0, s>>>(S->res.as<uint32_t>(), S->vis.as<uint64_t>(),
+                                               uint32_t(stride),
+                                               static_cast<uint32_t*>(S->h_res.dev),
+                                               static_cast<uint64_t*>(S->h_vis.dev));
+    LV_CUDA(ctx, cudaGetLastError());
+    LV_CUDA(ctx, cudaEventSynchronize(S->sel_t1));
+    const double t_kernels = now_ms();
+    float dev_ms = 0.f;
+    if (cudaEventElapsedTime(&dev_ms, S->sel_t0, S->sel_t1) != cudaSuccess)
+        cudaGetLastError();
     LV_CUDA(ctx, cudaStreamSynchronize(s));
     visible.assign(n, {});
     const uint32_t* hr = S->h_res.as<uint32_t>();
     for (uint32_t i = 0; i < n; ++i)
     {
         const uint32_t k = hr[LV_SELECT_RESULT_WORDS * i + LV_SEL_WRITTEN];
-        if (k)
-            LV_CUDA(ctx, cudaMemcpyAsync(S->h_vis.as<uint64_t>() + stride * i,
-                                         S->vis.as<uint64_t>() + stride * i, k * 8,
-                                         cudaMemcpyDeviceToHost, s));
-    }
-    LV_CUDA(ctx, cudaStreamSynchronize(s));
-    for (uint32_t i = 0; i < n; ++i)
-    {
-        const uint32_t k = hr[LV_SELECT_RESULT_WORDS * i + LV_SEL_WRITTEN];
         const uint64_t* p = S->h_vis.as<uint64_t>() + stride * i;
         visible[i].assign(p, p + k);
     }
+    add_time(S, &lv_server_profile::select_device_ms, dev_ms);
+    add_time(S, &lv_server_profile::select_ids_ms, now_ms() - t_kernels);
     return LV_OK;
 }
 
@@ -501,12 +546,14 @@ void loop_batched(lv_server* S)
             std::lock_guard<std::mutex> lk(S->m);
             S->current[bi] = f.tickets;
         }
-        bool overlapping;
+        /* one priority level below each batch still rendering: the oldest
+         * requests keep the SM slots first */
+        int level;
         {
             std::lock_guard<std::mutex> lk(S->m);
-            overlapping = !S->inflight.empty();
+            level = int(S->inflight.size());
         }
-        batch_set_low_priority(b, overlapping);
+        batch_set_priority_level(b, level);
         cudaStreamWaitEvent(ls, S->uploads_done, 0);
         const double t_launch = now_ms();
         const lv_status st = lv_batch_render(b, bv.data(), uint32_t(bv.size()), ls);
@@ -594,7 +641,8 @@ extern "C" lv_status lv_server_create(lv_ctx* ctx, const lv_server_config* cfg, 
     cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     if (cudaStreamCreateWithPriority(&S->sel_stream, cudaStreamNonBlocking, hi_prio) !=
             cudaSuccess ||
-        cudaEventCreateWithFlags(&S->uploads_done, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&S->uploads_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&S->sel_t0) != cudaSuccess || cudaEventCreate(&S->sel_t1) != cudaSuccess)
     {
         delete S;
         return fail(ctx, LV_EDEVICE, "server streams");
@@ -746,5 +794,9 @@ extern "C" void lv_server_destroy(lv_server* S)
             cudaStreamDestroy(ls);
     if (S->uploads_done)
         cudaEventDestroy(S->uploads_done);
+    if (S->sel_t0)
+        cudaEventDestroy(S->sel_t0);
+    if (S->sel_t1)
+        cudaEventDestroy(S->sel_t1);
     delete S;
 }
