@@ -552,6 +552,23 @@ def served_mode(ctx, args, dev, seed=11):
         out["capacity_%s" % mode] = ({"rate_req_s": top["rate_req_s"],
                                       "frames_per_s": top["frames_per_s"],
                                       "p99_ms": top["p99_ms"]} if top else None)
+    # the same at several objectives, the rate interpolated linearly between
+    # the last offered rate within the objective and the first beyond it
+    def rate_at(mode, slo):
+        pts = sorted((r[mode]["rate_req_s"], r[mode]["p99_ms"]) for r in out["rates"])
+        prev = None
+        for rate, p99 in pts:
+            if p99 > slo:
+                if prev is None:
+                    return None
+                r0, p0 = prev
+                return round(r0 + (slo - p0) / (p99 - p0) * (rate - r0), 1)
+            prev = (rate, p99)
+        return prev[0] if prev else None
+
+    out["rate_at_p99_slo"] = [{"slo_ms": slo, "served_req_s": rate_at("served", slo),
+                               "plain_req_s": rate_at("plain", slo)}
+                              for slo in (75, 100, 125, 150, 200, 300)]
     for v, _ in vols:
         v.close()
     for t in tfs:

@@ -488,6 +488,31 @@ __global__ void params_from_host_kernel(const uint4* __restrict__ src, uint4* __
         dst[i] = src[i];
 }
 
+/* Every kernel of a captured batch at the stream priority of the batch's
+ * level (the graph is instantiated to run its kernels at their own
+ * priorities, not the launch stream's): a server's older batches keep the
+ * SM slots first, as without graphs. */
+lv_status set_node_priority(lv_batch* b, cudaGraph_t g)
+{
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    const int high = greatest < least ? greatest + 1 : greatest;
+    cudaLaunchAttributeValue v{};
+    v.priority = std::min(high + b->prio_level, least);
+    size_t n = 0;
+    LV_CUDA(b->ctx, cudaGraphGetNodes(g, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    LV_CUDA(b->ctx, cudaGraphGetNodes(g, nodes.data(), &n));
+    for (cudaGraphNode_t node : nodes)
+    {
+        cudaGraphNodeType t;
+        LV_CUDA(b->ctx, cudaGraphNodeGetType(node, &t));
+        if (t == cudaGraphNodeTypeKernel)
+            LV_CUDA(b->ctx, cudaGraphKernelNodeSetAttribute(node, cudaLaunchAttributePriority, &v));
+    }
+    return LV_OK;
+}
+
 /* One view's counter words to mapped page-locked host memory by a kernel
  * rather than a copy: a copy waiting for its stream's ray cast holds up the
  * copies queued behind it on the copy engine (other batches' read-backs, a
@@ -930,6 +955,11 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
                 return st;
             }
             LV_CUDA(ctx, ce);
+            if (const lv_status ps = set_node_priority(b, g); ps != LV_OK)
+            {
+                cudaGraphDestroy(g);
+                return ps;
+            }
             if (it != b->graphs.end())
             {
                 cudaGraphExecUpdateResultInfo info{};
@@ -953,9 +983,9 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
                     cudaGraphExecDestroy(b->graphs.begin()->second);
                     b->graphs.erase(b->graphs.begin());
                 }
-                /* the kernels keep the priority of the streams they were
-                 * captured on (an update cannot change it: the priority
-                 * level is part of the cache key) */
+                /* the kernels run at their node priority, the level's
+                 * (an update cannot change it: the level is part of the
+                 * cache key) */
                 cudaGraphExec_t exec = nullptr;
                 const cudaError_t ie =
                     cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
