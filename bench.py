@@ -533,7 +533,8 @@ def served_mode(ctx, args, dev, seed=11):
     ctx.last_stats()
     out = {"volumes": "8 volumes 256^3..4096^3 u8/u16, 64^3 bricks: 6 blob, 2 fBm "
                       "(512^3 u16, 2048^3 u8)",
-           "pool_gib": args.pool_gib or 96, "slo_p99_ms": args.slo_ms, "rates": []}
+           "pool_gib": args.pool_gib or 96, "brick_layout": "compact",
+           "slo_p99_ms": args.slo_ms, "rates": []}
     for rate in args.serve_rates:
         reqs = pool[:counts[rate]]
         # every brick the stream needs made resident first, so neither mode
@@ -1106,7 +1107,10 @@ def gb300_arm(args, cfg):
         line["batched"] = batched_mode(bctx, args, dev)
         bctx.close()
     if "served" in modes:
-        sctx = lv.Context(local, pool_bytes=96 << 30)
+        # the serving mix (8 volumes up to 4096^3 sharing 96 GiB) is sized for
+        # one voxel per byte: with voxel pairs its uint8 working sets outgrow
+        # the pool; served and plain requests share this context's layout
+        sctx = lv.Context(local, pool_bytes=96 << 30, brick_layout=lv.BRICKS_COMPACT)
         line["served"] = served_mode(sctx, args, dev)
         sctx.close()
     if "outofcore" in modes:

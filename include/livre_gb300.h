@@ -189,6 +189,29 @@ lv_status lv_select_visible_noalloc(const lv_volume_info* vol,
 lv_status lv_pool_configure(lv_ctx* ctx, size_t bytes);
 /* Drops every resident brick (Cache::purge, livre/core/cache/Cache.cpp:186-192). */
 lv_status lv_pool_purge(lv_ctx* ctx);
+/* Brick layouts in the pool (no reference counterpart: the reference keeps
+ * one texture per brick, TextureObject.cpp:76-120). */
+enum
+{
+    LV_BRICKS_PAIRS = 0,  /* default: uint8 bricks of 64 or more voxels per
+                             row stored as voxel pairs (each voxel with its
+                             +x neighbour), so a trilinear sample reads four
+                             16-bit words instead of eight bytes: twice the
+                             pool bytes, a ~10 % faster ray cast on a 2048^3
+                             volume of 64^3 bricks; other bricks compact */
+    LV_BRICKS_COMPACT = 1 /* one voxel per element for every brick: twice as
+                             many large uint8 bricks per pool byte (a server
+                             whose volumes' visible sets outgrow the pool
+                             with pairs) */
+};
+/* Brick layout of the pool; like lv_pool_configure, before the first volume
+ * is created. */
+lv_status lv_pool_set_brick_layout(lv_ctx* ctx, uint32_t layout);
+/* Pool bytes one brick of a volume with this description occupies on ctx
+ * (its brick layout; ctx NULL: the default layout), for sizing the pool
+ * (TextureObject's texture size, livre/core/render/TextureObject.cpp:76-120,
+ * in whole 1 KiB units). */
+lv_status lv_brick_slot_bytes(const lv_ctx* ctx, const lv_volume_info* info, uint64_t* bytes);
 
 /* livre::DataSourcePlugin::getData (livre/data/DataSourcePlugin.h:81) as a C
  * callback: fill `dst` (page-locked host memory, `bytes` long: the node's

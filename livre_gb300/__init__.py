@@ -24,7 +24,7 @@ import weakref
 import numpy as np
 
 from . import _abi
-from ._abi import (BLOB_DEVICE, BLOB_HOST, DT_UINT8, DT_UINT16, FBM_DEVICE, FBM_HOST,
+from ._abi import (BLOB_DEVICE, BLOB_HOST, BRICKS_COMPACT, BRICKS_PAIRS, DT_UINT8, DT_UINT16, FBM_DEVICE, FBM_HOST,
                    FILTER_NEAREST,
                    FILTER_TRILINEAR, LAUNCH_GRID, LAUNCH_TILE_GRID, LAUNCH_TILE_QUEUE,
                    LAUNCH_WARP_REFILL, LAUNCH_WARP_TILES,
@@ -150,6 +150,14 @@ class VolumeInformation:
     @property
     def brick_bytes(self):
         return int(np.prod(self.max_block)) * self.bytes_per_voxel
+
+    @property
+    def slot_bytes(self):
+        """Pool bytes one brick occupies in the default brick layout
+        (lv_brick_slot_bytes; Context.slot_bytes for a context's layout)."""
+        out = C.c_uint64()
+        check(lib().lv_brick_slot_bytes(None, C.byref(self.info), C.byref(out)))
+        return int(out.value)
 
     def node_count(self):
         r = self.root_blocks
@@ -542,7 +550,9 @@ def _close_live_contexts():
 class Context:
     """One CUDA device; owns the brick pool (lv_ctx)."""
 
-    def __init__(self, device=0, pool_bytes=None):
+    def __init__(self, device=0, pool_bytes=None, brick_layout=None):
+        """brick_layout: BRICKS_PAIRS (the default) or BRICKS_COMPACT
+        (lv_pool_set_brick_layout)."""
         self._children = weakref.WeakSet()
         _live_contexts.add(self)
         self.handle = None
@@ -552,6 +562,16 @@ class Context:
         self.device = device
         if pool_bytes is not None:
             check(lib().lv_pool_configure(h, int(pool_bytes)), h)
+        if brick_layout is not None:
+            check(lib().lv_pool_set_brick_layout(h, int(brick_layout)), h)
+
+    def slot_bytes(self, vi):
+        """Pool bytes one brick of volume description vi occupies on this
+        context (lv_brick_slot_bytes)."""
+        out = C.c_uint64()
+        check(lib().lv_brick_slot_bytes(self.handle, C.byref(vi.info), C.byref(out)),
+              self.handle)
+        return int(out.value)
 
     def close(self):
         """Destroys the volumes and transfer functions of this context, then it

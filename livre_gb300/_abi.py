@@ -87,6 +87,9 @@ class BatchView(C.Structure):
                 ("d_rgba", C.c_void_p)]
 
 
+BRICKS_PAIRS = 0
+BRICKS_COMPACT = 1
+
 QUEUE_CTA_TILES = 0
 QUEUE_WARP_REFILL = 1
 QUEUE_VIEW_KERNELS = 2
@@ -149,6 +152,8 @@ GET_DATA_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_uint64, C.c_void_p, C.c_size_
 P = C.POINTER
 _SIGNATURES = {
     "lv_fill_regular_volume_info": (C.c_int, [P(VolumeInfo)]),
+    "lv_brick_slot_bytes": (C.c_int, [C.c_void_p, P(VolumeInfo), P(C.c_uint64)]),
+    "lv_pool_set_brick_layout": (C.c_int, [C.c_void_p, C.c_uint32]),
     "lv_ctx_create": (C.c_int, [C.c_int, P(C.c_void_p)]),
     "lv_ctx_destroy": (None, [C.c_void_p]),
     "lv_last_error": (C.c_char_p, [C.c_void_p]),

@@ -36,7 +36,8 @@ template <int DT>
 __global__ void __launch_bounds__(256)
     histogram_kernel(const uint8_t* __restrict__ pool, const HistJob* __restrict__ jobs,
                      uint32_t N0, uint32_t N1, uint32_t N2, uint32_t O0, uint32_t O1,
-                     uint32_t O2, uint32_t dt, uint32_t n_bins, float lo, float scale_bins,
+                     uint32_t O2, uint32_t dt, uint32_t u8_stride, uint32_t n_bins, float lo,
+                     float scale_bins,
                      unsigned long long* __restrict__ per_brick,
                      unsigned long long* __restrict__ acc)
 {
@@ -56,7 +57,7 @@ __global__ void __launch_bounds__(256)
         if (DT == LV_DT_UINT16)
             v = float(reinterpret_cast<const uint16_t*>(brick)[idx]);
         else if (DT == LV_DT_UINT8)
-            v = float(brick[idx]);
+            v = float(brick[u8_stride * idx]); /* 2: voxel pairs, the element's low byte */
         else /* kDtAny: the voxel type `dt` */
             switch (dt)
             {
@@ -138,7 +139,8 @@ extern "C" lv_status lv_histogram(lv_volume* vol, const uint64_t* ids, uint32_t 
                                            : histogram_kernel<kDtAny>;
     kernel<<<n, 256, smem, s>>>(ctx->pool->arena.as<uint8_t>(), djobs.as<HistJob>(),
                                 I.max_block[0], I.max_block[1], I.max_block[2], I.overlap[0],
-                                I.overlap[1], I.overlap[2], I.dtype, n_bins, range_lo, scale_bins,
+                                I.overlap[1], I.overlap[2], I.dtype, vol->stage_off ? 2u : 1u,
+                                n_bins, range_lo, scale_bins,
                                 per_brick ? dout.as<unsigned long long>() : nullptr,
                                 dacc.as<unsigned long long>());
     LV_CUDA(ctx, cudaGetLastError());

@@ -338,6 +338,20 @@ __device__ __forceinline__ float ldv_masked(const uint8_t* p, uint32_t dt, bool 
     return on ? ldv<DT>(p, dt) : 0.0f;
 }
 
+/* A voxel pair of a uint8 brick (pair_layout: the voxel in the low byte,
+ * its +x neighbour in the high byte), read only when `on` by a predicated
+ * 16-bit load; when !on the register holds whatever it held (any value
+ * converts to a finite float, and the sample is masked). */
+__device__ __forceinline__ uint32_t ld_pair_u8(const uint8_t* p, bool on)
+{
+    uint32_t v;
+    asm("{\n\t.reg .pred q;\n\t.reg .u64 g;\n\tcvta.to.global.u64 g, %1;\n\t"
+        "setp.ne.b32 q, %2, 0;\n\t@q ld.global.nc.u16 %0, [g];\n\t}"
+        : "=r"(v)
+        : "l"(p), "r"(uint32_t(on)));
+    return v;
+}
+
 /* The voxels a sample reads and its interpolation weights; loaded one
  * sample ahead of the compositing (march) so that the loads of the next
  * sample are in flight while the current one is composited. */
@@ -388,8 +402,12 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
     auto ld = [&](const uint8_t* q) {
         return MASKED ? ldv_masked<DT>(q, V.dtype, on) : ldv<DT>(q, V.dtype);
     };
-    const int bpv = DT == LV_DT_UINT16 ? 2 : DT == LV_DT_UINT8 ? 1 : int(V.bpv);
     constexpr int NX = EDGE > 1 ? EDGE : 0;
+    /* voxel pairs (pair_layout): known from the pitch for fixed-pitch
+     * kernels, else the view's flag */
+    const bool pairs = DT == LV_DT_UINT8 && (NX ? NX >= int(kPairMinRow) : V.pairs != 0);
+    /* bytes per stored voxel element */
+    const int bpv = DT == LV_DT_UINT16 ? 2 : DT == LV_DT_UINT8 ? (pairs ? 2 : 1) : int(V.bpv);
     const int n0 = NX ? NX : int(V.N[0]), n1 = NX ? NX : int(V.N[1]), n2 = int(V.N[2]);
     if (FILTER == LV_FILTER_NEAREST)
     {
@@ -432,6 +450,23 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         const uint8_t* p01 = p00 + dy;
         const uint8_t* p10 = p00 + dz;
         const uint8_t* p11 = p10 + dy;
+        if (DT == LV_DT_UINT8 && pairs)
+        {
+            /* four voxel pairs: (x, x + 1) of rows y, y + 1 in slices z, z + 1 */
+            auto ld2 = [&](const uint8_t* q) -> uint32_t {
+                return MASKED ? ld_pair_u8(q, on) : __ldg(reinterpret_cast<const uint16_t*>(q));
+            };
+            const uint32_t q00 = ld2(p00), q01 = ld2(p01), q10 = ld2(p10), q11 = ld2(p11);
+            T.c[0] = float(q00 & 0xFFu);
+            T.c[1] = float(q00 >> 8);
+            T.c[2] = float(q01 & 0xFFu);
+            T.c[3] = float(q01 >> 8);
+            T.c[4] = float(q10 & 0xFFu);
+            T.c[5] = float(q10 >> 8);
+            T.c[6] = float(q11 & 0xFFu);
+            T.c[7] = float(q11 >> 8);
+            return;
+        }
         T.c[0] = ld(p00);
         T.c[1] = ld(p00 + bpv);
         T.c[2] = ld(p01);
@@ -1580,6 +1615,15 @@ lv_status refill_views_dispatch(lv_ctx* ctx, const RayView* d_rays, const TileQu
     return LV_OK;
 }
 
+/* A fixed-pitch kernel decides the brick layout from its pitch at compile
+ * time (voxel pairs for uint8 rows of kPairMinRow or more); a view whose
+ * pool keeps such bricks compact (LV_BRICKS_COMPACT) takes the generic-pitch
+ * kernels, which read the layout from the view. */
+bool fixed_pitch_layout(const RayView& V)
+{
+    return V.dtype != LV_DT_UINT8 || (V.pairs != 0) == (V.N[0] >= kPairMinRow);
+}
+
 /* Scratch bytes of the longest-first order of V's tiles. */
 size_t order_bytes_of(const RayView& V, const lv_render_launch& L)
 {
@@ -1804,7 +1848,8 @@ lv_status plain_dispatch(lv_ctx* ctx, const RayView& V, const lv_render_launch& 
                          cudaStream_t s, uint8_t* scratch)
 {
     if (EDGE == 0 && F == LV_FILTER_TRILINEAR && L.kind == LV_LAUNCH_TILE_GRID &&
-        V.N[0] == V.N[1] && (V.N[0] == 66 || V.N[0] == 34 || V.N[0] == 130))
+        V.N[0] == V.N[1] && (V.N[0] == 66 || V.N[0] == 34 || V.N[0] == 130) &&
+        fixed_pitch_layout(V))
     {
         if (L.lookahead)
             return V.N[0] == 66   ? tiles_nx_dispatch<DT, F, 66, 1>(ctx, V, L, s, scratch)
@@ -1876,7 +1921,8 @@ size_t tile_order_bytes(const RayView& V, const lv_render_launch& L)
 int batch_group(const RayView& V)
 {
     const int v = kernel_variant(V.dtype, V.filter, V.edge);
-    if (v >= 8 || V.filter != LV_FILTER_TRILINEAR || V.edge != 0 || V.N[0] != V.N[1])
+    if (v >= 8 || V.filter != LV_FILTER_TRILINEAR || V.edge != 0 || V.N[0] != V.N[1] ||
+        !fixed_pitch_layout(V))
         return v < 8 ? v : kBatchGroups + v;
     const int pitch = V.N[0] == 34 ? 0 : V.N[0] == 66 ? 1 : V.N[0] == 130 ? 2 : -1;
     if (pitch < 0)

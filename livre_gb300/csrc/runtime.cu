@@ -69,6 +69,67 @@ __global__ void words_to_host_kernel(const uint32_t* __restrict__ src, uint32_t*
     __threadfence_system();
 }
 
+/* Expands uint8 bricks into voxel pairs in place (pair_layout). Block b
+ * takes the slot at arena + offsets[b], whose canonical bytes (`voxels` of
+ * them, x fastest, rows of n0) are at slot + stage_off, stage_off >= voxels
+ * and 256-byte aligned. Element j is written at slot + 2j and overwrites
+ * canonical bytes of index 2j - stage_off and 2j + 1 - stage_off, both
+ * below j: the block takes chunks of elements in increasing order, reading
+ * a chunk's canonical bytes (and the next one) before any of its writes, so
+ * no element reads a byte an earlier write has replaced. */
+constexpr uint32_t kExpandThreads = 512;
+constexpr uint32_t kExpandPer = 16; /* elements per thread and chunk */
+
+__global__ void __launch_bounds__(kExpandThreads)
+    expand_pairs_kernel(uint8_t* __restrict__ arena, const uint64_t* __restrict__ offsets,
+                        uint32_t n0, uint32_t voxels, uint32_t stage_off)
+{
+    uint8_t* slot = arena + offsets[blockIdx.x];
+    const uint8_t* canon = slot + stage_off;
+    constexpr uint32_t chunk = kExpandThreads * kExpandPer;
+    for (uint32_t j0 = 0; j0 < voxels; j0 += chunk)
+    {
+        const uint32_t j = j0 + threadIdx.x * kExpandPer;
+        uint32_t v[kExpandPer + 1];
+        if (j + kExpandPer <= voxels)
+        {
+            const uint4 w = *reinterpret_cast<const uint4*>(canon + j); /* 16-byte aligned */
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (uint32_t k = 0; k < kExpandPer; ++k)
+                v[k] = (ws[k / 4] >> (8 * (k % 4))) & 0xFFu;
+            v[kExpandPer] = j + kExpandPer < voxels ? canon[j + kExpandPer] : 0u;
+        }
+        else
+#pragma unroll
+            for (uint32_t k = 0; k <= kExpandPer; ++k)
+                v[k] = j + k < voxels ? canon[j + k] : 0u;
+        __syncthreads(); /* the chunk read before any of its writes */
+        if (j + kExpandPer <= voxels)
+        {
+            uint32_t out[kExpandPer / 2];
+#pragma unroll
+            for (uint32_t k = 0; k < kExpandPer; k += 2)
+            {
+                const uint32_t e0 = v[k] | ((((j + k) % n0) == n0 - 1 ? v[k] : v[k + 1]) << 8);
+                const uint32_t e1 =
+                    v[k + 1] | ((((j + k + 1) % n0) == n0 - 1 ? v[k + 1] : v[k + 2]) << 8);
+                out[k / 2] = e0 | (e1 << 16);
+            }
+            uint4* dst = reinterpret_cast<uint4*>(slot + 2ull * j); /* 32-byte aligned */
+            dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
+            dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
+        }
+        else
+            for (uint32_t k = 0; k < kExpandPer && j + k < voxels; ++k)
+            {
+                const uint32_t hi = ((j + k) % n0) == n0 - 1 ? v[k] : v[k + 1];
+                reinterpret_cast<uint16_t*>(slot)[j + k] = uint16_t(v[k] | (hi << 8));
+            }
+        __syncthreads(); /* the chunk written before the next one reads */
+    }
+}
+
 lv_status words_to_host(lv_ctx* ctx, const void* d_src, const PinnedBuffer& host,
                         size_t word_offset, uint32_t n, cudaStream_t s)
 {
@@ -188,6 +249,7 @@ lv_status ensure_renderer(lv_ctx* ctx)
     cudaEventCreateWithFlags(&r->pending_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->render_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->upload_event, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->expand_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->frame_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->resolve_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->fork, cudaEventDisableTiming);
@@ -382,6 +444,7 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     std::unordered_map<lv_volume*, std::vector<uint32_t>> stamps;
     std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>> updates;
     std::vector<uint64_t> gen_ids, gen_offsets;
+    std::vector<uint64_t> expand; /* slots to expand into voxel pairs */
     uint8_t* arena = P.arena.as<uint8_t>();
     lv_status st = LV_OK;
     /* the bookkeeping of a brick placed in `unit` */
@@ -441,9 +504,11 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                     break;
                 }
                 const size_t slot = (ring + j) % ring_n;
-                LV_CUDA(ctx, cudaMemcpyAsync(arena + uint64_t(unit) * kSlotUnit,
+                LV_CUDA(ctx, cudaMemcpyAsync(arena + uint64_t(unit) * kSlotUnit + vol->stage_off,
                                              vol->staging[slot]->ptr, vol->brick_bytes,
                                              cudaMemcpyHostToDevice, up));
+                if (vol->stage_off)
+                    expand.push_back(uint64_t(unit) * kSlotUnit);
                 LV_CUDA(ctx, cudaEventRecord(vol->staging_ev[slot], up));
                 bytes_loaded += vol->brick_bytes;
                 place(todo[g0 + j].second, unit);
@@ -470,15 +535,17 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
             if (vol->kind == SRC_BLOB_HOST)
             {
                 const uint8_t* src = vol->host_store.as<uint8_t>() + idx * vol->brick_bytes;
-                LV_CUDA(ctx, cudaMemcpyAsync(arena + uint64_t(unit) * kSlotUnit, src,
-                                             vol->brick_bytes, cudaMemcpyHostToDevice, up));
+                LV_CUDA(ctx, cudaMemcpyAsync(arena + uint64_t(unit) * kSlotUnit + vol->stage_off,
+                                             src, vol->brick_bytes, cudaMemcpyHostToDevice, up));
                 bytes_loaded += vol->brick_bytes;
             }
             else /* generated on the device below */
             {
                 gen_ids.push_back(id);
-                gen_offsets.push_back(uint64_t(unit) * kSlotUnit);
+                gen_offsets.push_back(uint64_t(unit) * kSlotUnit + vol->stage_off);
             }
+            if (vol->stage_off)
+                expand.push_back(uint64_t(unit) * kSlotUnit);
             place(idx, unit);
         }
     if (!gen_ids.empty())
@@ -506,6 +573,21 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
         if (g != LV_OK)
             return g;
     }
+    if (!expand.empty())
+    {
+        /* the offsets' buffer is read by the previous expansion until it ends */
+        if (R.expand_recorded)
+            LV_CUDA(ctx, cudaEventSynchronize(R.expand_done));
+        LV_CUDA(ctx, R.h_expand.reserve(sizeof(uint64_t) * expand.size()));
+        std::memcpy(R.h_expand.ptr, expand.data(), sizeof(uint64_t) * expand.size());
+        const uint32_t voxels = uint32_t(vol->brick_bytes); /* uint8: one byte per voxel */
+        expand_pairs_kernel<<<uint32_t(expand.size()), kExpandThreads, 0, up>>>(
+            arena, static_cast<const uint64_t*>(R.h_expand.dev), vol->info.max_block[0], voxels,
+            uint32_t(vol->stage_off));
+        LV_CUDA(ctx, cudaGetLastError());
+        LV_CUDA(ctx, cudaEventRecord(R.expand_done, up));
+        R.expand_recorded = true;
+    }
     lv_status u = apply_updates(ctx, updates, up);
     if (u != LV_OK)
         return u;
@@ -514,7 +596,7 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     return st;
 }
 
-void volume_layout(lv_volume* v)
+void volume_layout(lv_volume* v, uint32_t brick_layout)
 {
     uint64_t off = 0;
     for (uint32_t L = 0; L <= kMaxLevels; ++L)
@@ -529,7 +611,15 @@ void volume_layout(lv_volume* v)
     v->brick_bytes = uint64_t(v->info.max_block[0]) * v->info.max_block[1] *
                      v->info.max_block[2] * bytes_per_voxel(v->info.dtype) *
                      v->info.comp_count;
-    v->slot_units = uint32_t(round_units(v->brick_bytes));
+    /* voxel pairs: 2 bytes per voxel, the canonical bytes staged in the
+     * slot's upper part (256-byte aligned, at or past the brick's voxel
+     * count so that the in-place expansion never overwrites bytes it has
+     * still to read) */
+    v->stage_off = brick_layout == LV_BRICKS_PAIRS &&
+                           pair_layout(v->info.dtype, v->info.max_block[0])
+                       ? (v->brick_bytes + 255) & ~uint64_t(255)
+                       : 0;
+    v->slot_units = uint32_t(round_units(v->stage_off + v->brick_bytes));
 }
 
 lv_status volume_init(lv_ctx* ctx, lv_volume* v)
@@ -538,7 +628,7 @@ lv_status volume_init(lv_ctx* ctx, lv_volume* v)
         return fail(ctx, LV_EINVAL, "volume depth must be 1..15 (fill the info first)");
     if (bytes_per_voxel(v->info.dtype) == 0 || v->info.comp_count != 1)
         return fail(ctx, LV_EINVAL, "unsupported voxel type or component count");
-    volume_layout(v);
+    volume_layout(v, ctx->brick_layout);
     if (v->n_nodes > (uint64_t(1) << 28))
         return fail(ctx, LV_EINVAL, "octree too large for a dense page table");
     lv_status st = ensure_pool(ctx);
@@ -669,6 +759,7 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     V.Lf = Lf;
     V.dtype = info.dtype;
     V.bpv = bytes_per_voxel(info.dtype);
+    V.pairs = vol->stage_off != 0;
     V.filter = desc.filter == LV_FILTER_TRILINEAR ? LV_FILTER_TRILINEAR : LV_FILTER_NEAREST;
     /* the transfer function's range when valid, else the type's
      * (RayCastRenderer.cpp:279-284) */
@@ -723,6 +814,19 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
 using namespace lv;
 
 extern "C" uint32_t lv_abi_version(void) { return LV_ABI_VERSION; }
+
+extern "C" lv_status lv_brick_slot_bytes(const lv_ctx* ctx, const lv_volume_info* info,
+                                        uint64_t* bytes)
+{
+    if (!info || !bytes || bytes_per_voxel(info->dtype) == 0 || info->comp_count != 1)
+        return LV_EINVAL;
+    lv_volume v;
+    v.info = *info;
+    v.info.depth = 0; /* the layout of a brick only */
+    volume_layout(&v, ctx ? ctx->brick_layout : uint32_t(LV_BRICKS_PAIRS));
+    *bytes = uint64_t(v.slot_units) * kSlotUnit;
+    return LV_OK;
+}
 
 extern "C" lv_status lv_fill_regular_volume_info(lv_volume_info* info)
 {
@@ -787,6 +891,7 @@ extern "C" void lv_ctx_destroy(lv_ctx* ctx)
         cudaEventDestroy(ctx->renderer->pending_event);
         cudaEventDestroy(ctx->renderer->render_event);
         cudaEventDestroy(ctx->renderer->upload_event);
+        cudaEventDestroy(ctx->renderer->expand_done);
         cudaEventDestroy(ctx->renderer->frame_done);
         cudaEventDestroy(ctx->renderer->resolve_done);
         cudaEventDestroy(ctx->renderer->fork);
@@ -822,6 +927,18 @@ extern "C" lv_status lv_pool_configure(lv_ctx* ctx, size_t bytes)
     if (bytes < kSlotUnit || bytes / kSlotUnit > (uint64_t(1) << kLeafSlotBits))
         return fail(ctx, LV_EINVAL, "pool size must be in [1 KiB, 128 GiB]");
     ctx->pool_bytes = bytes;
+    return LV_OK;
+}
+
+extern "C" lv_status lv_pool_set_brick_layout(lv_ctx* ctx, uint32_t layout)
+{
+    if (!ctx)
+        return LV_EINVAL;
+    if (layout != LV_BRICKS_PAIRS && layout != LV_BRICKS_COMPACT)
+        return fail(ctx, LV_EINVAL, "unknown brick layout");
+    if (ctx->pool)
+        return fail(ctx, LV_EINVAL, "pool already allocated");
+    ctx->brick_layout = layout;
     return LV_OK;
 }
 

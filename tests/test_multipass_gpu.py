@@ -10,7 +10,6 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 TOL = 1.0 / 255.0
-SLOT = 6 * 1024   # an (16 + 2)^3 uint8 brick takes 6 KiB slot units
 PER_PASS = 64
 
 
@@ -59,7 +58,7 @@ def test_multipass_matches_oracle(oracle, early, k):
     import livre_gb300 as lv
     vi = lv.VolumeInformation(128, 16, 1)
     ovol = oracle.volume(128, 16, 1)
-    ctx = lv.Context(0, pool_bytes=PER_PASS * SLOT)
+    ctx = lv.Context(0, pool_bytes=PER_PASS * vi.slot_bytes)
     try:
         vol = ctx.blob_volume(vi, 12, 7)
         tf_rgba = lv.gaussian_peaks_tf(256, seed=5)
@@ -90,7 +89,7 @@ def test_multipass_matches_oracle(oracle, early, k):
 def test_one_pass_when_the_set_fits(oracle):
     import livre_gb300 as lv
     vi = lv.VolumeInformation(128, 16, 1)
-    ctx = lv.Context(0, pool_bytes=PER_PASS * SLOT)
+    ctx = lv.Context(0, pool_bytes=PER_PASS * vi.slot_bytes)
     try:
         vol = ctx.blob_volume(vi, 12, 7)
         tf = ctx.transfer_function(lv.linear_ramp_tf())

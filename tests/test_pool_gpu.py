@@ -10,10 +10,10 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def small_ctx(n_slots, brick_bytes):
+def small_ctx(n_slots, vi):
+    """A context whose pool holds n_slots bricks of volume vi."""
     import livre_gb300 as lv
-    slot = ((brick_bytes + 1023) // 1024) * 1024
-    return lv.Context(0, pool_bytes=n_slots * slot)
+    return lv.Context(0, pool_bytes=n_slots * vi.slot_bytes)
 
 
 def test_cache_known_answer():
@@ -21,7 +21,7 @@ def test_cache_known_answer():
     refresh), 3 -> 1 is evicted; purge empties the cache."""
     import livre_gb300 as lv
     vol = lv.VolumeInformation(64, 16, 1)
-    ctx = small_ctx(2, vol.brick_bytes)
+    ctx = small_ctx(2, vol)
     v = ctx.blob_volume(vol, 4, 1)
     a, b, c = (lv.NodeId(1, p).id for p in [(0, 0, 0), (0, 0, 1), (0, 1, 0)])
     assert v.load([a]) == 1
@@ -45,7 +45,7 @@ def test_eviction_skips_bricks_in_use(oracle):
     mv, proj = lv.orbit_camera(0, 8, vol.world_size, 64, 64, radius_scale=1.0)
     vis, _ = oracle.select_visible(ovol, mv, proj, 64, 1.0)
     vis = [int(i) for i in vis]
-    ctx = small_ctx(len(vis) + 3, vol.brick_bytes)
+    ctx = small_ctx(len(vis) + 3, vol)
     v = ctx.blob_volume(vol, 6, 2)
     others = [n.id for n in vol.all_nodes() if n.id not in set(vis)][:5]
     assert v.load(others) == 5

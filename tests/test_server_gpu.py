@@ -66,7 +66,7 @@ def test_server_admission_by_pool_memory(oracle):
     ovol = oracle.volume(128, 32, 1)
     cams = [lv.orbit_camera(k, 4, vi.world_size, 48, 48, radius_scale=1.0) for k in range(4)]
     sizes = [len(oracle.select_visible(ovol, mv, pr, 48, 0.7)[0]) for mv, pr in cams]
-    slot = ((vi.brick_bytes + 1023) // 1024) * 1024
+    slot = vi.slot_bytes
     ctx = lv.Context(0, pool_bytes=max(sizes) * slot + slot)
     v = ctx.blob_volume(vi, 9, 4)
     tf = ctx.transfer_function(lv.linear_ramp_tf())

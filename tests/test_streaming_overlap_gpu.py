@@ -56,7 +56,7 @@ def test_back_to_back_frames_equal_waited_frames(native, placement, pool):
         assert st["error_flags"] == 0 and st["n_passes"] == 1
         most = max(most, st["n_visible"])
     union = ctx.totals()["bricks_uploaded"]
-    slot = -(-vi.brick_bytes // 1024) * 1024
+    slot = vi.slot_bytes
     vol.close()
     tf.close()
     ctx.close()
