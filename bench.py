@@ -100,9 +100,10 @@ def parse():
 
 
 # DRAM bytes (read + write) of one ray-cast launch of the 2048^3 / 1080p
-# orbit, measured by ncu on a GB300 (18.64 MB read, 0.08 MB written: the
-# visible bricks once; the 8-byte-per-sample gather is served by L1/L2).
-RAYCAST_DRAM_BYTES_PER_LAUNCH = 18.72e6
+# orbit, measured by ncu on a GB300 (37.11 MB read, 2.29 MB written: the
+# visible bricks once, stored as voxel pairs; the 8-byte-per-sample gather is
+# served by L1/L2).
+RAYCAST_DRAM_BYTES_PER_LAUNCH = 39.40e6
 
 
 def transfer_function(cfg):
