@@ -417,7 +417,11 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         T.c[0] = ld(brick + ((z * n1 + y) * n0 + x) * bpv);
         return;
     }
-    const float fx0 = floorf(s[0]), fy0 = floorf(s[1]), fz0 = floorf(s[2]);
+    /* floor by adding 2^23 rounding down (exact for |s| < 2^22), no
+     * conversion instruction */
+    const float fx0 = __fadd_rd(s[0], 8388608.0f) - 8388608.0f;
+    const float fy0 = __fadd_rd(s[1], 8388608.0f) - 8388608.0f;
+    const float fz0 = __fadd_rd(s[2], 8388608.0f) - 8388608.0f;
     T.fx = s[0] - fx0;
     T.fy = s[1] - fy0;
     T.fz = s[2] - fz0;
@@ -444,7 +448,8 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
          * [O - 1/2, O + B - 1/2], so the base voxel is in [0, N - 2] on each
          * axis and all eight taps are in the slot. One unsigned clamp of the
          * linear base keeps any tap inside the slot whatever the inputs. */
-        const uint32_t base = min(uint32_t((iz * n1 + iy) * n0 + ix), H.max_base);
+        const uint32_t base =
+            min(__float2uint_rz(fmaf(fmaf(fz0, float(n1), fy0), float(n0), fx0)), H.max_base);
         const int dy = n0 * bpv, dz = n0 * n1 * bpv;
         const uint8_t* p00 = brick + base * bpv;
         const uint8_t* p01 = p00 + dy;
@@ -511,8 +516,11 @@ template <int TFS, class HV>
 __device__ __forceinline__ float4 tf_lookup(const HV& H, float v)
 {
     const float s = fminf(fmaxf(fmaf(v, H.tf_mul, H.tf_add), 0.0f), H.tf_last);
-    const int i0 = int(s);
-    const float f = s - float(i0);
+    /* floor(s) (s in [0, tf_last]) by adding 2^23 rounding down: its bits
+     * carry the integer, no conversion instruction */
+    const float y = __fadd_rd(s, 8388608.0f);
+    const int i0 = int(__float_as_uint(y) - 0x4B000000u);
+    const float f = s - (y - 8388608.0f);
     /* TFS: the table is in shared memory (generic loads); else read-only
      * global memory, the texel pair's 32 bytes (value, difference) in one
      * 256-bit load: the table is a device allocation, so every pair is

@@ -14,8 +14,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def make(ctx, lv, source):
-    vi = lv.VolumeInformation(256, 64, 1)  # 66^3 slots: pairs in the default layout
+def make(ctx, lv, source, block=64):
+    vi = lv.VolumeInformation(256, block, 1)  # (block + 2)^3 slots: pairs by default
     if source == "device":
         return vi, ctx.blob_volume(vi, 24, 11, 4)
     if source == "host":
@@ -28,16 +28,17 @@ def make(ctx, lv, source):
     return vi, ctx.callback_volume(vi, get_data)
 
 
-@pytest.mark.parametrize("source", ["device", "host", "callback"])
-def test_pairs_equal_compact(source):
+@pytest.mark.parametrize("source,block", [("device", 64), ("host", 64), ("callback", 64),
+                                          ("device", 128)])
+def test_pairs_equal_compact(source, block):
     import livre_gb300 as lv
     frames = {}
+    n = (block + 2) ** 3
     for layout in (lv.BRICKS_PAIRS, lv.BRICKS_COMPACT):
-        ctx = lv.Context(0, pool_bytes=256 << 20, brick_layout=layout)
-        vi, vol = make(ctx, lv, source)
-        assert ctx.slot_bytes(vi) == (((66 ** 3 + 255) // 256 * 256 + 66 ** 3 + 1023) // 1024
-                                      * 1024 if layout == lv.BRICKS_PAIRS
-                                      else (66 ** 3 + 1023) // 1024 * 1024)
+        ctx = lv.Context(0, pool_bytes=512 << 20, brick_layout=layout)
+        vi, vol = make(ctx, lv, source, block)
+        assert ctx.slot_bytes(vi) == (((n + 255) // 256 * 256 + n + 1023) // 1024 * 1024
+                                      if layout == lv.BRICKS_PAIRS else (n + 1023) // 1024 * 1024)
         tf = ctx.transfer_function(lv.gaussian_peaks_tf(256, seed=9))
         out = []
         for k, (kind, filt, lookahead) in enumerate([
