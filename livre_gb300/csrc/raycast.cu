@@ -394,14 +394,12 @@ __device__ __forceinline__ HotView hot_view(const RayView& V)
  * one base address and offsets to the other taps, valid when every overlap
  * >= 1; EDGE = n > 1 is EDGE = 0 for bricks of n x n voxels in x and y (the
  * row and slice pitches become immediate offsets of one pointer). */
-template <int DT, int FILTER, int EDGE, class HV, bool MASKED = false>
+template <int DT, int FILTER, int EDGE, class HV>
 __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const uint8_t* brick,
-                                          const float s[3], Taps<FILTER>& T, bool on = true)
+                                          const float s[3], Taps<FILTER>& T, bool on)
 {
-    /* MASKED: the voxels are read only when `on` (0 otherwise) */
-    auto ld = [&](const uint8_t* q) {
-        return MASKED ? ldv_masked<DT>(q, V.dtype, on) : ldv<DT>(q, V.dtype);
-    };
+    /* the voxels are read only when `on` (the sample has data) */
+    auto ld = [&](const uint8_t* q) { return ldv_masked<DT>(q, V.dtype, on); };
     constexpr int NX = EDGE > 1 ? EDGE : 0;
     /* voxel pairs (pair_layout): known from the pitch for fixed-pitch
      * kernels, else the view's flag */
@@ -459,7 +457,7 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         {
             /* four voxel pairs: (x, x + 1) of rows y, y + 1 in slices z, z + 1 */
             auto ld2 = [&](const uint8_t* q) -> uint32_t {
-                return MASKED ? ld_pair_u8(q, on) : __ldg(reinterpret_cast<const uint16_t*>(q));
+                return ld_pair_u8(q, on);
             };
             const uint32_t q00 = ld2(p00), q01 = ld2(p01), q10 = ld2(p10), q11 = ld2(p11);
             T.c[0] = float(q00 & 0xFFu);
@@ -845,7 +843,7 @@ __device__ __forceinline__ bool fetch_sample(const RayView& V, const HV& H, RayS
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         sc[a] = fmaf(t, r.sa[a], r.sb[a]);
-    load_taps<DT, FILTER, EDGE, HV, true>(V, H, r.brick, sc, T, valid);
+    load_taps<DT, FILTER, EDGE>(V, H, r.brick, sc, T, valid);
     return live;
 }
 
