@@ -112,7 +112,7 @@ struct lv_batch
     uint32_t launches = 0;
     uint32_t last_n = 0;
     uint32_t sel_generation = 0; /* b->sel.generation the cached graphs use */
-    uint64_t captures = 0, replays = 0, updates = 0;
+    uint64_t captures = 0, replays = 0;
     /* the last lv_batch_autotune: every candidate and its mean ray-cast ms */
     std::vector<lv_batch_config> tune_cfgs;
     std::vector<float> tune_ms;
@@ -245,8 +245,8 @@ lv_status ensure_regions(lv_batch* b, const lv_batch_view* views, uint32_t n,
     LV_CUDA(ctx, b->zeroed.reserve(sizeof(uint32_t) * (kOutWords * vcap + 64)));
     LV_CUDA(ctx, b->leafs.reserve(sizeof(uint32_t) * b->cells_stride * vcap));
     /* per view: visible + render ids (u64) + render slots + view stamps
-     * (u32); then the missing lists of all views, contiguous so that one
-     * plain copy brings them to the host */
+     * (u32); then the missing lists of all views, contiguous (one
+     * read-back kernel brings them to the host) */
     const uint64_t lists_bytes = lists_per_view(b) * vcap + b->missing_stride * 8 * vcap;
     b->lists.release();
     LV_CUDA(ctx, b->lists.reserve(lists_bytes));
@@ -964,10 +964,7 @@ extern "C" lv_status lv_batch_render(lv_batch* b, const lv_batch_view* views, ui
             {
                 cudaGraphExecUpdateResultInfo info{};
                 if (cudaGraphExecUpdate(it->second, g, &info) == cudaSuccess)
-                {
-                    ++b->updates;
                     ++b->replays;
-                }
                 else
                 {
                     cudaGetLastError(); /* topology changed: instantiate anew */

@@ -743,8 +743,7 @@ lv_status run_selection(lv_ctx* ctx, const LodView* host_views,
 
 lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* dviews,
                             uint32_t n_views, uint32_t total_roots, uint32_t max_depth,
-                            cudaStream_t stream, const uint32_t* d_total_roots,
-                            uint32_t level_ctas)
+                            cudaStream_t stream, const uint32_t* d_total_roots)
 {
     const uint32_t cap = S.frontier_capacity;
     if (total_roots > cap)
@@ -758,11 +757,10 @@ lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* dviews
     LV_CUDA(ctx, cudaGetLastError());
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const uint32_t grid = level_ctas ? level_ctas : 2u * uint32_t(sms);
     for (uint32_t l = 0; l < max_depth; ++l)
     {
         const int in = l & 1, out = in ^ 1;
-        lod_level_kernel<<<grid, 256, 0, stream>>>(
+        lod_level_kernel<<<2 * sms, 256, 0, stream>>>(
             dviews, S.ids[in].as<uint64_t>(), S.view[in].as<uint32_t>(),
             counts + l, S.ids[out].as<uint64_t>(), S.view[out].as<uint32_t>(),
             counts + l + 1, cap, overflow);

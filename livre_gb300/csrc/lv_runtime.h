@@ -213,14 +213,10 @@ uint32_t selection_launches(lv_ctx* ctx, uint32_t n_views, uint32_t depth,
                             bool allow_fused = true);
 
 /* Enqueues the selection kernels for n views whose constants are already
- * on the device (capturable: no host synchronisation). level_ctas: CTAs of
- * each per-level launch (grid-stride), 0 = two per SM. A selection that
- * must start while other kernels fill the SMs (a server's admission) asks
- * for few: each level launch waits until its CTAs find free slots. */
+ * on the device (capturable: no host synchronisation). */
 lv_status enqueue_selection(lv_ctx* ctx, SelectScratch& S, const LodView* d_views,
                             uint32_t n_views, uint32_t total_roots, uint32_t max_depth,
-                            cudaStream_t stream, const uint32_t* d_total_roots = nullptr,
-                            uint32_t level_ctas = 0);
+                            cudaStream_t stream, const uint32_t* d_total_roots = nullptr);
 /* Grows the frontier queues of S to hold `nodes` per level (synchronises `s`
  * when it reallocates). */
 lv_status reserve_frontier(lv_ctx* ctx, SelectScratch& S, uint64_t nodes, cudaStream_t s);

@@ -93,10 +93,6 @@ struct lv_server_hook
  * behind it. */
 constexpr int kSlots = lv::kBatchPriorityLevels;
 
-/* CTAs of each level launch of the admission selection (grid-stride over
- * the frontier) */
-constexpr uint32_t kAdmissionCtas = 16;
-
 struct lv_server
 {
     lv_ctx* ctx = nullptr;
@@ -304,10 +300,7 @@ lv_status dry_run(lv_server* S, const std::vector<Req*>& cand,
             static_cast<const uint32_t*>(S->h_views.dev), S->views.as<uint32_t>(), words);
         LV_CUDA(ctx, cudaGetLastError());
     }
-    /* a narrow grid: under load the SMs are full of ray-cast CTAs, and each
-     * level launch waits until its CTAs find free slots */
-    st = enqueue_selection(ctx, S->sel, S->views.as<LodView>(), n, roots, depth, s, nullptr,
-                           kAdmissionCtas);
+    st = enqueue_selection(ctx, S->sel, S->views.as<LodView>(), n, roots, depth, s);
     if (st != LV_OK)
         return st;
     LV_CUDA(ctx, cudaEventRecord(S->sel_t1, s));
