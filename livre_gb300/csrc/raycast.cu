@@ -352,16 +352,42 @@ __device__ __forceinline__ uint32_t ld_pair_u8(const uint8_t* p, bool on)
     return v;
 }
 
+/* The four voxel pairs of a trilinear sample in a fixed-pitch pair-layout
+ * brick: rows y, y + 1 of slices z, z + 1 at byte offsets 0, DY, DZ and
+ * DZ + DY from p, read only when `on` under one predicate. */
+template <int DY, int DZ>
+__device__ __forceinline__ void ld_pairs4(const uint8_t* p, bool on, uint32_t (&q)[4])
+{
+    asm("{\n\t.reg .pred q;\n\t.reg .u64 g;\n\tcvta.to.global.u64 g, %4;\n\t"
+        "setp.ne.b32 q, %5, 0;\n\t"
+        "@q ld.global.nc.u16 %0, [g];\n\t"
+        "@q ld.global.nc.u16 %1, [g+%6];\n\t"
+        "@q ld.global.nc.u16 %2, [g+%7];\n\t"
+        "@q ld.global.nc.u16 %3, [g+%8];\n\t}"
+        : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3])
+        : "l"(p), "r"(uint32_t(on)), "n"(DY), "n"(DZ), "n"(DZ + DY));
+}
+
 /* The voxels a sample reads and its interpolation weights; loaded one
  * sample ahead of the compositing (march) so that the loads of the next
- * sample are in flight while the current one is composited. */
+ * sample are in flight while the current one is composited. The trilinear
+ * taps of the fixed-pitch voxel-pair kernels (raw_taps) stay as the four
+ * loaded pair words (voxel x in the low byte, x + 1 in the next) until the
+ * sample is composited: four registers per tap set instead of eight. */
 template <int FILTER>
 struct Taps
 {
     static constexpr int N = FILTER == LV_FILTER_TRILINEAR ? 8 : 1;
     float c[N];
+    uint32_t q[4]; /* raw_taps: rows (y, z), (y + 1, z), (y, z + 1), (y + 1, z + 1) */
     float fx, fy, fz;
 };
+
+template <int DT, int FILTER, int EDGE>
+__host__ __device__ constexpr bool raw_taps()
+{
+    return DT == LV_DT_UINT8 && FILTER == LV_FILTER_TRILINEAR && EDGE >= int(kPairMinRow);
+}
 
 /* The view constants the per-sample steps read (the transfer function and
  * its coordinate map, the early-termination opacity, the last trilinear
@@ -416,12 +442,15 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         return;
     }
     /* floor by adding 2^23 rounding down (exact for |s| < 2^22), no
-     * conversion instruction */
-    const float fx0 = __fadd_rd(s[0], 8388608.0f) - 8388608.0f;
-    const float fy0 = __fadd_rd(s[1], 8388608.0f) - 8388608.0f;
+     * conversion instruction; x and y as one packed pair */
+    const float2 kM = make_float2(8388608.0f, 8388608.0f);
+    const float2 sxy = make_float2(s[0], s[1]);
+    const float2 fxy0 = __fadd2_rn(__fadd2_rd(sxy, kM), make_float2(-8388608.0f, -8388608.0f));
+    const float fx0 = fxy0.x, fy0 = fxy0.y;
     const float fz0 = __fadd_rd(s[2], 8388608.0f) - 8388608.0f;
-    T.fx = s[0] - fx0;
-    T.fy = s[1] - fy0;
+    const float2 fxy = __ffma2_rn(fxy0, make_float2(-1.0f, -1.0f), sxy); /* s - floor(s) */
+    T.fx = fxy.x;
+    T.fy = fxy.y;
     T.fz = s[2] - fz0;
     const int ix = int(fx0), iy = int(fy0), iz = int(fz0);
     if (EDGE == 1)
@@ -453,13 +482,19 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
         const uint8_t* p01 = p00 + dy;
         const uint8_t* p10 = p00 + dz;
         const uint8_t* p11 = p10 + dy;
+        if (raw_taps<DT, FILTER, EDGE>())
+        {
+            /* four voxel pairs (x, x + 1) of rows y, y + 1 in slices z, z + 1,
+             * kept raw until the sample is composited */
+            ld_pairs4<2 * NX, 2 * NX * NX>(p00, on, T.q);
+            return;
+        }
         if (DT == LV_DT_UINT8 && pairs)
         {
-            /* four voxel pairs: (x, x + 1) of rows y, y + 1 in slices z, z + 1 */
-            auto ld2 = [&](const uint8_t* q) -> uint32_t {
-                return ld_pair_u8(q, on);
-            };
-            const uint32_t q00 = ld2(p00), q01 = ld2(p01), q10 = ld2(p10), q11 = ld2(p11);
+            /* the pair layout in a generic-pitch kernel: four pair loads,
+             * converted here */
+            const uint32_t q00 = ld_pair_u8(p00, on), q01 = ld_pair_u8(p01, on);
+            const uint32_t q10 = ld_pair_u8(p10, on), q11 = ld_pair_u8(p11, on);
             T.c[0] = float(q00 & 0xFFu);
             T.c[1] = float(q00 >> 8);
             T.c[2] = float(q01 & 0xFFu);
@@ -490,17 +525,35 @@ __device__ __forceinline__ void load_taps(const RayView& V, const HV& H, const u
  * b - a as fma(a, -1, b) is the same single rounding), paired so that every
  * result lands in the register pair the next stage reads: (a0, a2) and
  * (a1, a3), then (b0, b1). */
-template <int FILTER>
+template <int FILTER, bool RAW>
 __device__ __forceinline__ float interp(const Taps<FILTER>& T)
 {
     if (FILTER == LV_FILTER_NEAREST)
         return T.c[0];
     const float2 m1 = make_float2(-1.0f, -1.0f);
     const float2 fx = make_float2(T.fx, T.fx);
-    const float2 lo0 = make_float2(T.c[0], T.c[4]), hi0 = make_float2(T.c[1], T.c[5]);
-    const float2 lo1 = make_float2(T.c[2], T.c[6]), hi1 = make_float2(T.c[3], T.c[7]);
-    const float2 a02 = __ffma2_rn(__ffma2_rn(lo0, m1, hi0), fx, lo0);
-    const float2 a13 = __ffma2_rn(__ffma2_rn(lo1, m1, hi1), fx, lo1);
+    float2 a02, a13;
+    if (RAW)
+    {
+        /* a voxel byte b placed by a byte permute into the mantissa of 2^23
+         * is the float 2^23 + b (exact, no conversion instruction): the
+         * difference of two such floats is hi - lo exactly, and subtracting
+         * 2^23 gives lo exactly, so every lerp sees the values above */
+        auto lo = [](uint32_t q) { return __uint_as_float(__byte_perm(q, 0x4B000000u, 0x7440)); };
+        auto hi = [](uint32_t q) { return __uint_as_float(__byte_perm(q, 0x4B000000u, 0x7441)); };
+        const float2 mM = make_float2(-8388608.0f, -8388608.0f);
+        const float2 lo0 = make_float2(lo(T.q[0]), lo(T.q[2])), hi0 = make_float2(hi(T.q[0]), hi(T.q[2]));
+        const float2 lo1 = make_float2(lo(T.q[1]), lo(T.q[3])), hi1 = make_float2(hi(T.q[1]), hi(T.q[3]));
+        a02 = __ffma2_rn(__ffma2_rn(lo0, m1, hi0), fx, __fadd2_rn(lo0, mM));
+        a13 = __ffma2_rn(__ffma2_rn(lo1, m1, hi1), fx, __fadd2_rn(lo1, mM));
+    }
+    else
+    {
+        const float2 lo0 = make_float2(T.c[0], T.c[4]), hi0 = make_float2(T.c[1], T.c[5]);
+        const float2 lo1 = make_float2(T.c[2], T.c[6]), hi1 = make_float2(T.c[3], T.c[7]);
+        a02 = __ffma2_rn(__ffma2_rn(lo0, m1, hi0), fx, lo0);
+        a13 = __ffma2_rn(__ffma2_rn(lo1, m1, hi1), fx, lo1);
+    }
     const float2 b01 = __ffma2_rn(__ffma2_rn(a02, m1, a13), make_float2(T.fy, T.fy), a02);
     return fmaf(b01.y - b01.x, T.fz, b01.x);
 }
@@ -852,12 +905,12 @@ __device__ __forceinline__ bool fetch_sample(const RayView& V, const HV& H, RayS
  * opacity is reached. A sample without data (!valid) is blended with opacity
  * 0 (the colour and opacity stay bit for bit as they were) and not counted,
  * so the march needs no branch around it. */
-template <int FILTER, int TFS, class HV>
+template <int FILTER, int TFS, bool RAW, class HV>
 __device__ __forceinline__ bool composite_sample(const HV& H, RayState& r, float ac,
                                                  const Taps<FILTER>& T, bool valid,
                                                  uint32_t& nsamp)
 {
-    const float4 src = tf_lookup<TFS>(H, interp<FILTER>(T));
+    const float4 src = tf_lookup<TFS>(H, interp<FILTER, RAW>(T));
     const float am = fminf(src.w, 1.0f - 1.0f / 256.0f);
     const float alpha = valid ? 1.0f - ex2_approx(ac * lg2_approx(1.0f - am)) : 0.0f;
     const float w = alpha * (1.0f - r.dst.w);
@@ -878,7 +931,8 @@ __device__ __forceinline__ bool ray_step(const RayView& V, const HV& H, RayState
     Taps<FILTER> T;
     bool valid;
     const bool live = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T, valid);
-    const bool cont = composite_sample<FILTER, TFS>(H, r, ac, T, valid, nsamp);
+    const bool cont =
+        composite_sample<FILTER, TFS, raw_taps<DT, FILTER, EDGE>()>(H, r, ac, T, valid, nsamp);
     return live && cont;
 }
 
@@ -923,16 +977,17 @@ __device__ float4 march(const RayView& V, const HV& H, const RayGeom& g, float s
      * next sample into one while the other is composited. A sample without
      * data is fetched and composited masked, so each sample has one
      * divergent region (a brick lookup) and one loop exit. */
+    constexpr bool RAW = raw_taps<DT, FILTER, EDGE>();
     Taps<FILTER> T0, T1;
     bool v0, v1;
     bool live0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0, v0);
     while (live0)
     {
         const bool live1 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T1, v1);
-        if (!(composite_sample<FILTER, TFS>(H, r, ac, T0, v0, nsamp) && live1))
+        if (!(composite_sample<FILTER, TFS, RAW>(H, r, ac, T0, v0, nsamp) && live1))
             break;
         live0 = fetch_sample<DT, FILTER, EDGE>(V, H, r, step, T0, v0);
-        if (!composite_sample<FILTER, TFS>(H, r, ac, T1, v1, nsamp))
+        if (!composite_sample<FILTER, TFS, RAW>(H, r, ac, T1, v1, nsamp))
             break;
     }
     flush_error(V, r);
