@@ -104,6 +104,12 @@ struct PinnedBuffer
     {
         return static_cast<T*>(ptr);
     }
+    /* the same memory as the device addresses it (mapped) */
+    template <class T>
+    T* as_dev() const
+    {
+        return static_cast<T*>(dev);
+    }
 };
 
 /* Scratch of the LOD selection: two frontier queues + per-level counters. */
@@ -328,6 +334,11 @@ struct Renderer
     PinnedBuffer h_expand;
     cudaEvent_t expand_done = nullptr;
     bool expand_recorded = false;
+    /* (source, slot) offsets of the host-store bricks gather_bricks_kernel
+     * reads, mapped; rewritten only once gather_done has completed */
+    PinnedBuffer h_gather;
+    cudaEvent_t gather_done = nullptr;
+    bool gather_recorded = false;
 };
 
 

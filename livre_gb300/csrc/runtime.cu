@@ -130,6 +130,68 @@ __global__ void __launch_bounds__(kExpandThreads)
     }
 }
 
+/* Copies bricks from mapped page-locked host memory straight into their
+ * slots, in the pool's layout: voxel pairs (pairs != 0, pair_layout: element
+ * j = v[j] | v[j + 1] << 8 within a row of n0, the last voxel of a row with
+ * itself) or the bytes as they are. One kernel reads every missing brick of
+ * a frame over the host link at once, where a copy-engine transfer per brick
+ * (and an expansion pass after it) costs a transfer's set-up per brick.
+ * Brick blockIdx.x is read at src + offs[2b] and written at arena +
+ * offs[2b + 1] (a slot, 1 KiB aligned); gridDim.y blocks share a brick, each
+ * a run of whole 8-byte words. `bytes` is a multiple of 8 and every source
+ * offset is a multiple of `bytes`, so every word load is 8-byte aligned. A
+ * voxel's +x neighbour is the next byte of its word, the next lane's first
+ * byte, or (at the end of a block's run) one byte read on its own. */
+constexpr uint32_t kGatherThreads = 256;
+
+__global__ void __launch_bounds__(kGatherThreads)
+    gather_bricks_kernel(uint8_t* __restrict__ arena, const uint8_t* __restrict__ src,
+                         const uint64_t* __restrict__ offs, uint32_t bytes, uint32_t n0,
+                         uint32_t pairs)
+{
+    const uint8_t* s = src + offs[2 * blockIdx.x];
+    uint8_t* d = arena + offs[2 * blockIdx.x + 1];
+    const uint32_t words = bytes / 8;
+    const uint32_t per = (words + gridDim.y - 1) / gridDim.y;
+    const uint32_t w0 = min(words, blockIdx.y * per), w1 = min(words, w0 + per);
+    const uint32_t lane = threadIdx.x & 31u;
+    /* every lane runs every pass (the shuffle below needs the whole warp) */
+    for (uint32_t base = w0; base < w1; base += kGatherThreads)
+    {
+        const uint32_t w = base + threadIdx.x;
+        const bool in = w < w1;
+        const uint2 v = in ? *reinterpret_cast<const uint2*>(s + 8ull * w) : make_uint2(0u, 0u);
+        if (!pairs)
+        {
+            if (in)
+                *reinterpret_cast<uint2*>(d + 8ull * w) = v;
+            continue;
+        }
+        /* the byte after this word: the next lane's first byte while that
+         * lane's word is in this block's run, else read here */
+        uint32_t next = __shfl_down_sync(0xFFFFFFFFu, v.x & 0xFFu, 1);
+        if (in && (lane == 31u || w + 1 >= w1))
+            next = w + 1 < words ? uint32_t(s[8ull * w + 8]) : 0u;
+        if (!in)
+            continue;
+        const uint32_t b[9] = {v.x & 0xFFu,         (v.x >> 8) & 0xFFu, (v.x >> 16) & 0xFFu,
+                               v.x >> 24,           v.y & 0xFFu,        (v.y >> 8) & 0xFFu,
+                               (v.y >> 16) & 0xFFu, v.y >> 24,          next};
+        uint32_t x = (8u * w) % n0; /* column of the word's first voxel */
+        uint32_t e[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+        {
+            e[k] = b[k] | ((x == n0 - 1u ? b[k] : b[k + 1]) << 8);
+            x = x + 1u == n0 ? 0u : x + 1u;
+        }
+        /* 16 bytes at slot + 16 w: 16-byte aligned */
+        *reinterpret_cast<uint4*>(d + 16ull * w) =
+            make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16),
+                       e[6] | (e[7] << 16));
+    }
+}
+
 lv_status words_to_host(lv_ctx* ctx, const void* d_src, const PinnedBuffer& host,
                         size_t word_offset, uint32_t n, cudaStream_t s)
 {
@@ -250,6 +312,7 @@ lv_status ensure_renderer(lv_ctx* ctx)
     cudaEventCreateWithFlags(&r->render_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->upload_event, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->expand_done, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&r->gather_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->frame_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->resolve_done, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&r->fork, cudaEventDisableTiming);
@@ -445,6 +508,9 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>> updates;
     std::vector<uint64_t> gen_ids, gen_offsets;
     std::vector<uint64_t> expand; /* slots to expand into voxel pairs */
+    /* host-store bricks read by gather_bricks_kernel: (source, slot) offsets */
+    std::vector<uint64_t> gather;
+    const bool gathered = vol->kind == SRC_BLOB_HOST && vol->brick_bytes % 8 == 0;
     uint8_t* arena = P.arena.as<uint8_t>();
     lv_status st = LV_OK;
     /* the bookkeeping of a brick placed in `unit` */
@@ -532,7 +598,13 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                 st = fail(ctx, LV_EAGAIN, "brick pool full of bricks in use");
                 break;
             }
-            if (vol->kind == SRC_BLOB_HOST)
+            if (gathered)
+            {
+                gather.push_back(idx * vol->brick_bytes);
+                gather.push_back(uint64_t(unit) * kSlotUnit);
+                bytes_loaded += vol->brick_bytes;
+            }
+            else if (vol->kind == SRC_BLOB_HOST)
             {
                 const uint8_t* src = vol->host_store.as<uint8_t>() + idx * vol->brick_bytes;
                 LV_CUDA(ctx, cudaMemcpyAsync(arena + uint64_t(unit) * kSlotUnit + vol->stage_off,
@@ -544,7 +616,7 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                 gen_ids.push_back(id);
                 gen_offsets.push_back(uint64_t(unit) * kSlotUnit + vol->stage_off);
             }
-            if (vol->stage_off)
+            if (vol->stage_off && !gathered)
                 expand.push_back(uint64_t(unit) * kSlotUnit);
             place(idx, unit);
         }
@@ -572,6 +644,28 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                                      dids.as<uint64_t>() + gen_ids.size(), up);
         if (g != LV_OK)
             return g;
+    }
+    if (!gather.empty())
+    {
+        /* the offsets' buffer is read by the previous gather until it ends */
+        if (R.gather_recorded)
+            LV_CUDA(ctx, cudaEventSynchronize(R.gather_done));
+        LV_CUDA(ctx, R.h_gather.reserve(sizeof(uint64_t) * gather.size()));
+        std::memcpy(R.h_gather.ptr, gather.data(), sizeof(uint64_t) * gather.size());
+        const uint32_t nb = uint32_t(gather.size() / 2);
+        /* about four blocks per SM in all, at least one pass per block */
+        int sms = 0;
+        LV_CUDA(ctx, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device));
+        const uint32_t words = uint32_t(vol->brick_bytes / 8);
+        const uint32_t split = std::max(
+            1u, std::min((4u * uint32_t(sms) + nb - 1) / nb,
+                         (words + kGatherThreads - 1) / kGatherThreads));
+        gather_bricks_kernel<<<dim3(nb, split), kGatherThreads, 0, up>>>(
+            arena, vol->host_store.as_dev<uint8_t>(), static_cast<const uint64_t*>(R.h_gather.dev),
+            uint32_t(vol->brick_bytes), vol->info.max_block[0], vol->stage_off != 0);
+        LV_CUDA(ctx, cudaGetLastError());
+        LV_CUDA(ctx, cudaEventRecord(R.gather_done, up));
+        R.gather_recorded = true;
     }
     if (!expand.empty())
     {
@@ -892,6 +986,7 @@ extern "C" void lv_ctx_destroy(lv_ctx* ctx)
         cudaEventDestroy(ctx->renderer->render_event);
         cudaEventDestroy(ctx->renderer->upload_event);
         cudaEventDestroy(ctx->renderer->expand_done);
+        cudaEventDestroy(ctx->renderer->gather_done);
         cudaEventDestroy(ctx->renderer->frame_done);
         cudaEventDestroy(ctx->renderer->resolve_done);
         cudaEventDestroy(ctx->renderer->fork);
