@@ -105,6 +105,11 @@ struct RayView
     float tf_last;        /* tfn - 1 */
     uint32_t accumulate;  /* 1: rays start from the colour already in out (a
                              later pass of a multi-pass frame) */
+    uint32_t skip_if_missing; /* 1: a synchronous frame's first ray cast, queued
+                                 before its miss count reached the host: it
+                                 renders nothing if the residency pass counted
+                                 misses (the host streams them and renders the
+                                 frame again) */
     uint32_t max_base;    /* last trilinear base voxel of a brick:
                              (N2-2)*N1*N0 + (N1-2)*N0 + N0-2 */
     float early;

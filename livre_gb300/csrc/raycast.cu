@@ -994,10 +994,20 @@ __device__ float4 march(const RayView& V, const HV& H, const RayGeom& g, float s
     return r.dst;
 }
 
+/* The ray cast of a view whose frame will be rendered again
+ * (RayView::skip_if_missing): every block of the launch returns at once. */
+__device__ __forceinline__ bool skip_frame(const RayView& V)
+{
+    return V.skip_if_missing &&
+           *static_cast<const volatile uint32_t*>(V.counters + FC_MISSING) != 0u;
+}
+
 /* LA: one-sample look-ahead */
 template <int DT, int FILTER, int EDGE, int LA>
 __global__ void __launch_bounds__(256) raycast_kernel(const RayView V)
 {
+    if (skip_frame(V))
+        return;
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t py = blockIdx.y * blockDim.y + threadIdx.y;
     const uint32_t n = frame_samples(V);
@@ -1200,6 +1210,8 @@ __global__ void __launch_bounds__(256)
     raycast_queue_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h,
                          const uint32_t* __restrict__ order)
 {
+    if (skip_frame(V))
+        return;
     __shared__ uint32_t s_item;
     const uint32_t n = frame_samples(V);
     const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
@@ -1241,6 +1253,8 @@ __global__ void __launch_bounds__(256)
     raycast_tiles_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h,
                          const uint32_t* __restrict__ order)
 {
+    if (skip_frame(V))
+        return;
     const uint32_t n = frame_samples(V);
     const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
     const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
@@ -1270,6 +1284,8 @@ __global__ void __launch_bounds__(128)
     raycast_warp_tiles_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h,
                               const uint32_t* __restrict__ order)
 {
+    if (skip_frame(V))
+        return;
     const uint32_t n = frame_samples(V);
     const float step = __fdiv_rn(1.0f, __uint2float_rn(n));
     const float ac = __fdiv_rn(32.0f, __uint2float_rn(n));
@@ -1556,6 +1572,8 @@ __global__ void __launch_bounds__(kRefillThreads, kRefillMinCtas)
     raycast_refill_kernel(const RayView V, uint32_t tile_w, uint32_t tile_h, uint32_t checks,
                           const uint32_t* __restrict__ order)
 {
+    if (skip_frame(V))
+        return;
     TileQueue Q{};
     Q.tile_w = tile_w;
     Q.tile_h = tile_h;

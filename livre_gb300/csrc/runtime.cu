@@ -69,6 +69,22 @@ __global__ void words_to_host_kernel(const uint32_t* __restrict__ src, uint32_t*
     __threadfence_system();
 }
 
+/* A synchronous frame's counters and its missing list (as many ids as the
+ * residency pass appended, at most cap) into mapped page-locked host
+ * memory: the host learns which bricks to stream when it learns how many,
+ * without a copy queued behind the frame's first ray cast. */
+__global__ void counters_to_host_kernel(const uint32_t* __restrict__ counters,
+                                        const uint64_t* __restrict__ missing, uint32_t* words,
+                                        uint64_t* ids, uint32_t cap)
+{
+    const uint32_t n = min(counters[FC_MISSING], cap);
+    if (blockIdx.x == 0 && threadIdx.x < FC_WORDS)
+        words[threadIdx.x] = counters[threadIdx.x];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        ids[i] = missing[i];
+    __threadfence_system();
+}
+
 /* Expands uint8 bricks into voxel pairs in place (pair_layout). Block b
  * takes the slot at arena + offsets[b], whose canonical bytes (`voxels` of
  * them, x fastest, rows of n0) are at slot + stage_off, stage_off >= voxels
@@ -1864,17 +1880,23 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         st = resolve();
         if (st != LV_OK)
             return st;
-        st = words_to_host(ctx, R.counters.ptr, R.h_counters, 0, FC_WORDS, s);
-        if (st != LV_OK)
-            return st;
+        /* the counters and the missing ids, through the host mapping */
+        counters_to_host_kernel<<<8, 256, 0, s>>>(
+            R.counters.as<uint32_t>(), R.missing.as<uint64_t>(), R.h_counters.as_dev<uint32_t>(),
+            R.h_missing.as_dev<uint64_t>(), RV.missing_capacity);
+        LV_CUDA(ctx, cudaGetLastError());
         LV_CUDA(ctx, cudaEventRecord(R.resolve_done, s));
         /* a volume that streamed last frame likely misses again: then the
          * ray cast waits for the streaming instead of running twice (unless
-         * this frame's misses were streamed beside the previous frame) */
+         * this frame's misses were streamed beside the previous frame).
+         * Queued before the miss count is known, the ray cast returns at
+         * once if there are misses (skip_if_missing). */
         const bool queued = !vol->streamed_last || prefetched;
         if (queued)
         {
+            V.skip_if_missing = 1u;
             st = after_resolve();
+            V.skip_if_missing = 0u;
             if (st != LV_OK)
                 return st;
         }
@@ -1884,10 +1906,6 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
             st = after_resolve();
         else if (missing)
         {
-            LV_CUDA(ctx, cudaMemcpyAsync(R.h_missing.ptr, R.missing.ptr,
-                                         sizeof(uint64_t) * missing,
-                                         cudaMemcpyDeviceToHost, s));
-            LV_CUDA(ctx, cudaStreamSynchronize(s));
             uint32_t loaded = 0;
             uint64_t bytes = 0;
             st = timed_stream(R.h_missing.as<uint64_t>(), missing, frame, loaded, bytes);
