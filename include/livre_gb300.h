@@ -193,16 +193,17 @@ lv_status lv_pool_purge(lv_ctx* ctx);
  * one texture per brick, TextureObject.cpp:76-120). */
 enum
 {
-    LV_BRICKS_PAIRS = 0,  /* default: uint8 bricks of 64 or more voxels per
-                             row stored as voxel pairs (each voxel with its
-                             +x neighbour), so a trilinear sample reads four
-                             16-bit words instead of eight bytes: twice the
-                             pool bytes, a ~10 % faster ray cast on a 2048^3
+    LV_BRICKS_QUADS = 0,  /* default: uint8 bricks of 64 to 1024 voxels per
+                             row stored as voxel quads (each voxel with its
+                             +x, +y and +x+y neighbours in one 32-bit
+                             element), so a trilinear sample reads two words
+                             instead of eight bytes: four times the pool
+                             bytes, a ~15 % faster ray cast on a 2048^3
                              volume of 64^3 bricks; other bricks compact */
-    LV_BRICKS_COMPACT = 1 /* one voxel per element for every brick: twice as
-                             many large uint8 bricks per pool byte (a server
-                             whose volumes' visible sets outgrow the pool
-                             with pairs) */
+    LV_BRICKS_COMPACT = 1 /* one voxel per element for every brick: four
+                             times as many large uint8 bricks per pool byte
+                             (a server whose volumes' visible sets outgrow
+                             the pool with quads) */
 };
 /* Brick layout of the pool; like lv_pool_configure, before the first volume
  * is created. */

@@ -24,7 +24,7 @@ import weakref
 import numpy as np
 
 from . import _abi
-from ._abi import (BLOB_DEVICE, BLOB_HOST, BRICKS_COMPACT, BRICKS_PAIRS, DT_UINT8, DT_UINT16, FBM_DEVICE, FBM_HOST,
+from ._abi import (BLOB_DEVICE, BLOB_HOST, BRICKS_COMPACT, BRICKS_QUADS, DT_UINT8, DT_UINT16, FBM_DEVICE, FBM_HOST,
                    FILTER_NEAREST,
                    FILTER_TRILINEAR, LAUNCH_GRID, LAUNCH_TILE_GRID, LAUNCH_TILE_QUEUE,
                    LAUNCH_WARP_REFILL, LAUNCH_WARP_TILES,
@@ -551,7 +551,7 @@ class Context:
     """One CUDA device; owns the brick pool (lv_ctx)."""
 
     def __init__(self, device=0, pool_bytes=None, brick_layout=None):
-        """brick_layout: BRICKS_PAIRS (the default) or BRICKS_COMPACT
+        """brick_layout: BRICKS_QUADS (the default) or BRICKS_COMPACT
         (lv_pool_set_brick_layout)."""
         self._children = weakref.WeakSet()
         _live_contexts.add(self)

@@ -87,7 +87,7 @@ class BatchView(C.Structure):
                 ("d_rgba", C.c_void_p)]
 
 
-BRICKS_PAIRS = 0
+BRICKS_QUADS = 0
 BRICKS_COMPACT = 1
 
 QUEUE_CTA_TILES = 0

@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256)
         if (DT == LV_DT_UINT16)
             v = float(reinterpret_cast<const uint16_t*>(brick)[idx]);
         else if (DT == LV_DT_UINT8)
-            v = float(brick[u8_stride * idx]); /* 2: voxel pairs, the element's low byte */
+            v = float(brick[u8_stride * idx]); /* 4: voxel quads, the element's byte 0 */
         else /* kDtAny: the voxel type `dt` */
             switch (dt)
             {
@@ -139,7 +139,7 @@ extern "C" lv_status lv_histogram(lv_volume* vol, const uint64_t* ids, uint32_t 
                                            : histogram_kernel<kDtAny>;
     kernel<<<n, 256, smem, s>>>(ctx->pool->arena.as<uint8_t>(), djobs.as<HistJob>(),
                                 I.max_block[0], I.max_block[1], I.max_block[2], I.overlap[0],
-                                I.overlap[1], I.overlap[2], I.dtype, vol->stage_off ? 2u : 1u,
+                                I.overlap[1], I.overlap[2], I.dtype, vol->stage_off ? 4u : 1u,
                                 n_bins, range_lo, scale_bins,
                                 per_brick ? dout.as<unsigned long long>() : nullptr,
                                 dacc.as<unsigned long long>());

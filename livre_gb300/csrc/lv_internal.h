@@ -24,19 +24,22 @@ constexpr uint64_t kInvalidNode = ~0ull;
 /* Pool addresses are stored as 1 KiB units (27 bits: 128 GiB). */
 constexpr uint64_t kSlotUnit = 1024;
 
-/* Brick layout in the pool for uint8 bricks of at least kPairMinRow voxels
- * per row: voxel pairs. Element i of a brick (the voxels in x-fastest
- * order) holds voxel i in its low byte and its +x neighbour in its high byte
- * (the voxel itself at the end of a row), so a trilinear sample's eight
- * voxels are four aligned 16-bit loads instead of eight byte loads. A single
- * voxel is the element's low byte. Twice the bytes per brick. Smaller uint8
- * bricks and the other voxel types keep one voxel per element (on the 256^3
- * / 32^3-brick workload, whose frame time is its longest rays' chains, the
- * pairs measured slower). */
-constexpr uint32_t kPairMinRow = 64;
-__host__ __device__ constexpr bool pair_layout(uint32_t dtype, uint32_t row_voxels)
+/* Brick layout in the pool for uint8 bricks of kQuadMinRow to kQuadMaxRow
+ * voxels per row: voxel quads. Element i of a brick (the voxels in
+ * x-fastest order) is 32 bits: voxel i in byte 0, its +x neighbour in byte
+ * 1, its +y neighbour in byte 2 and its +x+y neighbour in byte 3 (a
+ * neighbour past the end of a row or slice is the voxel itself), so a
+ * trilinear sample's eight voxels are two aligned 32-bit loads (slices z and
+ * z + 1) instead of eight byte loads. A single voxel is the element's byte
+ * 0. Four times the bytes per brick. Smaller uint8 bricks and the other
+ * voxel types keep one voxel per element (on the 256^3 / 32^3-brick
+ * workload, whose frame time is its longest rays' chains, wider elements
+ * measured slower). */
+constexpr uint32_t kQuadMinRow = 64;
+constexpr uint32_t kQuadMaxRow = 1024;
+__host__ __device__ constexpr bool quad_layout(uint32_t dtype, uint32_t row_voxels)
 {
-    return dtype == LV_DT_UINT8 && row_voxels >= kPairMinRow;
+    return dtype == LV_DT_UINT8 && row_voxels >= kQuadMinRow && row_voxels <= kQuadMaxRow;
 }
 
 LV_HD uint32_t nid_level(uint64_t id) { return uint32_t(id & 0xFu); }
@@ -98,7 +101,7 @@ struct RayView
     uint32_t bpv;     /* bytes per voxel */
     uint32_t filter;
     uint32_t edge;    /* 1: some overlap is 0, clamp every trilinear tap */
-    uint32_t pairs;   /* bricks stored as voxel pairs (pair_layout) */
+    uint32_t quads;   /* bricks stored as voxel quads (quad_layout) */
     float dmul, dadd; /* density = value * dmul + dadd */
     float tf_mul, tf_add; /* TF texel coordinate = value * tf_mul + tf_add
                              = density * tfn - 0.5 */

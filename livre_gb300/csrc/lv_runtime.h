@@ -158,7 +158,7 @@ struct lv_ctx
     lv::Pool* pool = nullptr;
     lv::Renderer* renderer = nullptr;
     size_t pool_bytes = size_t(3072) << 20;
-    uint32_t brick_layout = LV_BRICKS_PAIRS; /* lv_pool_set_brick_layout */
+    uint32_t brick_layout = LV_BRICKS_QUADS; /* lv_pool_set_brick_layout */
     /* lv_render's ray cast */
     lv_render_launch launch{LV_LAUNCH_TILE_GRID, 8, 8, 0, LV_ORDER_LONGEST_FIRST, 1};
     /* host fetchers of callback sources (created on first use) */
@@ -328,7 +328,7 @@ struct Renderer
     /* device-generated bricks: ids and slot offsets */
     DeviceBuffer gen;
     PinnedBuffer h_gen;
-    /* slot offsets of the uint8 bricks to expand into voxel pairs, read by
+    /* slot offsets of the uint8 bricks to expand into voxel quads, read by
      * the expansion kernel from mapped memory; free again once
      * expand_done has completed */
     PinnedBuffer h_expand;
@@ -431,9 +431,10 @@ struct lv_volume
     lv::PinnedBuffer host_store;
     uint64_t brick_bytes = 0;
     uint32_t slot_units = 0;
-    /* uint8 volumes store their bricks as voxel pairs (lv_internal.h,
-     * kPairLayout): a brick's canonical bytes are written at slot +
-     * stage_off, then expanded in place; 0 for the other types */
+    /* uint8 volumes of quad_layout rows store their bricks as voxel quads
+     * (lv_internal.h) unless the pool keeps them compact: a brick's
+     * canonical bytes are written at slot + stage_off, then expanded in
+     * place (or gathered straight into the quads); 0 for the others */
     uint64_t stage_off = 0;
     uint64_t level_offset[lv::kMaxLevels + 1] = {};
     uint64_t n_nodes = 0;

@@ -85,126 +85,129 @@ __global__ void counters_to_host_kernel(const uint32_t* __restrict__ counters,
     __threadfence_system();
 }
 
-/* Expands uint8 bricks into voxel pairs in place (pair_layout). Block b
+/* Voxel quads (quad_layout) of elements [j0, j0 + m) of a uint8 brick with
+ * rows of n0 voxels and slices of n1 rows, from its canonical bytes c[i] =
+ * byte j0 + i for i < min(voxels - j0, m + n0 + 1) (the elements' own bytes,
+ * then one row and one byte more: every neighbour a quad takes), written as
+ * 32-bit elements at q[j0 ..]. j0 is a multiple of 4 and q 16-byte aligned:
+ * four elements per 16-byte store. A neighbour past the end of a row or
+ * slice is the voxel itself. */
+__device__ __forceinline__ void quads_from_bytes(const uint8_t* c, uint32_t* q, uint32_t j0,
+                                                 uint32_t m, uint32_t n0, uint32_t n1)
+{
+    for (uint32_t k = 4u * threadIdx.x; k < m; k += 4u * blockDim.x)
+    {
+        uint32_t x = (j0 + k) % n0, y = ((j0 + k) / n0) % n1;
+        uint32_t e[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (uint32_t t = 0; t < 4; ++t)
+        {
+            const uint32_t i = k + t;
+            if (i < m)
+            {
+                const bool xr = x + 1u < n0, yr = y + 1u < n1;
+                const uint32_t b0 = c[i];
+                const uint32_t b1 = xr ? c[i + 1] : b0;
+                const uint32_t b2 = yr ? c[i + n0] : b0;
+                const uint32_t b3 = xr && yr ? c[i + n0 + 1] : xr ? b1 : b2;
+                e[t] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+            }
+            if (++x == n0)
+            {
+                x = 0u;
+                y = y + 1u == n1 ? 0u : y + 1u;
+            }
+        }
+        if (k + 4u <= m)
+            *reinterpret_cast<uint4*>(q + j0 + k) = make_uint4(e[0], e[1], e[2], e[3]);
+        else
+            for (uint32_t t = 0; k + t < m; ++t)
+                q[j0 + k + t] = e[t];
+    }
+}
+
+/* Elements a block turns into quads per pass, and the canonical bytes it
+ * stages for them (one row of at most kQuadMaxRow voxels and one byte more,
+ * rounded up to whole 8-byte words). */
+constexpr uint32_t kQuadRun = 4096;
+constexpr uint32_t kQuadStage = kQuadRun + kQuadMaxRow + 8;
+
+/* Expands uint8 bricks into voxel quads in place (quad_layout). Block b
  * takes the slot at arena + offsets[b], whose canonical bytes (`voxels` of
- * them, x fastest, rows of n0) are at slot + stage_off, stage_off >= voxels
- * and 256-byte aligned. Element j is written at slot + 2j and overwrites
- * canonical bytes of index 2j - stage_off and 2j + 1 - stage_off, both
- * below j: the block takes chunks of elements in increasing order, reading
- * a chunk's canonical bytes (and the next one) before any of its writes, so
- * no element reads a byte an earlier write has replaced. */
+ * them, x fastest, rows of n0, slices of n1 rows) are at slot + stage_off,
+ * stage_off >= 3 * voxels and 256-byte aligned. The block takes runs of
+ * elements in increasing order, staging a run's canonical bytes (and the
+ * row after them) in shared memory before any of its writes; the run ending
+ * at element j writes slot bytes below 4j <= stage_off + j, so no later run
+ * finds a canonical byte replaced. */
 constexpr uint32_t kExpandThreads = 512;
-constexpr uint32_t kExpandPer = 16; /* elements per thread and chunk */
 
 __global__ void __launch_bounds__(kExpandThreads)
-    expand_pairs_kernel(uint8_t* __restrict__ arena, const uint64_t* __restrict__ offsets,
-                        uint32_t n0, uint32_t voxels, uint32_t stage_off)
+    expand_quads_kernel(uint8_t* __restrict__ arena, const uint64_t* __restrict__ offsets,
+                        uint32_t n0, uint32_t n1, uint32_t voxels, uint32_t stage_off)
 {
+    __shared__ uint32_t s_c[kQuadStage / 4];
+    uint8_t* sb = reinterpret_cast<uint8_t*>(s_c);
     uint8_t* slot = arena + offsets[blockIdx.x];
     const uint8_t* canon = slot + stage_off;
-    constexpr uint32_t chunk = kExpandThreads * kExpandPer;
-    for (uint32_t j0 = 0; j0 < voxels; j0 += chunk)
+    for (uint32_t j0 = 0; j0 < voxels; j0 += kQuadRun)
     {
-        const uint32_t j = j0 + threadIdx.x * kExpandPer;
-        uint32_t v[kExpandPer + 1];
-        if (j + kExpandPer <= voxels)
-        {
-            const uint4 w = *reinterpret_cast<const uint4*>(canon + j); /* 16-byte aligned */
-            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-            for (uint32_t k = 0; k < kExpandPer; ++k)
-                v[k] = (ws[k / 4] >> (8 * (k % 4))) & 0xFFu;
-            v[kExpandPer] = j + kExpandPer < voxels ? canon[j + kExpandPer] : 0u;
-        }
-        else
-#pragma unroll
-            for (uint32_t k = 0; k <= kExpandPer; ++k)
-                v[k] = j + k < voxels ? canon[j + k] : 0u;
-        __syncthreads(); /* the chunk read before any of its writes */
-        if (j + kExpandPer <= voxels)
-        {
-            uint32_t out[kExpandPer / 2];
-#pragma unroll
-            for (uint32_t k = 0; k < kExpandPer; k += 2)
-            {
-                const uint32_t e0 = v[k] | ((((j + k) % n0) == n0 - 1 ? v[k] : v[k + 1]) << 8);
-                const uint32_t e1 =
-                    v[k + 1] | ((((j + k + 1) % n0) == n0 - 1 ? v[k + 1] : v[k + 2]) << 8);
-                out[k / 2] = e0 | (e1 << 16);
-            }
-            uint4* dst = reinterpret_cast<uint4*>(slot + 2ull * j); /* 32-byte aligned */
-            dst[0] = make_uint4(out[0], out[1], out[2], out[3]);
-            dst[1] = make_uint4(out[4], out[5], out[6], out[7]);
-        }
-        else
-            for (uint32_t k = 0; k < kExpandPer && j + k < voxels; ++k)
-            {
-                const uint32_t hi = ((j + k) % n0) == n0 - 1 ? v[k] : v[k + 1];
-                reinterpret_cast<uint16_t*>(slot)[j + k] = uint16_t(v[k] | (hi << 8));
-            }
-        __syncthreads(); /* the chunk written before the next one reads */
+        const uint32_t m = min(kQuadRun, voxels - j0);
+        const uint32_t L = min(voxels - j0, m + n0 + 1u);
+        /* canon + j0 is 4-byte aligned (stage_off 256-aligned, j0 a
+         * multiple of kQuadRun) */
+        const uint32_t* cw = reinterpret_cast<const uint32_t*>(canon + j0);
+        for (uint32_t i = threadIdx.x; i < L / 4u; i += blockDim.x)
+            s_c[i] = cw[i];
+        for (uint32_t i = (L / 4u) * 4u + threadIdx.x; i < L; i += blockDim.x)
+            sb[i] = canon[j0 + i];
+        __syncthreads(); /* the run staged before any of its writes */
+        quads_from_bytes(sb, reinterpret_cast<uint32_t*>(slot), j0, m, n0, n1);
+        __syncthreads(); /* the run written before the next one is staged */
     }
 }
 
 /* Copies bricks from mapped page-locked host memory straight into their
- * slots, in the pool's layout: voxel pairs (pairs != 0, pair_layout: element
- * j = v[j] | v[j + 1] << 8 within a row of n0, the last voxel of a row with
- * itself) or the bytes as they are. One kernel reads every missing brick of
- * a frame over the host link at once, where a copy-engine transfer per brick
- * (and an expansion pass after it) costs a transfer's set-up per brick.
- * Brick blockIdx.x is read at src + offs[2b] and written at arena +
- * offs[2b + 1] (a slot, 1 KiB aligned); gridDim.y blocks share a brick, each
- * a run of whole 8-byte words. `bytes` is a multiple of 8 and every source
- * offset is a multiple of `bytes`, so every word load is 8-byte aligned. A
- * voxel's +x neighbour is the next byte of its word, the next lane's first
- * byte, or (at the end of a block's run) one byte read on its own. */
+ * slots, in the pool's layout: voxel quads (quads != 0) or the bytes as they
+ * are. One kernel reads every missing brick of a frame over the host link
+ * at once, where a copy-engine transfer per brick (and an expansion pass
+ * after it) costs a transfer's set-up per brick. Brick blockIdx.x is read at
+ * src + offs[2b] and written at arena + offs[2b + 1] (a slot, 1 KiB
+ * aligned); gridDim.y blocks share a brick, each a run of whole 8-byte
+ * words. `bytes` is a multiple of 8 and every source offset a multiple of
+ * `bytes`, so every word load is 8-byte aligned. For quads a block stages a
+ * run's canonical bytes and the row after them in shared memory. */
 constexpr uint32_t kGatherThreads = 256;
 
 __global__ void __launch_bounds__(kGatherThreads)
     gather_bricks_kernel(uint8_t* __restrict__ arena, const uint8_t* __restrict__ src,
                          const uint64_t* __restrict__ offs, uint32_t bytes, uint32_t n0,
-                         uint32_t pairs)
+                         uint32_t n1, uint32_t quads)
 {
+    __shared__ uint2 s_w[kQuadStage / 8];
     const uint8_t* s = src + offs[2 * blockIdx.x];
     uint8_t* d = arena + offs[2 * blockIdx.x + 1];
     const uint32_t words = bytes / 8;
     const uint32_t per = (words + gridDim.y - 1) / gridDim.y;
     const uint32_t w0 = min(words, blockIdx.y * per), w1 = min(words, w0 + per);
-    const uint32_t lane = threadIdx.x & 31u;
-    /* every lane runs every pass (the shuffle below needs the whole warp) */
-    for (uint32_t base = w0; base < w1; base += kGatherThreads)
+    if (!quads)
     {
-        const uint32_t w = base + threadIdx.x;
-        const bool in = w < w1;
-        const uint2 v = in ? *reinterpret_cast<const uint2*>(s + 8ull * w) : make_uint2(0u, 0u);
-        if (!pairs)
-        {
-            if (in)
-                *reinterpret_cast<uint2*>(d + 8ull * w) = v;
-            continue;
-        }
-        /* the byte after this word: the next lane's first byte while that
-         * lane's word is in this block's run, else read here */
-        uint32_t next = __shfl_down_sync(0xFFFFFFFFu, v.x & 0xFFu, 1);
-        if (in && (lane == 31u || w + 1 >= w1))
-            next = w + 1 < words ? uint32_t(s[8ull * w + 8]) : 0u;
-        if (!in)
-            continue;
-        const uint32_t b[9] = {v.x & 0xFFu,         (v.x >> 8) & 0xFFu, (v.x >> 16) & 0xFFu,
-                               v.x >> 24,           v.y & 0xFFu,        (v.y >> 8) & 0xFFu,
-                               (v.y >> 16) & 0xFFu, v.y >> 24,          next};
-        uint32_t x = (8u * w) % n0; /* column of the word's first voxel */
-        uint32_t e[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k)
-        {
-            e[k] = b[k] | ((x == n0 - 1u ? b[k] : b[k + 1]) << 8);
-            x = x + 1u == n0 ? 0u : x + 1u;
-        }
-        /* 16 bytes at slot + 16 w: 16-byte aligned */
-        *reinterpret_cast<uint4*>(d + 16ull * w) =
-            make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16),
-                       e[6] | (e[7] << 16));
+        for (uint32_t w = w0 + threadIdx.x; w < w1; w += kGatherThreads)
+            *reinterpret_cast<uint2*>(d + 8ull * w) = *reinterpret_cast<const uint2*>(s + 8ull * w);
+        return;
+    }
+    const uint32_t j1 = 8u * w1;
+    for (uint32_t j0 = 8u * w0; j0 < j1; j0 += kQuadRun)
+    {
+        const uint32_t m = min(kQuadRun, j1 - j0);
+        /* bytes - j0 is a multiple of 8, so whole words stay in the brick */
+        const uint32_t nw = (min(bytes - j0, m + n0 + 1u) + 7u) / 8u;
+        for (uint32_t i = threadIdx.x; i < nw; i += kGatherThreads)
+            s_w[i] = *reinterpret_cast<const uint2*>(s + j0 + 8ull * i);
+        __syncthreads();
+        quads_from_bytes(reinterpret_cast<const uint8_t*>(s_w), reinterpret_cast<uint32_t*>(d), j0,
+                         m, n0, n1);
+        __syncthreads();
     }
 }
 
@@ -678,7 +681,8 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
                          (words + kGatherThreads - 1) / kGatherThreads));
         gather_bricks_kernel<<<dim3(nb, split), kGatherThreads, 0, up>>>(
             arena, vol->host_store.as_dev<uint8_t>(), static_cast<const uint64_t*>(R.h_gather.dev),
-            uint32_t(vol->brick_bytes), vol->info.max_block[0], vol->stage_off != 0);
+            uint32_t(vol->brick_bytes), vol->info.max_block[0], vol->info.max_block[1],
+            vol->stage_off != 0);
         LV_CUDA(ctx, cudaGetLastError());
         LV_CUDA(ctx, cudaEventRecord(R.gather_done, up));
         R.gather_recorded = true;
@@ -691,9 +695,9 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
         LV_CUDA(ctx, R.h_expand.reserve(sizeof(uint64_t) * expand.size()));
         std::memcpy(R.h_expand.ptr, expand.data(), sizeof(uint64_t) * expand.size());
         const uint32_t voxels = uint32_t(vol->brick_bytes); /* uint8: one byte per voxel */
-        expand_pairs_kernel<<<uint32_t(expand.size()), kExpandThreads, 0, up>>>(
-            arena, static_cast<const uint64_t*>(R.h_expand.dev), vol->info.max_block[0], voxels,
-            uint32_t(vol->stage_off));
+        expand_quads_kernel<<<uint32_t(expand.size()), kExpandThreads, 0, up>>>(
+            arena, static_cast<const uint64_t*>(R.h_expand.dev), vol->info.max_block[0],
+            vol->info.max_block[1], voxels, uint32_t(vol->stage_off));
         LV_CUDA(ctx, cudaGetLastError());
         LV_CUDA(ctx, cudaEventRecord(R.expand_done, up));
         R.expand_recorded = true;
@@ -721,13 +725,13 @@ void volume_layout(lv_volume* v, uint32_t brick_layout)
     v->brick_bytes = uint64_t(v->info.max_block[0]) * v->info.max_block[1] *
                      v->info.max_block[2] * bytes_per_voxel(v->info.dtype) *
                      v->info.comp_count;
-    /* voxel pairs: 2 bytes per voxel, the canonical bytes staged in the
-     * slot's upper part (256-byte aligned, at or past the brick's voxel
-     * count so that the in-place expansion never overwrites bytes it has
-     * still to read) */
-    v->stage_off = brick_layout == LV_BRICKS_PAIRS &&
-                           pair_layout(v->info.dtype, v->info.max_block[0])
-                       ? (v->brick_bytes + 255) & ~uint64_t(255)
+    /* voxel quads: 4 bytes per voxel, the canonical bytes staged in the
+     * slot's upper part (256-byte aligned, at or past three times the
+     * brick's voxel count so that the in-place expansion never overwrites
+     * bytes it has still to read): a slot of about 4 bytes per voxel */
+    v->stage_off = brick_layout == LV_BRICKS_QUADS &&
+                           quad_layout(v->info.dtype, v->info.max_block[0])
+                       ? (3 * v->brick_bytes + 255) & ~uint64_t(255)
                        : 0;
     v->slot_units = uint32_t(round_units(v->stage_off + v->brick_bytes));
 }
@@ -869,7 +873,7 @@ lv_status make_ray_view(lv_ctx* ctx, const lv_volume* vol, const lv_tf* tf,
     V.Lf = Lf;
     V.dtype = info.dtype;
     V.bpv = bytes_per_voxel(info.dtype);
-    V.pairs = vol->stage_off != 0;
+    V.quads = vol->stage_off != 0;
     V.filter = desc.filter == LV_FILTER_TRILINEAR ? LV_FILTER_TRILINEAR : LV_FILTER_NEAREST;
     /* the transfer function's range when valid, else the type's
      * (RayCastRenderer.cpp:279-284) */
@@ -933,7 +937,7 @@ extern "C" lv_status lv_brick_slot_bytes(const lv_ctx* ctx, const lv_volume_info
     lv_volume v;
     v.info = *info;
     v.info.depth = 0; /* the layout of a brick only */
-    volume_layout(&v, ctx ? ctx->brick_layout : uint32_t(LV_BRICKS_PAIRS));
+    volume_layout(&v, ctx ? ctx->brick_layout : uint32_t(LV_BRICKS_QUADS));
     *bytes = uint64_t(v.slot_units) * kSlotUnit;
     return LV_OK;
 }
@@ -1045,7 +1049,7 @@ extern "C" lv_status lv_pool_set_brick_layout(lv_ctx* ctx, uint32_t layout)
 {
     if (!ctx)
         return LV_EINVAL;
-    if (layout != LV_BRICKS_PAIRS && layout != LV_BRICKS_COMPACT)
+    if (layout != LV_BRICKS_QUADS && layout != LV_BRICKS_COMPACT)
         return fail(ctx, LV_EINVAL, "unknown brick layout");
     if (ctx->pool)
         return fail(ctx, LV_EINVAL, "pool already allocated");

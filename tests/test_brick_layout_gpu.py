@@ -1,6 +1,7 @@
 """Brick layouts of the pool (lv_pool_set_brick_layout): uint8 bricks of 64
-or more voxels per row are stored as voxel pairs by default (each voxel with
-its +x neighbour, written canonical and expanded in place on the device),
+to 1024 voxels per row are stored as voxel quads by default (each voxel with
+its +x, +y and +x+y neighbours; written canonical and expanded in place on
+the device, or gathered from a page-locked host store straight into quads),
 one voxel per byte with LV_BRICKS_COMPACT. The layout is internal: every
 frame and histogram must be bit for bit the same in both, for every way a
 brick reaches the pool (device generator, host store, a data-source
@@ -15,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 
 def make(ctx, lv, source, block=64):
-    vi = lv.VolumeInformation(256, block, 1)  # (block + 2)^3 slots: pairs by default
+    vi = lv.VolumeInformation(256, block, 1)  # (block + 2)^3 slots: quads by default
     if source == "device":
         return vi, ctx.blob_volume(vi, 24, 11, 4)
     if source == "host":
@@ -29,16 +30,16 @@ def make(ctx, lv, source, block=64):
 
 
 @pytest.mark.parametrize("source,block", [("device", 64), ("host", 64), ("callback", 64),
-                                          ("device", 128)])
-def test_pairs_equal_compact(source, block):
+                                          ("device", 128), ("host", 128)])
+def test_quads_equal_compact(source, block):
     import livre_gb300 as lv
     frames = {}
     n = (block + 2) ** 3
-    for layout in (lv.BRICKS_PAIRS, lv.BRICKS_COMPACT):
+    for layout in (lv.BRICKS_QUADS, lv.BRICKS_COMPACT):
         ctx = lv.Context(0, pool_bytes=512 << 20, brick_layout=layout)
         vi, vol = make(ctx, lv, source, block)
-        assert ctx.slot_bytes(vi) == (((n + 255) // 256 * 256 + n + 1023) // 1024 * 1024
-                                      if layout == lv.BRICKS_PAIRS else (n + 1023) // 1024 * 1024)
+        assert ctx.slot_bytes(vi) == (((3 * n + 255) // 256 * 256 + n + 1023) // 1024 * 1024
+                                      if layout == lv.BRICKS_QUADS else (n + 1023) // 1024 * 1024)
         tf = ctx.transfer_function(lv.gaussian_peaks_tf(256, seed=9))
         out = []
         for k, (kind, filt, lookahead) in enumerate([
@@ -59,11 +60,11 @@ def test_pairs_equal_compact(source, block):
         vol.close()
         tf.close()
         ctx.close()
-    pairs, compact = frames[lv.BRICKS_PAIRS], frames[lv.BRICKS_COMPACT]
-    for (a, na), (b, nb) in zip(pairs[:-1], compact[:-1]):
+    quads, compact = frames[lv.BRICKS_QUADS], frames[lv.BRICKS_COMPACT]
+    for (a, na), (b, nb) in zip(quads[:-1], compact[:-1]):
         assert na == nb and na > 0
         assert np.array_equal(a, b)
-    assert np.array_equal(pairs[-1][0], compact[-1][0]) and pairs[-1][0].sum() > 0
+    assert np.array_equal(quads[-1][0], compact[-1][0]) and quads[-1][0].sum() > 0
 
 
 def test_layout_fixed_once_the_pool_exists():
