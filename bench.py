@@ -99,11 +99,6 @@ def parse():
     return p.parse_args()
 
 
-# DRAM bytes (read + write) of one ray-cast launch of the 2048^3 / 1080p
-# orbit, measured by ncu on a GB300 (37.11 MB read, 2.29 MB written: the
-# visible bricks once, stored as voxel pairs; the 8-byte-per-sample gather is
-# served by L1/L2).
-RAYCAST_DRAM_BYTES_PER_LAUNCH = 39.46e6
 
 
 def transfer_function(cfg):
@@ -1084,10 +1079,12 @@ def gb300_arm(args, cfg):
         "gpu_launches": int(sum(s["n_launches"] for s in stats)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "traffic": RAYCAST_DRAM_BYTES_PER_LAUNCH if args.config == "plain2048"
-                     else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
-                                       "one raycast_tiles_kernel launch of this workload",
+                     "traffic": None,
+                     "traffic_note": "not yet captured with the voxel-quad brick layout; the "
+                                     "last ncu capture of this launch (voxel pairs, 2 bytes "
+                                     "per voxel) read 37.11 MB and wrote 2.35 MB: the visible "
+                                     "bricks once, the 8-byte-per-sample gather served by "
+                                     "L1/L2",
                      "algorithmic_bytes_per_launch": float(alg_bytes.mean()),
                      "kernel": "raycast_tiles_kernel<u8,trilinear>",
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800"},
