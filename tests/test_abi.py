@@ -49,3 +49,27 @@ def test_product_never_imports_oracle():
         if os.path.isfile(path) and path.endswith((".py", ".cu", ".h", ".cpp")):
             text = open(path).read()
             assert "pyoracle" not in text and "oracle/" not in text and "or_" + "raycast" not in text, path
+
+
+def test_brick_slot_bytes_by_layout(native):
+    """Pool bytes per brick (lv_brick_slot_bytes with no context: the default
+    layout). uint8 bricks of 64 to 1024 voxels per row are voxel quads: the
+    canonical bytes staged at three times the voxel count (256-byte
+    aligned), the slot rounded to whole 1 KiB units; every other brick keeps
+    one element per voxel. Host arithmetic only, no device call."""
+    import livre_gb300 as lv
+
+    def kib(b):
+        return (b + 1023) // 1024 * 1024
+
+    for voxels, block, overlap, dtype, quads in [
+            (2048, 64, 1, lv.DT_UINT8, True),     # 66^3: the 2048^3 headline bricks
+            (256, 128, 1, lv.DT_UINT8, True),     # 130^3
+            (256, 62, 1, lv.DT_UINT8, True),      # 64^3: the smallest quad row
+            (256, 32, 1, lv.DT_UINT8, False),     # 34^3: compact (rows under 64)
+            (1024, 128, 1, lv.DT_UINT16, False),  # uint16 stays compact
+    ]:
+        vi = lv.VolumeInformation(voxels, block, overlap, dtype=dtype)
+        n = (block + 2 * overlap) ** 3 * (2 if dtype == lv.DT_UINT16 else 1)
+        want = kib((3 * n + 255) // 256 * 256 + n) if quads else kib(n)
+        assert vi.slot_bytes == want, (voxels, block, dtype, vi.slot_bytes, want)
