@@ -479,10 +479,10 @@ lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
  * sample before compositing the current one (shorter latency per ray, more
  * registers per thread); 0 does not.
  * Default: {LV_LAUNCH_TILE_GRID, 8, 8, 0, LV_ORDER_LONGEST_FIRST, 1}, the
- * fastest on a 2048^3 volume at 1920x1080: 0.286 ms of ray cast per frame
- * (every brick resident, no L2 flush), against 0.295 ms for 8 x 16 tiles,
- * 0.333 ms without look-ahead, 0.35 ms in raster order, 0.37 ms for warp
- * tiles and 0.39 ms for the persistent tile queue; and the friendliest to
+ * fastest on a 2048^3 volume at 1920x1080: 0.234 ms of ray cast per frame
+ * (every brick resident, no L2 flush), against 0.239 ms for 8 x 16 tiles,
+ * 0.31 ms without look-ahead, 0.28 ms in raster order, 0.35 ms for warp
+ * tiles and 0.37 ms for the persistent tile queue; and the friendliest to
  * other work on the device (no resident grid).
  * No reference counterpart (the reference rasterises one brick at a time,
  * RayCastRenderer.cpp:503-571). */
