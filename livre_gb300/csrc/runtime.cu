@@ -1708,7 +1708,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
      * previous ones. The samples per ray come from the first pass's bricks,
      * as onFrameStart runs for the first pass only (Renderer.cpp,
      * RayCastRenderer.cpp:213-233). */
-    auto multipass = [&](uint32_t n_vis, uint64_t per_pass) -> lv_status {
+    auto multipass = [&](uint32_t n_vis, uint64_t per_pass, uint32_t first_frame) -> lv_status {
         const uint32_t m = uint32_t(std::min<uint64_t>(per_pass, 0xFFFFFFFFu));
         LV_CUDA(ctx, R.h_pass.reserve(sizeof(uint64_t) * n_vis));
         LV_CUDA(ctx, R.pass_count.reserve(sizeof(uint32_t)));
@@ -1745,7 +1745,7 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
         RV.synchronous = 1;
         for (uint32_t p = 0; p < passes; ++p)
         {
-            const uint32_t fp = p == 0 ? frame : ++R.frame;
+            const uint32_t fp = p == 0 ? first_frame : ++R.frame;
             const uint32_t first = p * m, cnt = std::min(m, n_vis - first);
             RV.frame = RV.view_frame = fp;
             LV_CUDA(ctx, cudaMemcpyAsync(R.visible.ptr, hp + first, sizeof(uint64_t) * cnt,
@@ -1854,32 +1854,22 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
     }
     R.passes = 0;
     bool multi = false;
+    /* bricks of this volume the pool holds at once: a visible set larger
+     * than that renders in passes (renderSync) */
     const uint64_t per_pass = ctx->pool->capacity_units / vol->slot_units;
-    if (desc->synchronous && per_pass > 0 && vol->n_nodes > per_pass)
+    if (desc->synchronous)
     {
-        /* the volume may not fit: look at the visible-set size first */
-        uint32_t* hs = R.h_counters.as<uint32_t>() + FC_WORDS;
-        LV_CUDA(ctx, cudaMemcpyAsync(hs, R.sel_result.ptr,
-                                     sizeof(uint32_t) * LV_SELECT_RESULT_WORDS,
-                                     cudaMemcpyDeviceToHost, s));
-        LV_CUDA(ctx, cudaStreamSynchronize(s));
-        const uint32_t n_vis = hs[LV_SEL_WRITTEN];
-        if (n_vis > per_pass)
-        {
-            multi = true;
-            st = multipass(n_vis, per_pass);
-            if (st != LV_OK)
-                return st;
-        }
-    }
-    if (!multi && desc->synchronous)
-    {
-        /* The residency pass's miss count goes to the host while the rest of
-         * the frame is already queued behind it; the host waits for the
-         * count only. A frame that missed bricks streams them and renders
-         * again (the first ray cast lacked them), unless its volume streamed
-         * in the previous frame too: then the ray cast is queued only after
-         * the count is known. */
+        /* The residency pass's miss count (and the selection's visible
+         * count, which reached the host before it) goes to the host while
+         * the rest of the frame is already queued behind it; the host waits
+         * for the counts only. A frame that missed bricks streams them and
+         * renders again (the first ray cast lacked them), unless its volume
+         * streamed in the previous frame too: then the ray cast is queued
+         * only after the count is known. A visible set larger than the pool
+         * cannot be resident at once, so it always misses: its queued ray
+         * cast returns at once, and the frame renders in passes instead,
+         * numbered after this residency pass so that the bricks it stamped
+         * are not held in the pool. */
         uint32_t* hc = R.h_counters.as<uint32_t>();
         st = resolve();
         if (st != LV_OK)
@@ -1905,29 +1895,43 @@ extern "C" lv_status lv_render(lv_ctx* ctx, lv_volume* vol, lv_tf* tf,
                 return st;
         }
         LV_CUDA(ctx, cudaEventSynchronize(R.resolve_done));
-        const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
-        if (!missing && !queued)
-            st = after_resolve();
-        else if (missing)
+        const uint32_t n_vis = hc[FC_WORDS + LV_SEL_WRITTEN];
+        if (per_pass > 0 && n_vis > per_pass)
         {
-            uint32_t loaded = 0;
-            uint64_t bytes = 0;
-            st = timed_stream(R.h_missing.as<uint64_t>(), missing, frame, loaded, bytes);
-            R.stats.n_uploaded += loaded;
-            R.stats.bytes_uploaded += bytes;
-            if (st != LV_OK && st != LV_EAGAIN)
+            multi = true;
+            st = multipass(n_vis, per_pass, ++R.frame);
+            if (st != LV_OK)
                 return st;
-            /* resolve again with the streamed bricks; what still misses
-             * (pool too small) is not rendered */
-            st = frame_tail();
-            if (queued)
-                R.launches += 3u;
-            else
-                R.launches += 1; /* one more residency pass */
+            /* this residency pass and its counters' copy, and the leaf fill
+             * and ray cast queued behind them */
+            R.launches += queued ? 4u : 2u;
         }
-        vol->streamed_last = R.stats.n_uploaded > 0;
+        else
+        {
+            const uint32_t missing = std::min<uint32_t>(hc[FC_MISSING], RV.missing_capacity);
+            if (!missing && !queued)
+                st = after_resolve();
+            else if (missing)
+            {
+                uint32_t loaded = 0;
+                uint64_t bytes = 0;
+                st = timed_stream(R.h_missing.as<uint64_t>(), missing, frame, loaded, bytes);
+                R.stats.n_uploaded += loaded;
+                R.stats.bytes_uploaded += bytes;
+                if (st != LV_OK && st != LV_EAGAIN)
+                    return st;
+                /* resolve again with the streamed bricks; what still misses
+                 * (pool too small) is not rendered */
+                st = frame_tail();
+                if (queued)
+                    R.launches += 3u;
+                else
+                    R.launches += 1; /* one more residency pass */
+            }
+            vol->streamed_last = R.stats.n_uploaded > 0;
+        }
     }
-    else if (!multi)
+    else
         st = frame_tail();
     if (st != LV_OK)
         return st;
