@@ -387,7 +387,8 @@ struct Taps
 template <int DT, int FILTER, int EDGE>
 __host__ __device__ constexpr bool raw_taps()
 {
-    return DT == LV_DT_UINT8 && FILTER == LV_FILTER_TRILINEAR && quad_layout(DT, EDGE > 1 ? EDGE : 0);
+    return DT == LV_DT_UINT8 && FILTER == LV_FILTER_TRILINEAR &&
+           quad_layout(DT, EDGE > 1 ? EDGE : 0);
 }
 
 /* The view constants the per-sample steps read (the transfer function and
