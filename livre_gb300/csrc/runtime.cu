@@ -526,7 +526,7 @@ lv_status stream_bricks(lv_ctx* ctx, lv_volume* vol, const uint64_t* ids,
     std::unordered_map<lv_volume*, std::vector<uint32_t>> stamps;
     std::vector<std::pair<lv_volume*, std::pair<uint64_t, int32_t>>> updates;
     std::vector<uint64_t> gen_ids, gen_offsets;
-    std::vector<uint64_t> expand; /* slots to expand into voxel pairs */
+    std::vector<uint64_t> expand; /* slots to expand into voxel quads */
     /* host-store bricks read by gather_bricks_kernel: (source, slot) offsets */
     std::vector<uint64_t> gather;
     const bool gathered = vol->kind == SRC_BLOB_HOST && vol->brick_bytes % 8 == 0;
